@@ -1,0 +1,396 @@
+#!/usr/bin/env python
+"""Benchmark of the Lennard-Jones neighbour-list force path on GB300.
+
+Workload (the reference's rho = 0.5 comparison case at 108,000 particles):
+FCC 30^3 cells x 4 = 108,000 particles, rho = 0.5, periodic cubic box
+L = (N / rho)^(1/3) = 60, jitter U[-0.05, 0.05) per coordinate from
+mt19937_64(20240601), cutoff 3.0 (CL2 = 9), search radius 3.3, i-sorted int32
+CSR half list (~37.6 partners per particle) built on the device, AoS double4
+and SoA positions, dt = 0.005.
+
+A step is one force call (p += F dt over the whole system).  L2 is flushed
+(512 MiB write) before every timed step; each step is timed with CUDA events
+on the engine's stream.  `value` is the best mixed-precision variant in
+G pair-interactions/s = P_half / t_call / 1e9 (P_half = i<j list pairs, the
+same count for gather and scatter); the FP64 path is reported beside it.
+
+e2e runs the reference's measure() through the C ABI (lj_measure_aos): host
+q, p and the CSR list uploaded from pinned memory, 100 force calls, p
+downloaded, every step.
+
+--impl reference times the reference's CPU force routine restated in C (the
+oracle; gather over the full list on every host core, project-written
+OpenMP -- the reference itself is single-threaded) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NCELL, DENSITY, JITTER, SEED = 30, 0.5, 0.05, 20240601
+RC, RS, DT = 3.0, 3.3, 0.005
+METRIC = "G pair-interactions/s, mixed vs plain FP64, same GB300, force rel err <=1e-5"
+UNIT = "G pair-interactions/s"
+WORKLOAD = ("LJ force call, FCC 108,000 particles, rho=0.5, periodic L=60, rc=3.0, "
+            "search 3.3, i-sorted int32 CSR, dt=0.005")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas only: every rank runs its own system)
+# ---------------------------------------------------------------------------
+class Dist:
+    def __init__(self, backend):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v, device=None):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64, device=device)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v, device=None):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64, device=device)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# roofline constants
+# ---------------------------------------------------------------------------
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(name):
+    """dram bytes per launch recorded from an ncu capture under profiles/."""
+    f = ROOT / "profiles" / name
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_call:"):
+            return float(line.split(":")[1].split()[0])
+    return None
+
+
+def algorithmic_bytes(method, layout, P, N):
+    # compulsory traffic per force call (each datum once): list indices, q, p
+    # read + write, number_of_partners + pointer
+    per_n = 104 if layout == "aos" else 80
+    return (8 if method == "gather" else 4) * P + per_n * N
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, dist):
+    import torch
+    import lj_gpu_gb300 as lj
+    from lj_gpu_gb300 import _build
+
+    _build.build()
+    dev = torch.device("cuda", dist.local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    q, L = lj.init_fcc(NCELL, DENSITY, JITTER, SEED)
+    N = q.shape[0]
+    qd = torch.from_numpy(q).to(dev)
+    qs = [torch.from_numpy(np.ascontiguousarray(q[:, d])).to(dev) for d in range(3)]
+    ctx = lj.Context(dist.local, stream=stream)
+    t0 = time.perf_counter()
+    ctx.build_list(qd, RS, box=L)
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    _, P, max_half = ctx.list_info("half")
+    _, P_full, max_full = ctx.list_info("full")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def time_variant(prec, method, layout, steps, warmup):
+        opts = lj.make_opts(dt=DT, cl2=RC * RC, box=L, precision=prec, method=method)
+        pd = torch.zeros_like(qd)
+        ps = [torch.zeros(N, dtype=torch.float64, device=dev) for _ in range(3)]
+
+        def call():
+            if layout == "aos":
+                ctx.force_aos(qd, pd, opts)
+            else:
+                ctx.force_soa(*qs, *ps, opts)
+
+        for _ in range(warmup):
+            flush.add_(1.0)
+            call()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        torch.cuda.synchronize()
+        dist.barrier()
+        for a, b in ev:
+            flush.add_(1.0)  # > L2: every timed call starts cold
+            a.record(stream)
+            call()
+            b.record(stream)
+        torch.cuda.synchronize()
+        dist.barrier()
+        ms = [a.elapsed_time(b) for a, b in ev]
+        return sum(ms)
+
+    variants = [(p, m, l) for p in ("mixed", "fp64") for m in ("gather", "scatter")
+                for l in ("aos", "soa")]
+    results = {}
+    clocks = None
+    for v in variants:
+        steps = args.steps if v[0] == "mixed" else max(3, min(args.steps, 20))
+        if v == ("mixed", "gather", "aos"):
+            with ClockSampler(dist.local) as cs:
+                ms = time_variant(*v, steps, args.warmup)
+            clocks = cs.summary()
+        else:
+            ms = time_variant(*v, steps, max(3, min(args.warmup, 5)))
+        t_max = dist.max(ms / steps / 1e3, dev)  # seconds per call, slowest rank
+        results["/".join(v)] = {"s_per_call": t_max, "steps": steps,
+                                "gpairs": dist.world * P / t_max / 1e9}
+
+    best_mixed = max((k for k in results if k.startswith("mixed")),
+                     key=lambda k: results[k]["gpairs"])
+    best_fp64 = max((k for k in results if k.startswith("fp64")),
+                    key=lambda k: results[k]["gpairs"])
+    head = results[best_mixed]
+    prec, method, layout = best_mixed.split("/")
+
+    # e2e: the reference's measure() through the C ABI with pinned host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        kind = "full" if method == "gather" else "half"
+        np_, ptr_, lst_ = ctx.get_list_csr(kind)
+        pin = lambda a: torch.from_numpy(a).pin_memory()
+        h_np, h_ptr, h_lst = pin(np_), pin(ptr_), pin(lst_)
+        ctx.set_list_csr(h_np, h_ptr, h_lst, kind=kind)
+        hq = pin(q)
+        hp = torch.zeros_like(hq).pin_memory()
+        opts = lj.make_opts(dt=DT, cl2=RC * RC, box=L, precision=prec, method=method)
+        ctx.measure_aos(hq, hp, opts, calls=100)  # warm-up
+        dist.barrier()
+        tot = 0.0
+        for _ in range(args.e2e_steps):
+            ms_total, _ = ctx.measure_aos(hq, hp, opts, calls=100)
+            tot += ms_total
+        dist.barrier()
+        t_step = dist.max(tot / args.e2e_steps / 1e3, dev)
+        h2d = hq.numel() * 8 * 2 + (h_np.numel() + h_ptr.numel() + h_lst.numel()) * 4
+        e2e = {"value": dist.world * P * 100 / t_step / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(hp.numel() * 8),
+               "step": "lj_measure_aos: H2D q,p,CSR + 100 force calls + D2H p",
+               "ms_per_step": t_step * 1e3}
+
+    hbm, peak_kind = peaks()
+    alg = algorithmic_bytes(method, layout, P, N)
+    achieved = alg / head["s_per_call"] / 1e9
+    traffic = profiled_traffic("force_mixed_gather_aos_108k_rho0.5.txt")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_call": alg,
+                "kernel": f"force call {best_mixed} (fixed-image pass + pair kernel)"}
+    fp = results[best_fp64]
+    fp_alg = algorithmic_bytes(best_fp64.split("/")[1], best_fp64.split("/")[2], P, N)
+    fp64 = {"value": fp["gpairs"], "variant": best_fp64, "ms_per_call": fp["s_per_call"] * 1e3,
+            "hbm_frac": fp_alg / fp["s_per_call"] / 1e9 / hbm,
+            "mixed_over_fp64": head["gpairs"] / fp["gpairs"]}
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(q, L, P, sample_calls=5)
+
+    line = {
+        "metric": METRIC, "value": dist.world * P / head["s_per_call"] / 1e9, "unit": UNIT,
+        "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": head["s_per_call"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math, f64 q/p",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "N": N, "pairs_half": P, "pairs_full": P_full,
+                   "max_row_half": max_half, "max_row_full": max_full, "box": L,
+                   "variant": best_mixed, "step": "one force call",
+                   "l2": "flushed before every timed call (512 MiB write)",
+                   "list_build_s": t_build, "parallelism": f"replicas x{dist.world}"},
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64": fp64,
+        "variants": {k: round(v["gpairs"], 3) for k, v in results.items()},
+        "clocks": clocks, "gpu_launches": 2 * args.steps,
+    }
+    ctx.close()
+    return line
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (oracle: the reference's algorithm restated in C)
+# ---------------------------------------------------------------------------
+def cpu_baseline(q, L, P, sample_calls=5):
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib as ol
+    full = ol.build_list(q, RS, box=L, full=True)
+    threads = ol.oracle().lj_or_max_threads()
+    p = np.zeros_like(q)
+    ol.force_gather_aos(q, p, *full, cl2=RC * RC, dt=DT, box=L, threads=threads)  # warm
+    t0 = time.perf_counter()
+    ol.force_gather_aos(q, p, *full, cl2=RC * RC, dt=DT, box=L, calls=sample_calls,
+                        threads=threads)
+    t = time.perf_counter() - t0
+    half = ol.build_list(q, RS, box=L)
+    t1 = time.perf_counter()
+    ol.force_sorted_aos(q, p, *half, cl2=RC * RC, dt=DT, box=L, calls=1)
+    t_single = time.perf_counter() - t1
+    return {"value": P * sample_calls / t / 1e9, "unit": UNIT, "cores": threads,
+            "kind": "port",
+            "sample": f"{sample_calls} full force calls of the 108,000-particle system, "
+                      "OpenMP gather over the full list (project-written parallelisation)",
+            "single_thread_force_sorted": P / t_single / 1e9}
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return None
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib as ol
+    q, L = ol.init_fcc_periodic(NCELL, DENSITY, JITTER, SEED)
+    full = ol.build_list(q, RS, box=L, full=True)
+    half = ol.build_list(q, RS, box=L)
+    P = len(half[2])
+    threads = ol.oracle().lj_or_max_threads()
+    p = np.zeros_like(q)
+    for _ in range(args.warmup):
+        ol.force_gather_aos(q, p, *full, cl2=RC * RC, dt=DT, box=L, threads=threads)
+    t0 = time.perf_counter()
+    ol.force_gather_aos(q, p, *full, cl2=RC * RC, dt=DT, box=L, calls=args.steps,
+                        threads=threads)
+    t = time.perf_counter() - t0
+    v = P * args.steps / t / 1e9
+    return {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "N": q.shape[0], "pairs_half": P,
+                   "step": "one force call", "parallelism": "host cores"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "every step is one full force call of the workload "
+                                   "(C restatement of the reference routine, OpenMP gather)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        dist = Dist("gloo")
+        line = run_reference(args, dist)
+    else:
+        dist = Dist("nccl")
+        line = run_ours(args, dist)
+    if dist.rank == 0 and line is not None:
+        print(json.dumps(line))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

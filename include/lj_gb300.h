@@ -1,0 +1,191 @@
+/*
+ * lj_gb300.h -- C ABI of the GB300 Lennard-Jones neighbour-list force engine.
+ *
+ * The engine keeps the force-routine contract of the reference
+ * (kohnakagawa/lj_gpu): positions q and momenta p, an i-sorted CSR neighbour
+ * list given as number_of_partners / pointer / sorted_list, a cutoff CL2, and
+ * the in-place kick
+ *
+ *     p_i += sum_j df(r_ij) * (q_j - q_i),   df = ((24 r^6 - 48) / r^14) * dt,
+ *     pairs with r2 > CL2 skipped,
+ *
+ * applied symmetrically (p_j -= ...) for a half list, as cpu_ref
+ * force_sorted does (cpu_ref/force_aos.cpp:192-224) and as the CUDA kernels do
+ * (cuda/kernel.cuh:5-34 gather over the full list, :238-469 scatter over the
+ * half list).
+ *
+ * Every entry point returns an int status (LJ_OK == 0) and never exits the
+ * process.  Device-pointer entry points are stream ordered and asynchronous;
+ * the stream argument is a cudaStream_t passed as void* (NULL = legacy default
+ * stream).  Memory passed in is owned by the caller.  A context is not thread
+ * safe: use one per host thread.
+ *
+ * Layouts: AoS q/p are double[n][4] (x, y, z, w; w unused and untouched,
+ * 32-byte aligned: the reference's double4 / cpu_ref q[N][4]).  SoA passes
+ * the three coordinate arrays separately (cpu_ref/force_soa.cpp q[X], q[Y],
+ * q[Z] rows).  Indices are int32, offsets in pointer[] are int32 (as in the
+ * reference), list lengths are int64.
+ */
+#ifndef LJ_GB300_H
+#define LJ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LJ_GB300_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------- */
+enum {
+  LJ_OK = 0,
+  LJ_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size or enum value        */
+  LJ_ERR_BAD_LIST = 2,         /* list failed validation (check_loadedpair)   */
+  LJ_ERR_CUDA = 3,             /* a CUDA runtime call failed                   */
+  LJ_ERR_OUT_OF_MEMORY = 4,    /* device or pinned allocation failed           */
+  LJ_ERR_LIST_OVERFLOW = 5,    /* a neighbour build exceeded its capacity      */
+  LJ_ERR_TIMEOUT = 6,          /* a bounded device-side wait gave up           */
+  LJ_ERR_NO_LIST = 7,          /* force called before a list was installed     */
+  LJ_ERR_UNSUPPORTED = 8       /* combination not provided                     */
+};
+
+/* ---- enumerations ------------------------------------------------------- */
+enum { LJ_PREC_FP64 = 0, LJ_PREC_MIXED = 1 };
+enum { LJ_LIST_HALF = 0, LJ_LIST_FULL = 1 };
+enum { LJ_WHERE_HOST = 0, LJ_WHERE_DEVICE = 1 };
+enum {
+  LJ_METHOD_AUTO = 0,         /* engine choice (tuned per precision)          */
+  LJ_METHOD_GATHER_FULL = 1,  /* full list, each row writes only its own p_i  */
+  LJ_METHOD_SCATTER_HALF = 2  /* half list, p_j updated with atomics          */
+};
+
+/* ---- options of one force call ------------------------------------------ */
+typedef struct lj_force_opts {
+  double dt;          /* kick length: p += F dt (reference dt)                 */
+  double cl2;         /* squared cutoff (reference CL2); r2 > cl2 is skipped  */
+  double box[3];      /* periodic box lengths, used when periodic != 0        */
+  int32_t periodic;   /* 0: open boundaries (the reference), 1: minimum image */
+  int32_t precision;  /* LJ_PREC_FP64 or LJ_PREC_MIXED                        */
+  int32_t method;     /* LJ_METHOD_*                                          */
+  int32_t lanes;      /* lanes per i-particle, 0 = default, else 1,2,4,..,32  */
+  int32_t block;      /* threads per block, 0 = default, else 64..1024        */
+  int32_t reserved[3];
+} lj_force_opts;
+
+/* dt = 0.001, cl2 = 9.0 (cpu_ref/force_aos.cpp:14,31-33), open box, FP64, auto */
+void lj_force_opts_default(lj_force_opts* opts);
+
+typedef struct lj_ctx lj_ctx;
+
+int lj_abi_version(void);
+const char* lj_status_string(int status);
+
+/* ---- context ------------------------------------------------------------ */
+int lj_ctx_create(lj_ctx** out, int device);
+void lj_ctx_destroy(lj_ctx* ctx);
+/* message of the last failing call on this context ("" if none) */
+const char* lj_ctx_last_error(const lj_ctx* ctx);
+/* stream used by every later call on ctx (cudaStream_t as void*) */
+int lj_ctx_set_stream(lj_ctx* ctx, void* stream);
+
+/* ---- neighbour lists ---------------------------------------------------- */
+/* Installs an i-sorted CSR list for n particles (replaces the reference's
+ * copy_to_gpu of sorted_list / number_of_partners / pointer,
+ * cuda/force_cuda.cu:302-312).  The arrays are copied into the context, so
+ * the caller may free them afterwards.  Validation follows check_loadedpair
+ * (cuda/force_cuda.cu:183-201) plus row bounds:
+ *   0 <= number_of_partners[i] < n, 0 <= pointer[i] <= n_entries,
+ *   pointer[i] + number_of_partners[i] <= n_entries, 0 <= sorted_list[k] < n.
+ * kind: LJ_LIST_HALF (each unordered pair once, as makepair with
+ * EN_ACTION_REACTION builds it) or LJ_LIST_FULL (each pair in both rows).
+ * A half list is expanded on the device into the full list the gather
+ * kernels use; both are kept. */
+int lj_list_set_csr(lj_ctx* ctx, int32_t n, const int32_t* number_of_partners,
+                    const int32_t* pointer, const int32_t* sorted_list, int64_t n_entries,
+                    int32_t kind, int32_t where);
+/* Installs the reference's unsorted (i, j) pair arrays (register_pair,
+ * cpu_ref/force_aos.cpp:60-74) and sorts them into a half CSR on the device
+ * exactly as sortpair does (cpu_ref/force_aos.cpp:100-120): rows in i order,
+ * entries of a row in pair-array order. */
+int lj_list_set_pairs(lj_ctx* ctx, int32_t n, const int32_t* i_particles,
+                      const int32_t* j_particles, int64_t n_pairs, int32_t where);
+/* Copies the installed list (kind LJ_LIST_HALF or LJ_LIST_FULL) into caller
+ * arrays of the given location.  *n_entries receives the entry count; if
+ * capacity is too small nothing is copied and LJ_ERR_LIST_OVERFLOW is
+ * returned. */
+int lj_list_get_csr(lj_ctx* ctx, int32_t kind, int32_t* number_of_partners, int32_t* pointer,
+                    int32_t* sorted_list, int64_t capacity, int64_t* n_entries, int32_t where);
+/* Number of particles and entries of the installed list (0 if none). */
+int lj_list_info(const lj_ctx* ctx, int32_t kind, int32_t* n, int64_t* n_entries,
+                 int32_t* max_row);
+
+/* ---- force calls (device pointers) -------------------------------------- */
+/* One force call p += F dt with the installed list: the context equivalent of
+ * one force_kernel_* launch (cuda/force_cuda.cu:334) or one cpu_ref
+ * force_sorted() call.  q and p are AoS double[n][4] on the device. */
+int lj_force_aos(lj_ctx* ctx, const double* q, double* p, int32_t n, const lj_force_opts* opts);
+/* SoA variant (cpu_ref/force_soa.cpp:163-195); six device arrays of n doubles */
+int lj_force_soa(lj_ctx* ctx, const double* qx, const double* qy, const double* qz, double* px,
+                 double* py, double* pz, int32_t n, const lj_force_opts* opts);
+
+/* Stateless FP64 drop-in for a reference kernel launch: the argument list of
+ * force_kernel_* (cuda/kernel.cuh:5-13) on AoS double4 buffers, with the list
+ * kind saying whether list is a full list (gather, like force_kernel_memopt /
+ * warp_unroll) or a half list (scatter with atomics, like the _with_aar
+ * kernels).  box == NULL gives open boundaries.  Allocates nothing and does
+ * not validate the list (the reference kernels do not either). */
+int lj_force_csr_fp64_aos(const double* q, double* p, int32_t n, double dt, double cl2,
+                          const int32_t* sorted_list, const int32_t* number_of_partners,
+                          const int32_t* pointer, int32_t kind, const double* box,
+                          void* stream);
+/* force_pair on the device (cpu_ref/force_aos.cpp:171-190): FP64 scatter over
+ * an unsorted (i, j) pair array, both ends updated with atomics. */
+int lj_force_pairs_fp64_aos(const double* q, double* p, int32_t n, double dt, double cl2,
+                            const int32_t* i_particles, const int32_t* j_particles,
+                            int64_t n_pairs, const double* box, void* stream);
+
+/* ---- system set-up (host memory, no GPU needed) -------------------------- */
+/* The reference's init() (cpu_ref/force_aos.cpp:142-169, add_particle :43-51):
+ * FCC cells of side (4/density)^(1/3), floor(box_len / side) cells per axis,
+ * jitter U[0, 0.1) per coordinate from std::mt19937(2) in call order x, y, z.
+ * q is AoS double[capacity][4]; *n_out receives the particle count.
+ * LJ_ERR_LIST_OVERFLOW if capacity is too small (nothing is written then). */
+int lj_init_reference(double density, double box_len, double* q, int32_t capacity,
+                      int32_t* n_out);
+/* Periodic FCC of ncell^3 cells (N = 4 ncell^3) at the given density, box
+ * L = ncell (4/density)^(1/3), each coordinate jittered by U[-jitter, jitter)
+ * from std::mt19937_64(seed) in order x, y, z and wrapped into [0, L).
+ * No reference counterpart (the reference has no periodic box). */
+int lj_init_fcc(int32_t ncell, double density, double jitter, uint64_t seed, double* q,
+                int32_t capacity, double* box_len);
+/* Maxwell-Boltzmann momenta at temperature T (m = 1): N(0, T) per component
+ * from std::mt19937_64(seed), total momentum removed.  p is AoS double[n][4].
+ * No reference counterpart (the reference never integrates). */
+int lj_init_momenta(double* p, int32_t n, double temperature, uint64_t seed);
+
+/* ---- on-device neighbour build ------------------------------------------ */
+enum { LJ_BUILD_HALF = 1, LJ_BUILD_FULL = 2 };
+/* Builds the neighbour list of the AoS device positions q on the GPU with a
+ * cell grid (cell side >= search_radius) and installs it in ctx, replacing
+ * the reference's O(N^2) makepair + sortpair (cpu_ref/force_aos.cpp:100-140,
+ * cuda/force_cuda.cu:122-163).  Membership is the reference's
+ * r2 < search_radius^2 with dx = q_i - q_j (minimum image when box != NULL);
+ * rows come out ascending in j, so the half list is exactly the reference's.
+ * kinds: LJ_BUILD_HALF | LJ_BUILD_FULL (which lists to keep). */
+int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double search_radius,
+                  const double* box, int32_t kinds);
+
+/* ---- host-buffer call (the reference's measure(), force_cuda.cu:319-342) - */
+/* Uploads q and p from host memory, runs `calls` force calls on the installed
+ * list, downloads p, and synchronises.  If the list was installed from host
+ * memory it is uploaded again first, as copy_to_gpu does.  ms_total covers
+ * the whole sequence, ms_calc only the force calls (either may be NULL). */
+int lj_measure_aos(lj_ctx* ctx, const double* q_host, double* p_host, int32_t n,
+                   const lj_force_opts* opts, int32_t calls, double* ms_total, double* ms_calc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LJ_GB300_H */

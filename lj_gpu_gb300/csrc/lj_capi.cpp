@@ -1,0 +1,842 @@
+// lj_capi.cpp -- implementation of the C ABI in include/lj_gb300.h.
+//
+// Host-side C++: argument checking, list installation (validation, half->full
+// expansion), buffer management and kernel dispatch.  No arithmetic of the
+// force path runs here; every force call is a CUDA launch on the context's
+// stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lj_gb300.h"
+#include "lj_internal.h"
+#include "lj_nlist.h"
+
+using namespace ljg;
+
+namespace {
+
+// Grow-only device buffer.
+template <typename T>
+struct DevBuf {
+  T* ptr = nullptr;
+  size_t cap = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+  cudaError_t ensure(size_t count) {
+    if (count <= cap && ptr) return cudaSuccess;
+    release();
+    const size_t c = count > 0 ? count : 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&ptr), c * sizeof(T));
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      return e;
+    }
+    cap = c;
+    return cudaSuccess;
+  }
+};
+
+struct DevList {
+  DevBuf<int32_t> np, ptr, list;
+  int n = 0;
+  int64_t entries = 0;
+  int max_row = 0;
+  bool valid = false;
+  Csr csr() const { return Csr{n, entries, np.ptr, ptr.ptr, list.ptr}; }
+};
+
+}  // namespace
+
+struct lj_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  DevList half, full;
+  // host copies when the list came from host memory (re-uploaded by measure)
+  bool list_from_host = false;
+  int32_t host_kind = LJ_LIST_HALF;
+  std::vector<int32_t> h_np, h_ptr, h_list;
+  // scratch
+  DevBuf<int4> qfix;
+  DevBuf<float> fscratch;
+  DevBuf<double> maxabs;
+  DevBuf<int32_t> err2;
+  DevBuf<int32_t> tmp_i32a, tmp_i32b;
+  DevBuf<int64_t> tmp_off;
+  DevBuf<unsigned char> tmp_scan;
+  DevBuf<double> mq, mp;  // device q / p for lj_measure_aos
+  // neighbour build
+  DevBuf<int32_t> b_cell, b_count, b_cursor, b_order, b_cnt_half, b_cnt_full;
+  DevBuf<int64_t> b_start, b_off_half, b_off_full;
+  DevBuf<int4> b_cq;
+  DevBuf<unsigned long long> b_minmax;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+};
+
+namespace {
+
+int fail(lj_ctx* ctx, int code, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    ctx->err = buf;
+  }
+  return code;
+}
+
+int cuda_fail(lj_ctx* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, e == cudaErrorMemoryAllocation ? LJ_ERR_OUT_OF_MEMORY : LJ_ERR_CUDA,
+              "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define LJ_CUDA(ctx, call, what)                 \
+  do {                                           \
+    cudaError_t e_ = (call);                     \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+  } while (0)
+
+bool pow2_lanes(int v) { return v == 1 || v == 2 || v == 4 || v == 8 || v == 16 || v == 32; }
+
+int check_opts(lj_ctx* ctx, const lj_force_opts* o) {
+  if (!o) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "opts is NULL");
+  if (!(o->precision == LJ_PREC_FP64 || o->precision == LJ_PREC_MIXED))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown precision %d", o->precision);
+  if (o->method < LJ_METHOD_AUTO || o->method > LJ_METHOD_SCATTER_HALF)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown method %d", o->method);
+  if (o->lanes != 0 && !pow2_lanes(o->lanes))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "lanes must be 0 or a power of two <= 32");
+  if (o->block != 0 && (o->block < 64 || o->block > 256 || (o->block % 32) != 0))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "block must be 0 or a multiple of 32 in [64, 256]");
+  if (!(o->cl2 >= 0.0) || !std::isfinite(o->dt))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "cl2 must be >= 0 and dt finite");
+  if (o->periodic) {
+    for (int d = 0; d < 3; d++)
+      if (!(o->box[d] > 0.0) || !std::isfinite(o->box[d]))
+        return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "periodic box lengths must be > 0");
+    const double mn = std::min(o->box[0], std::min(o->box[1], o->box[2]));
+    if (o->cl2 > 0.25 * mn * mn)
+      return fail(ctx, LJ_ERR_INVALID_ARGUMENT,
+                  "cutoff exceeds half the box: the minimum image is ambiguous");
+  }
+  return LJ_OK;
+}
+
+Periodic make_periodic(const lj_force_opts* o) {
+  Periodic b{};
+  b.on = o->periodic ? 1 : 0;
+  for (int d = 0; d < 3; d++) {
+    b.len[d] = b.on ? o->box[d] : 0.0;
+    b.half[d] = 0.5 * b.len[d];
+  }
+  return b;
+}
+
+// Default lanes per i-particle: chosen from the average row length so that a
+// group takes 4-8 strided steps per row.
+int default_lanes(int precision, int method, int64_t entries, int n) {
+  (void)precision;
+  (void)method;
+  const double avg = n > 0 ? (double)entries / n : 0.0;
+  if (avg <= 12) return 2;
+  if (avg <= 24) return 4;
+  if (avg <= 96) return 8;
+  return 16;
+}
+
+int copy_in(lj_ctx* ctx, int32_t* dst, const int32_t* src, size_t count, int where) {
+  if (count == 0) return LJ_OK;
+  LJ_CUDA(ctx,
+          cudaMemcpyAsync(dst, src, count * sizeof(int32_t),
+                          where == LJ_WHERE_HOST ? cudaMemcpyHostToDevice
+                                                 : cudaMemcpyDeviceToDevice,
+                          ctx->stream),
+          "list copy");
+  return LJ_OK;
+}
+
+// Validates the CSR in `l` on the device; synchronises.
+int validate(lj_ctx* ctx, const DevList& l) {
+  LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
+  const int32_t init[2] = {0, 0x7fffffff};
+  LJ_CUDA(ctx, cudaMemcpyAsync(ctx->err2.ptr, init, sizeof init, cudaMemcpyHostToDevice,
+                               ctx->stream), "err init");
+  LJ_CUDA(ctx, launch_validate_csr(l.csr(), ctx->err2.ptr, ctx->stream), "validate");
+  int32_t out[2];
+  LJ_CUDA(ctx, cudaMemcpyAsync(out, ctx->err2.ptr, sizeof out, cudaMemcpyDeviceToHost,
+                               ctx->stream), "err read");
+  LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "validate sync");
+  switch (out[0]) {
+    case 0: return LJ_OK;
+    case 1: return fail(ctx, LJ_ERR_BAD_LIST, "number_of_partners[%d] out of range", out[1]);
+    case 2: return fail(ctx, LJ_ERR_BAD_LIST, "pointer[%d] out of range", out[1]);
+    case 3: return fail(ctx, LJ_ERR_BAD_LIST, "row %d runs past the end of the list", out[1]);
+    default: return fail(ctx, LJ_ERR_BAD_LIST, "sorted_list[%d] out of range", out[1]);
+  }
+}
+
+// Builds ctx->full from ctx->half on the device.
+int expand_full(lj_ctx* ctx) {
+  const Csr h = ctx->half.csr();
+  const int n = h.n;
+  if ((int64_t)2 * h.entries > 0x7fffffffll)
+    return fail(ctx, LJ_ERR_UNSUPPORTED, "full list would exceed 2^31-1 entries");
+  LJ_CUDA(ctx, ctx->tmp_i32a.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->tmp_off.ensure((size_t)n + 1), "alloc");
+  LJ_CUDA(ctx, ctx->tmp_scan.ensure(scan_tmp_bytes(n)), "alloc");
+  LJ_CUDA(ctx, launch_full_from_half_count(h, ctx->tmp_i32a.ptr, ctx->stream), "count");
+  LJ_CUDA(ctx, launch_scan_counts(ctx->tmp_i32a.ptr, n, ctx->tmp_off.ptr, ctx->tmp_scan.ptr,
+                                  ctx->tmp_scan.cap, ctx->stream), "scan");
+  int64_t total = 0;
+  LJ_CUDA(ctx, cudaMemcpyAsync(&total, ctx->tmp_off.ptr + n, sizeof total,
+                               cudaMemcpyDeviceToHost, ctx->stream), "total");
+  LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+  DevList& f = ctx->full;
+  f.valid = false;
+  LJ_CUDA(ctx, f.np.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, f.ptr.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, f.list.ensure((size_t)total), "alloc");
+  LJ_CUDA(ctx, ctx->tmp_i32b.ensure((size_t)total), "alloc");
+  LJ_CUDA(ctx, launch_full_from_half_fill(h, ctx->tmp_off.ptr, ctx->tmp_i32a.ptr,
+                                          ctx->tmp_i32b.ptr, ctx->stream), "fill");
+  LJ_CUDA(ctx, launch_sort_rows_into(ctx->tmp_off.ptr, n, ctx->tmp_i32b.ptr, f.list.ptr,
+                                     ctx->stream), "sort");
+  LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
+  LJ_CUDA(ctx, launch_offsets_to_ptr(ctx->tmp_off.ptr, n, f.ptr.ptr, f.np.ptr, ctx->err2.ptr,
+                                     ctx->stream), "ptr");
+  int32_t mr = 0;
+  LJ_CUDA(ctx, cudaMemcpyAsync(&mr, ctx->err2.ptr, sizeof mr, cudaMemcpyDeviceToHost,
+                               ctx->stream), "max row");
+  LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+  f.n = n;
+  f.entries = total;
+  f.max_row = mr;
+  f.valid = true;
+  return LJ_OK;
+}
+
+int row_max(lj_ctx* ctx, DevList& l) {
+  // max row of an installed list (reuses the offsets->ptr reduction path)
+  std::vector<int32_t> np((size_t)l.n);
+  if (l.n > 0)
+    LJ_CUDA(ctx, cudaMemcpyAsync(np.data(), l.np.ptr, sizeof(int32_t) * (size_t)l.n,
+                                 cudaMemcpyDeviceToHost, ctx->stream), "np read");
+  LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+  int m = 0;
+  for (int v : np) m = std::max(m, v);
+  l.max_row = m;
+  return LJ_OK;
+}
+
+int install_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ptr,
+                const int32_t* list, int64_t entries, int32_t kind, int32_t where) {
+  DevList& l = kind == LJ_LIST_HALF ? ctx->half : ctx->full;
+  ctx->half.valid = false;
+  ctx->full.valid = false;
+  LJ_CUDA(ctx, l.np.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, l.ptr.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, l.list.ensure((size_t)entries), "alloc");
+  int rc;
+  if ((rc = copy_in(ctx, l.np.ptr, np, (size_t)n, where))) return rc;
+  if ((rc = copy_in(ctx, l.ptr.ptr, ptr, (size_t)n, where))) return rc;
+  if ((rc = copy_in(ctx, l.list.ptr, list, (size_t)entries, where))) return rc;
+  l.n = n;
+  l.entries = entries;
+  if ((rc = validate(ctx, l))) return rc;
+  if ((rc = row_max(ctx, l))) return rc;
+  l.valid = true;
+  if (kind == LJ_LIST_HALF) {
+    if ((rc = expand_full(ctx))) {
+      ctx->half.valid = false;
+      return rc;
+    }
+  }
+  return LJ_OK;
+}
+
+int resolve_method(lj_ctx* ctx, const lj_force_opts* o, int* method) {
+  int m = o->method;
+  if (m == LJ_METHOD_AUTO) {
+    if (o->precision == LJ_PREC_FP64)
+      m = ctx->half.valid ? LJ_METHOD_SCATTER_HALF : LJ_METHOD_GATHER_FULL;
+    else
+      m = LJ_METHOD_GATHER_FULL;
+  }
+  if (m == LJ_METHOD_SCATTER_HALF && !ctx->half.valid)
+    return fail(ctx, ctx->full.valid ? LJ_ERR_UNSUPPORTED : LJ_ERR_NO_LIST,
+                "scatter over a half list needs a half list installed");
+  if (m == LJ_METHOD_GATHER_FULL && !ctx->full.valid)
+    return fail(ctx, LJ_ERR_NO_LIST, "no neighbour list installed");
+  *method = m;
+  return LJ_OK;
+}
+
+int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts* o) {
+  int rc = check_opts(ctx, o);
+  if (rc) return rc;
+  int method;
+  if ((rc = resolve_method(ctx, o, &method))) return rc;
+  const DevList& l = method == LJ_METHOD_SCATTER_HALF ? ctx->half : ctx->full;
+  if (n != l.n)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "n = %d but the installed list has %d rows", n,
+                l.n);
+  ForceLaunch L{};
+  L.part = part;
+  L.csr = l.csr();
+  L.box = make_periodic(o);
+  L.dt = o->dt;
+  L.cl2 = o->cl2;
+  L.precision = o->precision;
+  L.method = method;
+  L.lanes = o->lanes ? o->lanes : default_lanes(o->precision, method, l.entries, l.n);
+  L.block = o->block ? o->block : 128;
+  if (n == 0) return LJ_OK;
+  if (o->precision == LJ_PREC_MIXED) {
+    LJ_CUDA(ctx, ctx->qfix.ensure((size_t)n), "alloc");
+    L.qfix = ctx->qfix.ptr;
+    double max_abs = 0.0;
+    if (!L.box.on) {
+      LJ_CUDA(ctx, ctx->maxabs.ensure(1), "alloc");
+      LJ_CUDA(ctx, launch_max_abs(part, n, ctx->maxabs.ptr, ctx->stream), "max_abs");
+      LJ_CUDA(ctx, cudaMemcpyAsync(&max_abs, ctx->maxabs.ptr, sizeof max_abs,
+                                   cudaMemcpyDeviceToHost, ctx->stream), "max_abs read");
+      LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+      if (!std::isfinite(max_abs))
+        return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "non-finite position");
+    }
+    make_fixed_frame(L, max_abs);
+    if (method == LJ_METHOD_SCATTER_HALF) {
+      LJ_CUDA(ctx, ctx->fscratch.ensure(3 * (size_t)n), "alloc");
+      L.fscratch = ctx->fscratch.ptr;
+    }
+    LJ_CUDA(ctx, launch_fixed_image(L, ctx->stream), "fixed image");
+  }
+  LJ_CUDA(ctx, launch_force(L, ctx->stream), "force launch");
+  return LJ_OK;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace
+
+extern "C" {
+
+void lj_force_opts_default(lj_force_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof *o);
+  o->dt = 0.001;
+  o->cl2 = 9.0;
+  o->precision = LJ_PREC_FP64;
+  o->method = LJ_METHOD_AUTO;
+}
+
+int lj_abi_version(void) { return LJ_GB300_ABI_VERSION; }
+
+const char* lj_status_string(int s) {
+  switch (s) {
+    case LJ_OK: return "ok";
+    case LJ_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case LJ_ERR_BAD_LIST: return "neighbour list failed validation";
+    case LJ_ERR_CUDA: return "CUDA error";
+    case LJ_ERR_OUT_OF_MEMORY: return "out of memory";
+    case LJ_ERR_LIST_OVERFLOW: return "list capacity exceeded";
+    case LJ_ERR_TIMEOUT: return "device wait timed out";
+    case LJ_ERR_NO_LIST: return "no neighbour list installed";
+    case LJ_ERR_UNSUPPORTED: return "unsupported combination";
+    default: return "unknown status";
+  }
+}
+
+int lj_ctx_create(lj_ctx** out, int device) {
+  if (!out) return LJ_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return LJ_ERR_CUDA;
+  if (device < 0 || device >= count) return LJ_ERR_INVALID_ARGUMENT;
+  if (cudaSetDevice(device) != cudaSuccess) return LJ_ERR_CUDA;
+  lj_ctx* c = new (std::nothrow) lj_ctx();
+  if (!c) return LJ_ERR_OUT_OF_MEMORY;
+  c->device = device;
+  for (auto& e : c->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      lj_ctx_destroy(c);
+      return LJ_ERR_CUDA;
+    }
+  *out = c;
+  return LJ_OK;
+}
+
+void lj_ctx_destroy(lj_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  else cudaDeviceSynchronize();
+  for (auto& e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  delete ctx;
+}
+
+const char* lj_ctx_last_error(const lj_ctx* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int lj_ctx_set_stream(lj_ctx* ctx, void* stream) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  return LJ_OK;
+}
+
+int lj_list_set_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ptr,
+                    const int32_t* list, int64_t entries, int32_t kind, int32_t where) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (n < 0 || entries < 0 || entries > 0x7fffffffll)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "n and n_entries must be in [0, 2^31)");
+  if (kind != LJ_LIST_HALF && kind != LJ_LIST_FULL)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown list kind %d", kind);
+  if (where != LJ_WHERE_HOST && where != LJ_WHERE_DEVICE)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown location %d", where);
+  if ((n > 0 && (!np || !ptr)) || (entries > 0 && !list))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "null list array");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  int rc = install_csr(ctx, n, np, ptr, list, entries, kind, where);
+  if (rc) return rc;
+  ctx->list_from_host = where == LJ_WHERE_HOST;
+  ctx->host_kind = kind;
+  if (ctx->list_from_host) {
+    ctx->h_np.assign(np, np + n);
+    ctx->h_ptr.assign(ptr, ptr + n);
+    ctx->h_list.assign(list, list + entries);
+  } else {
+    ctx->h_np.clear();
+    ctx->h_ptr.clear();
+    ctx->h_list.clear();
+  }
+  return LJ_OK;
+}
+
+int lj_list_set_pairs(lj_ctx* ctx, int32_t n, const int32_t* ip, const int32_t* jp,
+                      int64_t npairs, int32_t where) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (n < 0 || npairs < 0 || npairs > 0x7fffffffll)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "n and n_pairs must be in [0, 2^31)");
+  if (where != LJ_WHERE_HOST && where != LJ_WHERE_DEVICE)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown location %d", where);
+  if (npairs > 0 && (!ip || !jp)) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "null pair array");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  // Pair arrays in makepair order (non-decreasing i) are sorted on the device:
+  // the CSR list is then j_particles itself.  Any other order is sorted with a
+  // stable counting sort on the host, as the reference's sortpair does.
+  std::vector<int32_t> hi, hj;
+  const int32_t* dj = jp;
+  bool sorted_input = true;
+  if (where == LJ_WHERE_HOST) {
+    for (int64_t k = 1; k < npairs && sorted_input; k++) sorted_input = ip[k - 1] <= ip[k];
+  }
+  if (where == LJ_WHERE_DEVICE) {
+    LJ_CUDA(ctx, ctx->tmp_i32a.ensure((size_t)n), "alloc");
+    LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
+    const int32_t init[2] = {0, 0x7fffffff};
+    LJ_CUDA(ctx, cudaMemcpyAsync(ctx->err2.ptr, init, sizeof init, cudaMemcpyHostToDevice,
+                                 ctx->stream), "err init");
+    LJ_CUDA(ctx, launch_pairs_count(ip, npairs, n, ctx->tmp_i32a.ptr, ctx->err2.ptr,
+                                    ctx->stream), "pairs count");
+    int32_t out[2];
+    LJ_CUDA(ctx, cudaMemcpyAsync(out, ctx->err2.ptr, sizeof out, cudaMemcpyDeviceToHost,
+                                 ctx->stream), "err read");
+    LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    if (out[0] == 4) return fail(ctx, LJ_ERR_BAD_LIST, "i_particles[%d] out of range", out[1]);
+    sorted_input = out[0] == 0;
+    if (!sorted_input) {
+      hi.resize((size_t)npairs);
+      hj.resize((size_t)npairs);
+      LJ_CUDA(ctx, cudaMemcpy(hi.data(), ip, sizeof(int32_t) * (size_t)npairs,
+                              cudaMemcpyDeviceToHost), "pairs read");
+      LJ_CUDA(ctx, cudaMemcpy(hj.data(), jp, sizeof(int32_t) * (size_t)npairs,
+                              cudaMemcpyDeviceToHost), "pairs read");
+      ip = hi.data();
+      jp = hj.data();
+      where = LJ_WHERE_HOST;
+    }
+  }
+  if (where == LJ_WHERE_HOST) {
+    std::vector<int32_t> np((size_t)n, 0), ptr((size_t)n, 0), list((size_t)npairs);
+    for (int64_t k = 0; k < npairs; k++) {
+      if (ip[k] < 0 || ip[k] >= n)
+        return fail(ctx, LJ_ERR_BAD_LIST, "i_particles[%lld] out of range", (long long)k);
+      np[(size_t)ip[k]]++;
+    }
+    int64_t pos = 0;
+    for (int i = 0; i < n; i++) {
+      ptr[(size_t)i] = (int32_t)pos;
+      pos += np[(size_t)i];
+    }
+    std::vector<int32_t> cur(ptr);
+    for (int64_t k = 0; k < npairs; k++) list[(size_t)cur[(size_t)ip[k]]++] = jp[k];
+    return lj_list_set_csr(ctx, n, np.data(), ptr.data(), list.data(), npairs, LJ_LIST_HALF,
+                           LJ_WHERE_HOST);
+  }
+  // device, non-decreasing i: counts are in tmp_i32a; offsets by scan
+  LJ_CUDA(ctx, ctx->tmp_off.ensure((size_t)n + 1), "alloc");
+  LJ_CUDA(ctx, ctx->tmp_scan.ensure(scan_tmp_bytes(n)), "alloc");
+  LJ_CUDA(ctx, launch_scan_counts(ctx->tmp_i32a.ptr, n, ctx->tmp_off.ptr, ctx->tmp_scan.ptr,
+                                  ctx->tmp_scan.cap, ctx->stream), "scan");
+  DevBuf<int32_t> np_d, ptr_d;
+  LJ_CUDA(ctx, np_d.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, ptr_d.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
+  LJ_CUDA(ctx, launch_offsets_to_ptr(ctx->tmp_off.ptr, n, ptr_d.ptr, np_d.ptr, ctx->err2.ptr,
+                                     ctx->stream), "ptr");
+  LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+  return lj_list_set_csr(ctx, n, np_d.ptr, ptr_d.ptr, dj, npairs, LJ_LIST_HALF,
+                         LJ_WHERE_DEVICE);
+}
+
+int lj_list_get_csr(lj_ctx* ctx, int32_t kind, int32_t* np, int32_t* ptr, int32_t* list,
+                    int64_t capacity, int64_t* n_entries, int32_t where) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  if (kind != LJ_LIST_HALF && kind != LJ_LIST_FULL)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown list kind %d", kind);
+  if (where != LJ_WHERE_HOST && where != LJ_WHERE_DEVICE)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown location %d", where);
+  const DevList& l = kind == LJ_LIST_HALF ? ctx->half : ctx->full;
+  if (!l.valid) return fail(ctx, LJ_ERR_NO_LIST, "no list of that kind installed");
+  if (n_entries) *n_entries = l.entries;
+  if (capacity < l.entries) return fail(ctx, LJ_ERR_LIST_OVERFLOW, "capacity too small");
+  if ((l.n > 0 && (!np || !ptr)) || (l.entries > 0 && !list))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "null output array");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  const cudaMemcpyKind k =
+      where == LJ_WHERE_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if (l.n > 0) {
+    LJ_CUDA(ctx, cudaMemcpyAsync(np, l.np.ptr, sizeof(int32_t) * (size_t)l.n, k, ctx->stream),
+            "copy");
+    LJ_CUDA(ctx, cudaMemcpyAsync(ptr, l.ptr.ptr, sizeof(int32_t) * (size_t)l.n, k, ctx->stream),
+            "copy");
+  }
+  if (l.entries > 0)
+    LJ_CUDA(ctx, cudaMemcpyAsync(list, l.list.ptr, sizeof(int32_t) * (size_t)l.entries, k,
+                                 ctx->stream), "copy");
+  LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+  return LJ_OK;
+}
+
+int lj_list_info(const lj_ctx* ctx, int32_t kind, int32_t* n, int64_t* n_entries,
+                 int32_t* max_row) {
+  if (!ctx || (kind != LJ_LIST_HALF && kind != LJ_LIST_FULL)) return LJ_ERR_INVALID_ARGUMENT;
+  const DevList& l = kind == LJ_LIST_HALF ? ctx->half : ctx->full;
+  if (n) *n = l.valid ? l.n : 0;
+  if (n_entries) *n_entries = l.valid ? l.entries : 0;
+  if (max_row) *max_row = l.valid ? l.max_row : 0;
+  return LJ_OK;
+}
+
+int lj_force_aos(lj_ctx* ctx, const double* q, double* p, int32_t n, const lj_force_opts* o) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (n < 0) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "n < 0");
+  if (n > 0 && (!q || !p)) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "null q or p");
+  if (!aligned16(q) || !aligned16(p))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "AoS q and p must be 16-byte aligned");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  Particles part{};
+  part.soa = 0;
+  part.q = q;
+  part.p = p;
+  return run_force(ctx, part, n, o);
+}
+
+int lj_force_soa(lj_ctx* ctx, const double* qx, const double* qy, const double* qz, double* px,
+                 double* py, double* pz, int32_t n, const lj_force_opts* o) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (n < 0) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "n < 0");
+  if (n > 0 && (!qx || !qy || !qz || !px || !py || !pz))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "null SoA array");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  Particles part{};
+  part.soa = 1;
+  part.qx = qx;
+  part.qy = qy;
+  part.qz = qz;
+  part.px = px;
+  part.py = py;
+  part.pz = pz;
+  return run_force(ctx, part, n, o);
+}
+
+int lj_force_csr_fp64_aos(const double* q, double* p, int32_t n, double dt, double cl2,
+                          const int32_t* list, const int32_t* np, const int32_t* ptr,
+                          int32_t kind, const double* box, void* stream) {
+  if (n < 0 || (n > 0 && (!q || !p || !np || !ptr))) return LJ_ERR_INVALID_ARGUMENT;
+  if (kind != LJ_LIST_HALF && kind != LJ_LIST_FULL) return LJ_ERR_INVALID_ARGUMENT;
+  if (!aligned16(q) || !aligned16(p)) return LJ_ERR_INVALID_ARGUMENT;
+  if (!(cl2 >= 0.0) || !std::isfinite(dt)) return LJ_ERR_INVALID_ARGUMENT;
+  if (n == 0) return LJ_OK;
+  ForceLaunch L{};
+  L.part.soa = 0;
+  L.part.q = q;
+  L.part.p = p;
+  L.csr = Csr{n, 0, np, ptr, list};
+  if (box) {
+    L.box.on = 1;
+    for (int d = 0; d < 3; d++) {
+      if (!(box[d] > 0.0)) return LJ_ERR_INVALID_ARGUMENT;
+      L.box.len[d] = box[d];
+      L.box.half[d] = 0.5 * box[d];
+    }
+  }
+  L.dt = dt;
+  L.cl2 = cl2;
+  L.precision = LJ_PREC_FP64;
+  L.method = kind == LJ_LIST_FULL ? LJ_METHOD_GATHER_FULL : LJ_METHOD_SCATTER_HALF;
+  L.lanes = 8;
+  L.block = 128;
+  return launch_force(L, static_cast<cudaStream_t>(stream)) == cudaSuccess ? LJ_OK
+                                                                          : LJ_ERR_CUDA;
+}
+
+int lj_force_pairs_fp64_aos(const double* q, double* p, int32_t n, double dt, double cl2,
+                            const int32_t* ip, const int32_t* jp, int64_t npairs,
+                            const double* box, void* stream) {
+  if (n < 0 || npairs < 0 || (npairs > 0 && (!q || !p || !ip || !jp)))
+    return LJ_ERR_INVALID_ARGUMENT;
+  if (!aligned16(q) || !aligned16(p)) return LJ_ERR_INVALID_ARGUMENT;
+  if (!(cl2 >= 0.0) || !std::isfinite(dt)) return LJ_ERR_INVALID_ARGUMENT;
+  Particles part{};
+  part.q = q;
+  part.p = p;
+  Periodic b{};
+  if (box) {
+    b.on = 1;
+    for (int d = 0; d < 3; d++) {
+      if (!(box[d] > 0.0)) return LJ_ERR_INVALID_ARGUMENT;
+      b.len[d] = box[d];
+      b.half[d] = 0.5 * box[d];
+    }
+  }
+  return launch_force_pairs(part, n, ip, jp, npairs, b, dt, cl2,
+                            static_cast<cudaStream_t>(stream)) == cudaSuccess
+             ? LJ_OK
+             : LJ_ERR_CUDA;
+}
+
+int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const double* box,
+                  int32_t kinds) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (n < 0 || (n > 0 && !q)) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "bad n or q");
+  if (!aligned16(q)) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "q must be 16-byte aligned");
+  if (!(rs > 0.0) || !std::isfinite(rs))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "search radius must be > 0");
+  if (kinds < 1 || kinds > 3) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kinds must be 1..3");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  const bool want_half = kinds & LJ_BUILD_HALF, want_full = kinds & LJ_BUILD_FULL;
+  cudaStream_t s = ctx->stream;
+  CellGrid g{};
+  ForceLaunch F{};
+  F.part.soa = 0;
+  F.part.q = q;
+  F.csr.n = n;
+  double max_abs = 0.0;
+  if (box) {
+    g.periodic = 1;
+    for (int d = 0; d < 3; d++) {
+      if (!(box[d] > 0.0) || !std::isfinite(box[d]))
+        return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "box lengths must be > 0");
+      if (rs > 0.5 * box[d])
+        return fail(ctx, LJ_ERR_INVALID_ARGUMENT,
+                    "search radius exceeds half the box: the minimum image is ambiguous");
+      F.box.on = 1;
+      F.box.len[d] = box[d];
+      F.box.half[d] = 0.5 * box[d];
+      g.nc[d] = std::max(1, (int)std::floor(box[d] / rs));
+      g.nc[d] = std::min(g.nc[d], 1024);
+      g.lo[d] = 0.0;
+      g.inv_w[d] = g.nc[d] / box[d];
+    }
+  } else {
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if (n > 0) {
+      LJ_CUDA(ctx, ctx->b_minmax.ensure(6), "alloc");
+      LJ_CUDA(ctx, launch_minmax(q, n, ctx->b_minmax.ptr, s), "minmax");
+      unsigned long long k6[6];
+      LJ_CUDA(ctx, cudaMemcpyAsync(k6, ctx->b_minmax.ptr, sizeof k6, cudaMemcpyDeviceToHost, s),
+              "minmax read");
+      LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+      for (int d = 0; d < 3; d++) {
+        hi[d] = key_to_double(k6[d]);
+        lo[d] = key_to_double(~k6[3 + d]);
+        if (!std::isfinite(lo[d]) || !std::isfinite(hi[d]))
+          return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "non-finite position");
+        max_abs = std::max(max_abs, std::max(std::fabs(lo[d]), std::fabs(hi[d])));
+      }
+    }
+    // at most ~2 n cells overall, every side >= rs
+    const double cap = std::cbrt(2.0 * std::max(n, 1)) + 1.0;
+    for (int d = 0; d < 3; d++) {
+      const double ext = (hi[d] - lo[d]) * (1.0 + 1e-12) + 1e-300;
+      g.nc[d] = std::max(1, std::min((int)std::floor(ext / rs), (int)cap));
+      g.lo[d] = lo[d];
+      g.inv_w[d] = g.nc[d] / ext;
+    }
+  }
+  g.ncells = g.nc[0] * g.nc[1] * g.nc[2];
+  make_fixed_frame(F, max_abs);
+  LJ_CUDA(ctx, ctx->qfix.ensure((size_t)std::max(n, 1)), "alloc");
+  F.qfix = ctx->qfix.ptr;
+  LJ_CUDA(ctx, ctx->b_cell.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->b_order.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->b_cq.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->b_count.ensure((size_t)g.ncells), "alloc");
+  LJ_CUDA(ctx, ctx->b_cursor.ensure((size_t)g.ncells), "alloc");
+  LJ_CUDA(ctx, ctx->b_start.ensure((size_t)g.ncells + 1), "alloc");
+  LJ_CUDA(ctx, ctx->tmp_scan.ensure(scan_tmp_bytes(std::max(g.ncells, n))), "alloc");
+  if (n > 0) LJ_CUDA(ctx, launch_fixed_image(F, s), "fixed image");
+  LJ_CUDA(ctx, launch_bin(q, n, g, ctx->b_cell.ptr, ctx->b_count.ptr, s), "bin");
+  LJ_CUDA(ctx, launch_scan_counts(ctx->b_count.ptr, g.ncells, ctx->b_start.ptr, ctx->tmp_scan.ptr,
+                                  ctx->tmp_scan.cap, s), "cell scan");
+  LJ_CUDA(ctx, launch_place(ctx->b_cell.ptr, n, ctx->b_start.ptr, ctx->b_cursor.ptr, g.ncells,
+                            ctx->qfix.ptr, ctx->b_order.ptr, ctx->b_cq.ptr, s), "place");
+  BuildArgs a{};
+  a.q = q;
+  a.n = n;
+  a.grid = g;
+  a.search = rs;
+  for (int d = 0; d < 3; d++) {
+    a.box[d] = box ? box[d] : 0.0;
+    a.unit[d] = F.unit[d];
+  }
+  a.aniso = F.aniso;
+  a.start = ctx->b_start.ptr;
+  a.order = ctx->b_order.ptr;
+  a.cq = ctx->b_cq.ptr;
+  a.cell = ctx->b_cell.ptr;
+  a.want_half = want_half;
+  a.want_full = want_full;
+  LJ_CUDA(ctx, ctx->b_cnt_half.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->b_cnt_full.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->b_off_half.ensure((size_t)n + 1), "alloc");
+  LJ_CUDA(ctx, ctx->b_off_full.ensure((size_t)n + 1), "alloc");
+  a.cnt_half = ctx->b_cnt_half.ptr;
+  a.cnt_full = ctx->b_cnt_full.ptr;
+  LJ_CUDA(ctx, launch_walk(a, false, s), "count walk");
+  int64_t tot[2] = {0, 0};
+  ctx->half.valid = false;
+  ctx->full.valid = false;
+  for (int kind = 0; kind < 2; kind++) {
+    if (!(kind == 0 ? want_half : want_full)) continue;
+    int32_t* cnt = kind == 0 ? a.cnt_half : a.cnt_full;
+    int64_t* off = kind == 0 ? ctx->b_off_half.ptr : ctx->b_off_full.ptr;
+    LJ_CUDA(ctx, launch_scan_counts(cnt, n, off, ctx->tmp_scan.ptr, ctx->tmp_scan.cap, s),
+            "row scan");
+    LJ_CUDA(ctx, cudaMemcpyAsync(&tot[kind], off + n, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                 s), "total");
+  }
+  LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+  for (int kind = 0; kind < 2; kind++)
+    if (tot[kind] > 0x7fffffffll)
+      return fail(ctx, LJ_ERR_LIST_OVERFLOW, "list would exceed 2^31-1 entries");
+  a.off_half = ctx->b_off_half.ptr;
+  a.off_full = ctx->b_off_full.ptr;
+  LJ_CUDA(ctx, ctx->tmp_i32a.ensure((size_t)std::max<int64_t>(tot[0], 1)), "alloc");
+  LJ_CUDA(ctx, ctx->tmp_i32b.ensure((size_t)std::max<int64_t>(tot[1], 1)), "alloc");
+  a.out_half = ctx->tmp_i32a.ptr;
+  a.out_full = ctx->tmp_i32b.ptr;
+  LJ_CUDA(ctx, launch_walk(a, true, s), "fill walk");
+  LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
+  for (int kind = 0; kind < 2; kind++) {
+    if (!(kind == 0 ? want_half : want_full)) continue;
+    DevList& l = kind == 0 ? ctx->half : ctx->full;
+    const int64_t* off = kind == 0 ? a.off_half : a.off_full;
+    LJ_CUDA(ctx, l.np.ensure((size_t)n), "alloc");
+    LJ_CUDA(ctx, l.ptr.ensure((size_t)n), "alloc");
+    LJ_CUDA(ctx, l.list.ensure((size_t)std::max<int64_t>(tot[kind], 1)), "alloc");
+    LJ_CUDA(ctx, launch_sort_rows_into(off, n, kind == 0 ? a.out_half : a.out_full, l.list.ptr,
+                                       s), "row sort");
+    LJ_CUDA(ctx, launch_offsets_to_ptr(off, n, l.ptr.ptr, l.np.ptr, ctx->err2.ptr + kind, s),
+            "ptr");
+  }
+  int32_t mr[2] = {0, 0};
+  LJ_CUDA(ctx, cudaMemcpyAsync(mr, ctx->err2.ptr, sizeof mr, cudaMemcpyDeviceToHost, s), "read");
+  LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+  for (int kind = 0; kind < 2; kind++) {
+    if (!(kind == 0 ? want_half : want_full)) continue;
+    DevList& l = kind == 0 ? ctx->half : ctx->full;
+    l.n = n;
+    l.entries = tot[kind];
+    l.max_row = mr[kind];
+    l.valid = true;
+  }
+  ctx->list_from_host = false;
+  ctx->h_np.clear();
+  ctx->h_ptr.clear();
+  ctx->h_list.clear();
+  return LJ_OK;
+}
+
+int lj_measure_aos(lj_ctx* ctx, const double* q_host, double* p_host, int32_t n,
+                   const lj_force_opts* o, int32_t calls, double* ms_total, double* ms_calc) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (n < 0 || calls < 0) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "n and calls must be >= 0");
+  if (n > 0 && (!q_host || !p_host)) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "null q or p");
+  int rc = check_opts(ctx, o);
+  if (rc) return rc;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  const size_t bytes = sizeof(double) * 4 * (size_t)n;
+  LJ_CUDA(ctx, ctx->mq.ensure(4 * (size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->mp.ensure(4 * (size_t)n), "alloc");
+  cudaStream_t s = ctx->stream;
+  LJ_CUDA(ctx, cudaEventRecord(ctx->ev[0], s), "event");
+  // copy_to_gpu (cuda/force_cuda.cu:302-312): q, p and the list arrays
+  LJ_CUDA(ctx, cudaMemcpyAsync(ctx->mq.ptr, q_host, bytes, cudaMemcpyHostToDevice, s), "H2D q");
+  LJ_CUDA(ctx, cudaMemcpyAsync(ctx->mp.ptr, p_host, bytes, cudaMemcpyHostToDevice, s), "H2D p");
+  if (ctx->list_from_host) {
+    DevList& l = ctx->host_kind == LJ_LIST_HALF ? ctx->half : ctx->full;
+    if ((rc = copy_in(ctx, l.np.ptr, ctx->h_np.data(), ctx->h_np.size(), LJ_WHERE_HOST)))
+      return rc;
+    if ((rc = copy_in(ctx, l.ptr.ptr, ctx->h_ptr.data(), ctx->h_ptr.size(), LJ_WHERE_HOST)))
+      return rc;
+    if ((rc = copy_in(ctx, l.list.ptr, ctx->h_list.data(), ctx->h_list.size(), LJ_WHERE_HOST)))
+      return rc;
+  }
+  LJ_CUDA(ctx, cudaEventRecord(ctx->ev[1], s), "event");
+  Particles part{};
+  part.q = ctx->mq.ptr;
+  part.p = ctx->mp.ptr;
+  for (int c = 0; c < calls; c++)
+    if ((rc = run_force(ctx, part, n, o))) return rc;
+  LJ_CUDA(ctx, cudaEventRecord(ctx->ev[2], s), "event");
+  LJ_CUDA(ctx, cudaMemcpyAsync(p_host, ctx->mp.ptr, bytes, cudaMemcpyDeviceToHost, s), "D2H p");
+  LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+  float t_all = 0.f, t_calc = 0.f;
+  cudaEvent_t end;
+  LJ_CUDA(ctx, cudaEventCreate(&end), "event");
+  cudaEventRecord(end, s);
+  cudaEventSynchronize(end);
+  cudaEventElapsedTime(&t_all, ctx->ev[0], end);
+  cudaEventElapsedTime(&t_calc, ctx->ev[1], ctx->ev[2]);
+  cudaEventDestroy(end);
+  if (ms_total) *ms_total = t_all;
+  if (ms_calc) *ms_calc = t_calc;
+  return LJ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,589 @@
+// lj_force.cu -- Lennard-Jones neighbour-list force kernels for sm_103a.
+//
+// One force call is the kick p_i += sum_j df(r_ij) (q_j - q_i) with
+// df = (24 r^-8 - 48 r^-14) dt for r2 <= cl2, the arithmetic of
+// cpu_ref/force_aos.cpp:206-218 and cuda/kernel.cuh:22-31.
+//
+// Work mapping: a group of G lanes (G = 1..32, a power of two) owns one
+// i-particle and strides through its CSR row; the group's partial sums are
+// combined with xor shuffles (the role of warp_segment_reduce,
+// cuda/device_util.cuh:12-19, generalised to sub-warp groups).
+//
+//   FP64 gather (full list):   row sums only, one plain RMW of p_i.
+//   FP64 scatter (half list):  p_j -= f with RED.F64, p_i += row sum with one
+//                              atomic per row (the _with_aar kernels).
+//   mixed gather / scatter:    positions from the 32-bit fixed image, FP32
+//                              pair math with Kahan-compensated sums, FP64
+//                              only in the final p += F dt.
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+
+#include "lj_gb300.h"
+#include "lj_internal.h"
+
+namespace ljg {
+namespace {
+
+// ---------------------------------------------------------------------------
+// particle access
+// ---------------------------------------------------------------------------
+template <bool SOA>
+__device__ __forceinline__ double3 load_q(const Particles& P, int i) {
+  if (SOA) return make_double3(__ldg(P.qx + i), __ldg(P.qy + i), __ldg(P.qz + i));
+  const double* b = P.q + 4 * (size_t)i;
+  const double2 xy = __ldg(reinterpret_cast<const double2*>(b));
+  return make_double3(xy.x, xy.y, __ldg(b + 2));
+}
+
+template <bool SOA>
+__device__ __forceinline__ void add_p(const Particles& P, int i, double fx, double fy,
+                                      double fz) {
+  if (SOA) {
+    P.px[i] += fx;
+    P.py[i] += fy;
+    P.pz[i] += fz;
+  } else {
+    double* b = P.p + 4 * (size_t)i;
+    double2 xy = *reinterpret_cast<double2*>(b);
+    xy.x += fx;
+    xy.y += fy;
+    *reinterpret_cast<double2*>(b) = xy;
+    b[2] += fz;
+  }
+}
+
+// p_i = fma(f, s, p_i) per component: the single FP64 operation the mixed
+// path spends per particle and axis.
+template <bool SOA>
+__device__ __forceinline__ void kick_p(const Particles& P, int i, double fx, double fy,
+                                       double fz, const double* s) {
+  if (SOA) {
+    P.px[i] = fma(fx, s[0], P.px[i]);
+    P.py[i] = fma(fy, s[1], P.py[i]);
+    P.pz[i] = fma(fz, s[2], P.pz[i]);
+  } else {
+    double* b = P.p + 4 * (size_t)i;
+    double2 xy = *reinterpret_cast<double2*>(b);
+    xy.x = fma(fx, s[0], xy.x);
+    xy.y = fma(fy, s[1], xy.y);
+    *reinterpret_cast<double2*>(b) = xy;
+    b[2] = fma(fz, s[2], b[2]);
+  }
+}
+
+template <bool SOA>
+__device__ __forceinline__ void red_p(const Particles& P, int i, double fx, double fy,
+                                      double fz) {
+  if (SOA) {
+    atomicAdd(P.px + i, fx);
+    atomicAdd(P.py + i, fy);
+    atomicAdd(P.pz + i, fz);
+  } else {
+    double* b = P.p + 4 * (size_t)i;
+    atomicAdd(b + 0, fx);
+    atomicAdd(b + 1, fy);
+    atomicAdd(b + 2, fz);
+  }
+}
+
+__device__ __forceinline__ double flip_sign(double x) {
+  return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
+}
+
+// Constants of one launch, kept in registers / constant bank.
+struct Fp64Consts {
+  double c24, c48;  // 24 dt, 48 dt
+  long long cl2_bits;
+  double len[3];
+  long long half_bits[3];
+};
+
+// Separation q_j - q_i with the minimum image, FP64 (same expression on every
+// path so FP64 and mixed kernels agree on the cutoff mask).
+template <bool PBC>
+__device__ __forceinline__ double3 sep_fp64(const double3& qi, const double3& qj,
+                                            const Fp64Consts& k) {
+  double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
+  if (PBC) {
+    dx = min_image_fp64(dx, k.len[0], k.half_bits[0]);
+    dy = min_image_fp64(dy, k.len[1], k.half_bits[1]);
+    dz = min_image_fp64(dz, k.len[2], k.half_bits[2]);
+  }
+  return make_double3(dx, dy, dz);
+}
+
+__device__ __forceinline__ double r2_fp64(const double3& d) {
+  return fma(d.z, d.z, fma(d.y, d.y, d.x * d.x));
+}
+
+// true when the reference would skip the pair (r2 > CL2); NaN is not skipped,
+// exactly as `if (r2 > CL2) continue;` behaves.
+__device__ __forceinline__ bool beyond_cutoff(double r2, long long cl2_bits) {
+  const long long b = dbits(r2);
+  return b > cl2_bits && b <= 0x7ff0000000000000ll;
+}
+
+// df of the reference formula, with dt folded into the constants.
+__device__ __forceinline__ double df_fp64(double r2, const Fp64Consts& k) {
+  const double inv = rcp_fp64_in_range(r2) ? rcp_fp64(r2) : 1.0 / r2;
+  const double r6 = inv * inv * inv;
+  return (r6 * inv) * fma(-k.c48, r6, k.c24);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 gather over the full list
+// ---------------------------------------------------------------------------
+template <int G, bool PBC, bool SOA>
+__global__ void __launch_bounds__(256) k_gather_fp64(const Particles P, const Csr C,
+                                                     const Fp64Consts K) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / G;
+  const int lane = t & (G - 1);
+  const bool valid = i < C.n;
+  int cnt = 0, k0 = 0;
+  double3 qi = make_double3(0, 0, 0);
+  if (valid) {
+    cnt = __ldg(C.np + i);
+    k0 = __ldg(C.ptr + i);
+    qi = load_q<SOA>(P, i);
+  }
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  for (int k = lane; k < cnt; k += G) {
+    const int j = __ldg(C.list + k0 + k);
+    const double3 d = sep_fp64<PBC>(qi, load_q<SOA>(P, j), K);
+    const double r2 = r2_fp64(d);
+    if (beyond_cutoff(r2, K.cl2_bits)) continue;
+    const double df = df_fp64(r2, K);
+    fx = fma(df, d.x, fx);
+    fy = fma(df, d.y, fy);
+    fz = fma(df, d.z, fz);
+  }
+  if (G > 1) {
+    fx = group_reduce_fp64<G>(fx);
+    fy = group_reduce_fp64<G>(fy);
+    fz = group_reduce_fp64<G>(fz);
+  }
+  if (valid && lane == 0) add_p<SOA>(P, i, fx, fy, fz);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 scatter over the half list
+// ---------------------------------------------------------------------------
+template <int G, bool PBC, bool SOA>
+__global__ void __launch_bounds__(256) k_scatter_fp64(const Particles P, const Csr C,
+                                                      const Fp64Consts K) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / G;
+  const int lane = t & (G - 1);
+  const bool valid = i < C.n;
+  int cnt = 0, k0 = 0;
+  double3 qi = make_double3(0, 0, 0);
+  if (valid) {
+    cnt = __ldg(C.np + i);
+    k0 = __ldg(C.ptr + i);
+    qi = load_q<SOA>(P, i);
+  }
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  for (int k = lane; k < cnt; k += G) {
+    const int j = __ldg(C.list + k0 + k);
+    const double3 d = sep_fp64<PBC>(qi, load_q<SOA>(P, j), K);
+    const double r2 = r2_fp64(d);
+    if (beyond_cutoff(r2, K.cl2_bits)) continue;
+    const double ndf = flip_sign(df_fp64(r2, K));
+    const double jx = ndf * d.x, jy = ndf * d.y, jz = ndf * d.z;
+    fx -= jx;
+    fy -= jy;
+    fz -= jz;
+    red_p<SOA>(P, j, jx, jy, jz);
+  }
+  if (G > 1) {
+    fx = group_reduce_fp64<G>(fx);
+    fy = group_reduce_fp64<G>(fy);
+    fz = group_reduce_fp64<G>(fz);
+  }
+  if (valid && lane == 0) red_p<SOA>(P, i, fx, fy, fz);
+}
+
+// ---------------------------------------------------------------------------
+// force_pair on the device: unsorted pair array, both ends by atomics
+// ---------------------------------------------------------------------------
+template <bool PBC>
+__global__ void __launch_bounds__(256) k_pairs_fp64(const Particles P, const int32_t* ip,
+                                                    const int32_t* jp, int64_t npairs,
+                                                    const Fp64Consts K) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npairs;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int i = __ldg(ip + k), j = __ldg(jp + k);
+    const double3 d = sep_fp64<PBC>(load_q<false>(P, i), load_q<false>(P, j), K);
+    const double r2 = r2_fp64(d);
+    if (beyond_cutoff(r2, K.cl2_bits)) continue;
+    const double df = df_fp64(r2, K);
+    const double fx = df * d.x, fy = df * d.y, fz = df * d.z;
+    red_p<false>(P, i, fx, fy, fz);
+    red_p<false>(P, j, flip_sign(fx), flip_sign(fy), flip_sign(fz));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision
+// ---------------------------------------------------------------------------
+struct MixedConsts {
+  float cl2_lo, cl2_hi;  // r2 (pair units) certainly inside / possibly inside
+  float k_hi, k_lo;      // 1/unit^2 split in two floats (isotropic frames)
+  float u_hi[3], u_lo[3];  // per-axis unit split in two floats (anisotropic)
+  double fscale[3];      // unit * dt per axis (isotropic) or dt (anisotropic)
+  Fp64Consts f64;        // for the rare FP64 cutoff decision
+};
+
+template <bool SOA>
+__global__ void __launch_bounds__(256) k_fixed_image(const Particles P, int n,
+                                                     FixedAxis ax, FixedAxis ay, FixedAxis az,
+                                                     int4* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double3 q = load_q<SOA>(P, i);
+  out[i] = make_int4(to_fixed(q.x, ax), to_fixed(q.y, ay), to_fixed(q.z, az), 0);
+}
+
+template <bool SOA>
+__global__ void __launch_bounds__(256) k_max_abs(const Particles P, int n,
+                                                 unsigned long long* out) {
+  unsigned long long m = 0ull;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double3 q = load_q<SOA>(P, i);
+    const unsigned long long bx = (unsigned long long)dbits(q.x) & 0x7fffffffffffffffull;
+    const unsigned long long by = (unsigned long long)dbits(q.y) & 0x7fffffffffffffffull;
+    const unsigned long long bz = (unsigned long long)dbits(q.z) & 0x7fffffffffffffffull;
+    m = max(m, max(bx, max(by, bz)));
+  }
+  for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(kFullMask, m, off));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// Separation in pair units: fixed units (isotropic frame) or length
+// (anisotropic frame, unit applied per axis as a two-float product).
+template <bool ANISO>
+__device__ __forceinline__ float3 sep_mixed(const int4& a, const int4& b,
+                                            const MixedConsts& k) {
+  float dx = (float)wrap_sub(b.x, a.x);
+  float dy = (float)wrap_sub(b.y, a.y);
+  float dz = (float)wrap_sub(b.z, a.z);
+  if (ANISO) {
+    dx = fmaf(dx, k.u_hi[0], dx * k.u_lo[0]);
+    dy = fmaf(dy, k.u_hi[1], dy * k.u_lo[1]);
+    dz = fmaf(dz, k.u_hi[2], dz * k.u_lo[2]);
+  }
+  return make_float3(dx, dy, dz);
+}
+
+// Pair inside the cutoff?  Decided in FP32 away from the cutoff surface; for
+// the few pairs within a relative 4e-6 of it, recomputed in FP64 from the
+// FP64 positions with the FP64 kernels' expression, so the mixed mask is the
+// FP64 mask.
+template <bool PBC, bool SOA>
+__device__ __forceinline__ bool inside_mixed(float r2, const Particles& P, int i, int j,
+                                             const MixedConsts& k) {
+  if (r2 <= k.cl2_lo) return true;
+  if (!(r2 <= k.cl2_hi)) return false;
+  const double3 d = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, j), k.f64);
+  return !beyond_cutoff(r2_fp64(d), k.f64.cl2_bits);
+}
+
+// df / dt in pair units (24 r^-8 - 48 r^-14, r^-2 rescaled by 1/unit^2)
+template <bool ANISO>
+__device__ __forceinline__ float df_mixed(float r2, const MixedConsts& k) {
+  float inv;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
+  inv = fmaf(inv, fmaf(-r2, inv, 1.0f), inv);
+  if (!ANISO) inv = fmaf(inv, k.k_hi, inv * k.k_lo);
+  const float r6 = inv * inv * inv;
+  return (r6 * inv) * fmaf(-48.0f, r6, 24.0f);
+}
+
+template <int G, bool PBC, bool SOA, bool ANISO>
+__global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const Csr C,
+                                                      const int4* __restrict__ qfix,
+                                                      const MixedConsts K) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / G;
+  const int lane = t & (G - 1);
+  const bool valid = i < C.n;
+  int cnt = 0, k0 = 0;
+  int4 xi = make_int4(0, 0, 0, 0);
+  if (valid) {
+    cnt = __ldg(C.np + i);
+    k0 = __ldg(C.ptr + i);
+    xi = __ldg(qfix + i);
+  }
+  KahanF ax, ay, az;
+  ax.init();
+  ay.init();
+  az.init();
+  for (int k = lane; k < cnt; k += G) {
+    const int j = __ldg(C.list + k0 + k);
+    const float3 d = sep_mixed<ANISO>(xi, __ldg(qfix + j), K);
+    const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+    if (!inside_mixed<PBC, SOA>(r2, P, i, j, K)) continue;
+    const float df = df_mixed<ANISO>(r2, K);
+    ax.add(df * d.x);
+    ay.add(df * d.y);
+    az.add(df * d.z);
+  }
+  float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
+  if (G > 1) {
+    group_reduce_comp<G>(hx, lx);
+    group_reduce_comp<G>(hy, ly);
+    group_reduce_comp<G>(hz, lz);
+  }
+  if (valid && lane == 0)
+    kick_p<SOA>(P, i, widen_f32(hx + lx), widen_f32(hy + ly), widen_f32(hz + lz), K.fscale);
+}
+
+// Mixed scatter: FP32 partial forces per particle in a scratch array
+// (compensation lost on the j side), then one FP64 kick per particle.
+template <int G, bool PBC, bool SOA, bool ANISO>
+__global__ void __launch_bounds__(256) k_scatter_mixed(const Particles P, const Csr C,
+                                                       const int4* __restrict__ qfix,
+                                                       float* __restrict__ facc,
+                                                       const MixedConsts K) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / G;
+  const int lane = t & (G - 1);
+  const bool valid = i < C.n;
+  int cnt = 0, k0 = 0;
+  int4 xi = make_int4(0, 0, 0, 0);
+  if (valid) {
+    cnt = __ldg(C.np + i);
+    k0 = __ldg(C.ptr + i);
+    xi = __ldg(qfix + i);
+  }
+  KahanF ax, ay, az;
+  ax.init();
+  ay.init();
+  az.init();
+  for (int k = lane; k < cnt; k += G) {
+    const int j = __ldg(C.list + k0 + k);
+    const float3 d = sep_mixed<ANISO>(xi, __ldg(qfix + j), K);
+    const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+    if (!inside_mixed<PBC, SOA>(r2, P, i, j, K)) continue;
+    const float df = df_mixed<ANISO>(r2, K);
+    const float fx = df * d.x, fy = df * d.y, fz = df * d.z;
+    ax.add(fx);
+    ay.add(fy);
+    az.add(fz);
+    atomicAdd(facc + 3 * (size_t)j + 0, -fx);
+    atomicAdd(facc + 3 * (size_t)j + 1, -fy);
+    atomicAdd(facc + 3 * (size_t)j + 2, -fz);
+  }
+  float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
+  if (G > 1) {
+    group_reduce_comp<G>(hx, lx);
+    group_reduce_comp<G>(hy, ly);
+    group_reduce_comp<G>(hz, lz);
+  }
+  if (valid && lane == 0) {
+    atomicAdd(facc + 3 * (size_t)i + 0, hx + lx);
+    atomicAdd(facc + 3 * (size_t)i + 1, hy + ly);
+    atomicAdd(facc + 3 * (size_t)i + 2, hz + lz);
+  }
+}
+
+template <bool SOA>
+__global__ void __launch_bounds__(256) k_kick_from_scratch(const Particles P, int n,
+                                                           const float* __restrict__ facc,
+                                                           const MixedConsts K) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  kick_p<SOA>(P, i, widen_f32(facc[3 * (size_t)i]), widen_f32(facc[3 * (size_t)i + 1]),
+              widen_f32(facc[3 * (size_t)i + 2]), K.fscale);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+Fp64Consts make_fp64_consts(const Periodic& box, double dt, double cl2) {
+  Fp64Consts k{};
+  k.c24 = 24.0 * dt;
+  k.c48 = 48.0 * dt;
+  long long b;
+  std::memcpy(&b, &cl2, sizeof b);
+  k.cl2_bits = b;
+  for (int d = 0; d < 3; d++) {
+    k.len[d] = box.on ? box.len[d] : 0.0;
+    const double h = box.on ? box.half[d] : 0.0;
+    std::memcpy(&b, &h, sizeof b);
+    k.half_bits[d] = b;
+  }
+  return k;
+}
+
+void split_float(double v, float& hi, float& lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+MixedConsts make_mixed_consts(const ForceLaunch& L) {
+  MixedConsts k{};
+  k.f64 = make_fp64_consts(L.box, L.dt, L.cl2);
+  // pair units: fixed units (isotropic) or length (anisotropic)
+  const double u2 = L.aniso ? 1.0 : L.unit[0] * L.unit[0];
+  const double cl2u = L.cl2 / u2;
+  k.cl2_lo = (float)(cl2u * (1.0 - 4e-6));
+  k.cl2_hi = (float)(cl2u * (1.0 + 4e-6));
+  split_float(L.aniso ? 1.0 : 1.0 / u2, k.k_hi, k.k_lo);
+  for (int d = 0; d < 3; d++) {
+    split_float(L.unit[d], k.u_hi[d], k.u_lo[d]);
+    k.fscale[d] = L.aniso ? L.dt : L.unit[d] * L.dt;
+  }
+  return k;
+}
+
+template <typename F>
+cudaError_t dispatch_lanes(int lanes, F&& f) {
+  switch (lanes) {
+    case 1: return f(std::integral_constant<int, 1>{});
+    case 2: return f(std::integral_constant<int, 2>{});
+    case 4: return f(std::integral_constant<int, 4>{});
+    case 8: return f(std::integral_constant<int, 8>{});
+    case 16: return f(std::integral_constant<int, 16>{});
+    case 32: return f(std::integral_constant<int, 32>{});
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <bool A, bool B, typename F>
+cudaError_t with_bools(F&& f) {
+  return f(std::integral_constant<bool, A>{}, std::integral_constant<bool, B>{});
+}
+
+template <typename F>
+cudaError_t dispatch_bools(bool a, bool b, F&& f) {
+  if (a) return b ? with_bools<true, true>(f) : with_bools<true, false>(f);
+  return b ? with_bools<false, true>(f) : with_bools<false, false>(f);
+}
+
+}  // namespace
+
+void make_fixed_frame(ForceLaunch& L, double max_abs) {
+  auto axis_for = [](double scale, FixedAxis& ax) {
+    int e;
+    std::frexp(scale, &e);  // scale = f 2^e, f in [0.5, 1)
+    ax.sigma = 64 - e;      // mult = scale 2^sigma in [2^63, 2^64)
+    ax.mult = (unsigned long long)std::ldexp(scale, ax.sigma);
+    ax.pad = 0;
+  };
+  if (L.box.on) {
+    for (int d = 0; d < 3; d++) {
+      const double scale = 4294967296.0 / L.box.len[d];
+      axis_for(scale, L.axis[d]);
+      L.unit[d] = L.box.len[d] / 4294967296.0;
+    }
+    L.aniso = !(L.box.len[0] == L.box.len[1] && L.box.len[1] == L.box.len[2]);
+  } else {
+    // |X| <= 2^30 for every particle keeps |Xj - Xi| < 2^31
+    int e;
+    std::frexp(max_abs > 0 ? max_abs : 1.0, &e);  // max_abs < 2^e
+    const int k = 30 - e;
+    for (int d = 0; d < 3; d++) {
+      axis_for(std::ldexp(1.0, k), L.axis[d]);
+      L.unit[d] = std::ldexp(1.0, -k);
+    }
+    L.aniso = 0;
+  }
+}
+
+cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s) {
+  const int n = L.csr.n;
+  if (n == 0) return cudaSuccess;
+  const int blocks = (n + 255) / 256;
+  if (L.part.soa)
+    k_fixed_image<true><<<blocks, 256, 0, s>>>(L.part, n, L.axis[0], L.axis[1], L.axis[2],
+                                              L.qfix);
+  else
+    k_fixed_image<false><<<blocks, 256, 0, s>>>(L.part, n, L.axis[0], L.axis[1], L.axis[2],
+                                               L.qfix);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_max_abs(const Particles& part, int n, double* out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
+  if (e != cudaSuccess || n == 0) return e;
+  int blocks = (n + 255) / 256;
+  if (blocks > 1024) blocks = 1024;
+  auto* o = reinterpret_cast<unsigned long long*>(out);
+  if (part.soa) k_max_abs<true><<<blocks, 256, 0, s>>>(part, n, o);
+  else k_max_abs<false><<<blocks, 256, 0, s>>>(part, n, o);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
+  const int n = L.csr.n;
+  if (n == 0) return cudaSuccess;
+  const int block = L.block;
+  const long long threads = (long long)n * L.lanes;
+  const int blocks = (int)((threads + block - 1) / block);
+  const bool pbc = L.box.on != 0, soa = L.part.soa != 0;
+  if (L.precision == LJ_PREC_FP64) {
+    const Fp64Consts K = make_fp64_consts(L.box, L.dt, L.cl2);
+    const bool gather = L.method == LJ_METHOD_GATHER_FULL;
+    return dispatch_lanes(L.lanes, [&](auto g) {
+      return dispatch_bools(pbc, soa, [&](auto P, auto S) {
+        constexpr int G = decltype(g)::value;
+        if (gather)
+          k_gather_fp64<G, P.value, S.value><<<blocks, block, 0, s>>>(L.part, L.csr, K);
+        else
+          k_scatter_fp64<G, P.value, S.value><<<blocks, block, 0, s>>>(L.part, L.csr, K);
+        return cudaGetLastError();
+      });
+    });
+  }
+  const MixedConsts K = make_mixed_consts(L);
+  const bool gather = L.method == LJ_METHOD_GATHER_FULL;
+  if (!gather) {
+    cudaError_t e = cudaMemsetAsync(L.fscratch, 0, sizeof(float) * 3 * (size_t)n, s);
+    if (e != cudaSuccess) return e;
+  }
+  cudaError_t e = dispatch_lanes(L.lanes, [&](auto g) {
+    return dispatch_bools(pbc, soa, [&](auto P, auto S) {
+      constexpr int G = decltype(g)::value;
+      if (gather) {
+        if (L.aniso)
+          k_gather_mixed<G, P.value, S.value, true>
+              <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, K);
+        else
+          k_gather_mixed<G, P.value, S.value, false>
+              <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, K);
+      } else {
+        if (L.aniso)
+          k_scatter_mixed<G, P.value, S.value, true>
+              <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, L.fscratch, K);
+        else
+          k_scatter_mixed<G, P.value, S.value, false>
+              <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, L.fscratch, K);
+      }
+      return cudaGetLastError();
+    });
+  });
+  if (e != cudaSuccess || gather) return e;
+  const int kb = (n + 255) / 256;
+  if (soa) k_kick_from_scratch<true><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
+  else k_kick_from_scratch<false><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_force_pairs(const Particles& part, int n, const int32_t* ip,
+                               const int32_t* jp, int64_t npairs, const Periodic& box,
+                               double dt, double cl2, cudaStream_t s) {
+  (void)n;
+  if (npairs == 0) return cudaSuccess;
+  const Fp64Consts K = make_fp64_consts(box, dt, cl2);
+  long long blocks = (npairs + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  if (box.on) k_pairs_fp64<true><<<(int)blocks, 256, 0, s>>>(part, ip, jp, npairs, K);
+  else k_pairs_fp64<false><<<(int)blocks, 256, 0, s>>>(part, ip, jp, npairs, K);
+  return cudaGetLastError();
+}
+
+}  // namespace ljg

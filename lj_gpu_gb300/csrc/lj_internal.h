@@ -1,0 +1,93 @@
+// lj_internal.h -- declarations shared between the C-ABI layer and the CUDA
+// translation units.  Not part of the public interface.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lj_common.cuh"
+
+namespace ljg {
+
+// Where q / p live and how they are laid out.
+struct Particles {
+  int soa;              // 0: AoS double[n][4], 1: three arrays
+  const double* q;      // AoS
+  double* p;            // AoS
+  const double* qx;     // SoA
+  const double* qy;
+  const double* qz;
+  double* px;
+  double* py;
+  double* pz;
+};
+
+// A device CSR list.
+struct Csr {
+  int n;
+  int64_t entries;
+  const int32_t* np;
+  const int32_t* ptr;
+  const int32_t* list;
+};
+
+struct Periodic {
+  int on;
+  double len[3];
+  double half[3];
+};
+
+// Everything one force launch needs.
+struct ForceLaunch {
+  Particles part;
+  Csr csr;
+  Periodic box;
+  double dt;
+  double cl2;
+  int precision;   // LJ_PREC_*
+  int method;      // LJ_METHOD_GATHER_FULL / LJ_METHOD_SCATTER_HALF (resolved)
+  int lanes;       // 1..32
+  int block;       // threads per block
+  // mixed precision only
+  int4* qfix;      // n entries, written by the fixed-image pass
+  float* fscratch; // 3 n floats (scatter-half mixed only)
+  FixedAxis axis[3];
+  double unit[3];  // length per fixed unit on each axis
+  int aniso;       // axes with different units
+};
+
+// Fills axis[] / unit[] / aniso for a periodic box, or for an open box from
+// the largest coordinate magnitude (max_abs).
+void make_fixed_frame(ForceLaunch& L, double max_abs);
+
+// Launchers (return cudaError_t of the launch)
+cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s);
+cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s);
+cudaError_t launch_force_pairs(const Particles& part, int n, const int32_t* ip,
+                               const int32_t* jp, int64_t npairs, const Periodic& box,
+                               double dt, double cl2, cudaStream_t s);
+// Largest |coordinate| over all particles, written to *out (device double).
+cudaError_t launch_max_abs(const Particles& part, int n, double* out, cudaStream_t s);
+
+// ---- list kernels (lj_list.cu) ----
+// Validation; writes into err[0] a nonzero code and err[1] the first bad
+// index (the smallest is kept).
+cudaError_t launch_validate_csr(const Csr& c, int32_t* err, cudaStream_t s);
+// Exclusive scan of n int32 counts into out[0..n] (out[n] = total, int64).
+cudaError_t launch_scan_counts(const int32_t* counts, int n, int64_t* out, void* tmp,
+                               size_t tmp_bytes, cudaStream_t s);
+size_t scan_tmp_bytes(int n);
+// Full list from a half list: counts, offsets, fill, per-row sort.
+cudaError_t launch_full_from_half_count(const Csr& half, int32_t* deg, cudaStream_t s);
+cudaError_t launch_full_from_half_fill(const Csr& half, const int64_t* off, int32_t* cursor,
+                                       int32_t* full_list, cudaStream_t s);
+// Rows [off[i], off[i+1]) of `in` sorted ascending (stable) into `out`.
+cudaError_t launch_sort_rows_into(const int64_t* off, int n, const int32_t* in, int32_t* out,
+                                  cudaStream_t s);
+cudaError_t launch_offsets_to_ptr(const int64_t* off, int n, int32_t* ptr, int32_t* np,
+                                  int32_t* max_row, cudaStream_t s);
+// (i, j) pairs with non-decreasing i into CSR rows: counts per i.
+cudaError_t launch_pairs_count(const int32_t* ip, int64_t npairs, int n, int32_t* cnt,
+                               int32_t* err, cudaStream_t s);
+
+}  // namespace ljg

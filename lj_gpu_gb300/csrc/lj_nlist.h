@@ -1,0 +1,47 @@
+// lj_nlist.h -- cell grid and launchers of the on-device neighbour build.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <cuda_runtime.h>
+
+namespace ljg {
+
+struct CellGrid {
+  int nc[3];
+  int ncells;
+  int periodic;
+  double lo[3];     // grid origin
+  double inv_w[3];  // cells per unit length
+};
+
+struct BuildArgs {
+  const double* q;  // AoS double4, device
+  int n;
+  CellGrid grid;
+  double search;
+  double box[3];
+  double unit[3];   // length per fixed unit
+  int aniso;
+  const int64_t* start;
+  const int32_t* order;
+  const int4* cq;
+  const int32_t* cell;
+  int want_half, want_full;
+  int32_t* cnt_half;
+  int32_t* cnt_full;
+  const int64_t* off_half;
+  const int64_t* off_full;
+  int32_t* out_half;
+  int32_t* out_full;
+};
+
+double key_to_double(unsigned long long k);
+cudaError_t launch_minmax(const double* q, int n, unsigned long long* out6, cudaStream_t s);
+cudaError_t launch_bin(const double* q, int n, const CellGrid& g, int32_t* cell, int32_t* count,
+                       cudaStream_t s);
+cudaError_t launch_place(const int32_t* cell, int n, const int64_t* start, int32_t* cursor,
+                         int ncells, const int4* qfix, int32_t* order, int4* cq, cudaStream_t s);
+cudaError_t launch_walk(const BuildArgs& a, bool fill, cudaStream_t s);
+
+}  // namespace ljg

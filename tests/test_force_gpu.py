@@ -1,0 +1,336 @@
+"""Parity of the CUDA force path with the oracle, through the C ABI.
+
+FP64 path: <= 1e-12 relative per particle (norm of the 3-vector) against the
+oracle's force_sorted (cpu_ref/force_aos.cpp:192-224 restated).
+Mixed path: one force evaluation against the FP64 oracle with the tolerances
+written in MIXED_TOL.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+# one mixed force evaluation vs FP64: max |dF_i| / rms|F| and ||dF|| / ||F||
+MIXED_TOL = {"max_rel_rms": 1e-5, "global_rel": 2e-6}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def dev(a):
+    torch = _torch()
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    _torch().cuda.synchronize()
+    return t.cpu().numpy()
+
+
+SYSTEMS = {
+    # name: (builder, box)
+    "open_rho0.5": lambda: (ol.init_reference(0.5, 10.0), None),
+    "open_rho1": lambda: (ol.init_reference(1.0, 8.0), None),
+    "pbc_rho1": lambda: ol.init_fcc_periodic(6, 1.0, 0.05, seed=20240601),
+    "pbc_rho0.5": lambda: ol.init_fcc_periodic(5, 0.5, 0.05, seed=99),
+}
+
+
+def system(name):
+    q, box = SYSTEMS[name]()
+    half = ol.build_list(q, 3.3, box=box)
+    return q, box, half
+
+
+def run_engine(engine, q, half, box, precision, method, layout, calls, dt, lanes=0, ctx=None):
+    own = ctx is None
+    ctx = ctx or engine.Context(0)
+    try:
+        npp, ptr, lst = half
+        ctx.set_list_csr(dev(npp), dev(ptr), dev(lst), kind="half")
+        opts = engine.make_opts(dt=dt, cl2=9.0, box=box, precision=precision, method=method,
+                                lanes=lanes)
+        if layout == "aos":
+            qd, pd = dev(q), dev(np.zeros_like(q))
+            for _ in range(calls):
+                ctx.force_aos(qd, pd, opts)
+            return host(pd)
+        qs = [dev(q[:, d].copy()) for d in range(3)]
+        ps = [dev(np.zeros(q.shape[0])) for _ in range(3)]
+        for _ in range(calls):
+            ctx.force_soa(*qs, *ps, opts)
+        out = np.zeros_like(q)
+        for d in range(3):
+            out[:, d] = host(ps[d])
+        return out
+    finally:
+        if own:
+            ctx.close()
+
+
+def oracle_p(q, half, box, calls, dt):
+    return ol.force_sorted_aos(q, np.zeros_like(q), *half, dt=dt, box=box, calls=calls)
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+@pytest.mark.parametrize("method", ["scatter", "gather"])
+@pytest.mark.parametrize("layout", ["aos", "soa"])
+def test_fp64_matches_oracle(engine, name, method, layout):
+    q, box, half = system(name)
+    dt = 0.001 if box is None else 0.005
+    ref = oracle_p(q, half, box, 10, dt)
+    got = run_engine(engine, q, half, box, "fp64", method, layout, 10, dt)
+    e = ol.rel_errors(got, ref)
+    assert e["max_rel"] <= FP64_TOL, e
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32])
+def test_fp64_every_lane_width(engine, lanes):
+    q, box, half = system("pbc_rho1")
+    ref = oracle_p(q, half, box, 1, 0.005)
+    for method in ("scatter", "gather"):
+        got = run_engine(engine, q, half, box, "fp64", method, "aos", 1, 0.005, lanes=lanes)
+        assert ol.rel_errors(got, ref)["max_rel"] <= FP64_TOL, (method, lanes)
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+@pytest.mark.parametrize("method", ["gather", "scatter"])
+@pytest.mark.parametrize("layout", ["aos", "soa"])
+def test_mixed_error_bounds(engine, name, method, layout):
+    q, box, half = system(name)
+    dt = 0.005
+    ref = oracle_p(q, half, box, 1, dt)
+    got = run_engine(engine, q, half, box, "mixed", method, layout, 1, dt)
+    e = ol.rel_errors(got, ref)
+    for k, tol in MIXED_TOL.items():
+        assert e[k] <= tol, (k, e)
+
+
+@pytest.mark.parametrize("lanes", [1, 4, 8, 16, 32])
+def test_mixed_every_lane_width(engine, lanes):
+    q, box, half = system("pbc_rho1")
+    ref = oracle_p(q, half, box, 1, 0.005)
+    got = run_engine(engine, q, half, box, "mixed", "gather", "aos", 1, 0.005, lanes=lanes)
+    e = ol.rel_errors(got, ref)
+    assert e["max_rel_rms"] <= MIXED_TOL["max_rel_rms"], e
+
+
+def test_mixed_anisotropic_box(engine):
+    q, L = ol.init_fcc_periodic(6, 1.0, 0.05, seed=5)
+    box = np.array([L, L * 1.25, L * 0.9])
+    q = q.copy()
+    q[:, 1] *= 1.25
+    q[:, 2] *= 0.9
+    half = ol.build_list(q, 3.3, box=box)
+    ref = oracle_p(q, half, box, 1, 0.005)
+    for method in ("gather", "scatter"):
+        got = run_engine(engine, q, half, box, "mixed", method, "aos", 1, 0.005)
+        e = ol.rel_errors(got, ref)
+        assert e["max_rel_rms"] <= MIXED_TOL["max_rel_rms"], (method, e)
+        got64 = run_engine(engine, q, half, box, "fp64", method, "aos", 1, 0.005)
+        assert ol.rel_errors(got64, ref)["max_rel"] <= FP64_TOL
+
+
+def test_cutoff_boundary_pairs_follow_fp64_mask(engine):
+    """Isolated pairs at r2 within a few ulp of CL2: the mixed mask must be the
+    FP64 mask (a toggled pair would change F by |f(rc)| ~ 1e-2, i.e. 100 %)."""
+    rng = np.random.default_rng(1)
+    g = 8  # 8^3 pair sites 9 apart: only the planted pairs interact
+    centres = np.stack(np.meshgrid(*[np.arange(g) * 9.0] * 3, indexing="ij"), -1).reshape(-1, 3)
+    m = centres.shape[0]
+    dirs = rng.normal(size=(m, 3))
+    dirs /= np.linalg.norm(dirs, axis=1)[:, None]
+    r = 3.0 * (1 + rng.integers(-6, 7, size=m) * 2.0 ** -52)
+    q = np.zeros((2 * m, 4))
+    q[0::2, :3] = centres
+    q[1::2, :3] = centres + dirs * r[:, None]
+    half = ol.build_list(q, 3.3)
+    assert len(half[2]) == m
+    ref64 = run_engine(engine, q, half, None, "fp64", "gather", "aos", 1, 0.005)
+    inside = np.linalg.norm(ref64[:, :3], axis=1) > 0
+    assert 0 < inside.sum() < 2 * m  # both sides of the surface are exercised
+    for method in ("gather", "scatter"):
+        got = run_engine(engine, q, half, None, "mixed", method, "aos", 1, 0.005)
+        assert np.array_equal(np.linalg.norm(got[:, :3], axis=1) > 0, inside), method
+        assert ol.rel_errors(got, ref64)["max_rel"] <= 1e-5, method
+
+
+def test_stateless_drop_in(engine):
+    q, box, half = system("open_rho1")
+    full = ol.build_list(q, 3.3, full=True)
+    ref = oracle_p(q, half, None, 3, 0.001)
+    for kind, (npp, ptr, lst) in (("half", half), ("full", full)):
+        qd, pd = dev(q), dev(np.zeros_like(q))
+        for _ in range(3):
+            engine.force_csr_fp64_aos(qd, pd, 0.001, 9.0, dev(lst), dev(npp), dev(ptr),
+                                      kind=kind)
+        assert ol.rel_errors(host(pd), ref)["max_rel"] <= FP64_TOL, kind
+
+
+def test_force_pair_entry(engine, fixture_rho05):
+    f = fixture_rho05
+    qd, pd = dev(f["q"]), dev(np.zeros_like(f["q"]))
+    ii, jj = dev(f["i"]), dev(f["j"])
+    for _ in range(100):
+        engine.force_pairs_fp64_aos(qd, pd, 0.001, 9.0, ii, jj)
+    assert ol.rel_errors(host(pd), f["p_aos_pair"])["max_rel"] <= FP64_TOL
+
+
+@pytest.mark.parametrize("fx", ["fixture_rho05", "fixture_rho1"])
+def test_reference_fixtures(engine, fx, request):
+    """Engine vs the reference's own cpu_ref outputs (100 calls, dt = 0.001)."""
+    f = request.getfixturevalue(fx)
+    half = (f["np"], f["ptr"], f["list"])
+    for layout, key in (("aos", "p_aos_sorted"), ("soa", "p_soa_sorted")):
+        for method in ("scatter", "gather"):
+            got = run_engine(engine, f["q"], half, None, "fp64", method, layout, 100, 0.001)
+            assert ol.rel_errors(got, f[key])["max_rel"] <= FP64_TOL, (layout, method)
+
+
+def test_full_list_expansion_is_reference_full_list(engine):
+    q, box, half = system("pbc_rho0.5")
+    full = ol.build_list(q, 3.3, box=box, full=True)
+    with engine.Context(0) as ctx:
+        ctx.set_list_csr(dev(half[0]), dev(half[1]), dev(half[2]), kind="half")
+        got = ctx.get_list_csr("full")
+        for a, b in zip(got, full):
+            assert np.array_equal(a, b)
+        back = ctx.get_list_csr("half")
+        for a, b in zip(back, half):
+            assert np.array_equal(a, b)
+        assert ctx.list_info("full")[2] == int(full[0].max())
+
+
+def test_set_pairs_is_sortpair(engine, fixture_rho1):
+    f = fixture_rho1
+    n = f["q"].shape[0]
+    with engine.Context(0) as ctx:
+        for where in ("device", "host"):
+            ii, jj = (dev(f["i"]), dev(f["j"])) if where == "device" else (f["i"], f["j"])
+            ctx.set_list_pairs(n, ii, jj)
+            got = ctx.get_list_csr("half")
+            for a, b in zip(got, (f["np"], f["ptr"], f["list"])):
+                assert np.array_equal(a, b), where
+        # unsorted pair array: rows keep pair-array order (stable), as sortpair
+        rng = np.random.default_rng(0)
+        perm = rng.permutation(len(f["i"]))
+        ii, jj = f["i"][perm].copy(), f["j"][perm].copy()
+        order = np.argsort(ii, kind="stable")
+        for src in ((dev(ii), dev(jj)), (ii, jj)):
+            ctx.set_list_pairs(n, *src)
+            npp, ptr, lst = ctx.get_list_csr("half")
+            assert np.array_equal(npp, f["np"]) and np.array_equal(lst, jj[order])
+
+
+def test_bad_lists_are_rejected(engine):
+    q, box, half = system("open_rho0.5")
+    npp, ptr, lst = half
+    n = len(npp)
+    with engine.Context(0) as ctx:
+        with pytest.raises(engine.LJError) as e:
+            ctx.force_aos(dev(q), dev(np.zeros_like(q)), engine.make_opts())
+        assert e.value.status == engine.LJ_ERR_NO_LIST
+        bad = lst.copy()
+        bad[17] = n  # out of range j
+        with pytest.raises(engine.LJError) as e:
+            ctx.set_list_csr(dev(npp), dev(ptr), dev(bad))
+        assert e.value.status == engine.LJ_ERR_BAD_LIST and "sorted_list[17]" in str(e.value)
+        badn = npp.copy()
+        badn[3] = -1
+        with pytest.raises(engine.LJError) as e:
+            ctx.set_list_csr(badn, ptr, lst)  # host arrays
+        assert e.value.status == engine.LJ_ERR_BAD_LIST
+        badp = ptr.copy()
+        badp[0] = len(lst) - 1  # row 0 (np > 1) runs past the end
+        with pytest.raises(engine.LJError) as e:
+            ctx.set_list_csr(dev(npp), dev(badp), dev(lst))
+        assert e.value.status == engine.LJ_ERR_BAD_LIST
+        ctx.set_list_csr(dev(npp), dev(ptr), dev(lst))
+        with pytest.raises(engine.LJError) as e:  # n mismatch
+            ctx.force_aos(dev(q[:-1]), dev(np.zeros_like(q[:-1])), engine.make_opts())
+        assert e.value.status == engine.LJ_ERR_INVALID_ARGUMENT
+        with pytest.raises(engine.LJError):  # cutoff larger than half the box
+            ctx.force_aos(dev(q), dev(np.zeros_like(q)), engine.make_opts(box=5.0))
+
+
+def test_edge_cases(engine):
+    rng = np.random.default_rng(4)
+    # empty system, rows with np = 0, a single long row (> 1024 partners)
+    with engine.Context(0) as ctx:
+        e0 = np.zeros(0, np.int32)
+        ctx.set_list_csr(e0, e0, e0, kind="half")
+        ctx.force_aos(dev(np.zeros((0, 4))), dev(np.zeros((0, 4))), engine.make_opts())
+    n = 3000
+    q = np.zeros((n, 4))
+    q[0, :3] = 20.0
+    q[1:, :3] = 20.0 + rng.normal(scale=1.6, size=(n - 1, 3))
+    npp = np.zeros(n, np.int32)
+    npp[0] = n - 1
+    ptr = np.full(n, n - 1, np.int32)
+    ptr[0] = 0
+    lst = np.arange(1, n, dtype=np.int32)
+    half = (npp, ptr, lst)
+    ref = oracle_p(q, half, None, 1, 0.001)
+    for prec in ("fp64", "mixed"):
+        for method in ("scatter", "gather"):
+            got = run_engine(engine, q, half, None, prec, method, "aos", 1, 0.001)
+            e = ol.rel_errors(got, ref)
+            if prec == "fp64":
+                assert e["max_rel"] <= FP64_TOL, (method, e)
+            else:
+                assert e["max_rel_rms"] <= 1e-4, (method, e)
+
+
+def test_measure_host_buffers(engine, fixture_rho05):
+    f = fixture_rho05
+    with engine.Context(0) as ctx:
+        ctx.set_list_csr(f["np"], f["ptr"], f["list"])  # host list, re-uploaded per measure
+        p = np.zeros_like(f["q"])
+        t_all, t_calc = ctx.measure_aos(np.ascontiguousarray(f["q"]), p, engine.make_opts(),
+                                        calls=100)
+        assert t_all >= t_calc > 0
+        assert ol.rel_errors(p, f["p_aos_sorted"])["max_rel"] <= FP64_TOL
+
+
+def test_golden_print_density05(engine):
+    """The reference's headline case end to end on the GPU: N = 62,500, 100 calls."""
+    q = ol.init_reference(0.5, 50.0)
+    half = ol.build_list(q, 3.3)
+    got = run_engine(engine, q, half, None, "fp64", "scatter", "aos", 100, 0.001)
+    gold = [[float(v) for v in r.split()] for r in
+            (ol.ROOT / "tests" / "golden" / "ref_density0.5.dat").read_text().split("\n")[:10]]
+    rows = [[float(v) for v in r.split()] for r in ol.golden_rows(got)]
+    assert np.abs(np.array(rows) - np.array(gold)).max() <= 1.5e-10
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_device_list_build_is_reference_list(engine, name):
+    q, box, half = system(name)
+    full = ol.build_list(q, 3.3, box=box, full=True)
+    with engine.Context(0) as ctx:
+        ctx.build_list(dev(q), 3.3, box=box)
+        for kind, want in (("half", half), ("full", full)):
+            got = ctx.get_list_csr(kind)
+            for a, b in zip(got, want):
+                assert np.array_equal(a, b), kind
+        # and a build of one kind only
+        ctx.build_list(dev(q), 3.3, box=box, kinds=("full",))
+        assert ctx.list_info("half")[0] == 0
+        for a, b in zip(ctx.get_list_csr("full"), full):
+            assert np.array_equal(a, b)
+
+
+def test_device_list_build_large_periodic(engine):
+    """The headline system: 108,000 particles, rho = 0.5, L = 60."""
+    q, L = ol.init_fcc_periodic(30, 0.5, 0.05, seed=20240601)
+    half = ol.build_list(q, 3.3, box=L)
+    with engine.Context(0) as ctx:
+        ctx.build_list(dev(q), 3.3, box=L)
+        got = ctx.get_list_csr("half")
+        for a, b in zip(got, half):
+            assert np.array_equal(a, b)
