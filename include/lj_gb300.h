@@ -70,8 +70,11 @@ typedef struct lj_force_opts {
   int32_t precision;  /* LJ_PREC_FP64 or LJ_PREC_MIXED                        */
   int32_t method;     /* LJ_METHOD_*                                          */
   int32_t lanes;      /* lanes per i-particle, 0 = default, else 1,2,4,..,32  */
-  int32_t block;      /* threads per block, 0 = default, else 64..1024        */
-  int32_t reserved[3];
+  int32_t block;      /* threads per block, 0 = default, else 64..256         */
+  int32_t kernel;     /* kernel generation: 0 = default, 1 = simple strided,
+                         2 = unrolled / compacted (see lj_force.cu)           */
+  int32_t unroll;     /* entries per lane in flight (kernel 2), 0 = default   */
+  int32_t reserved;
 } lj_force_opts;
 
 /* dt = 0.001, cl2 = 9.0 (cpu_ref/force_aos.cpp:14,31-33), open box, FP64, auto */

@@ -53,12 +53,14 @@ class ForceOpts(C.Structure):
         ("method", C.c_int32),
         ("lanes", C.c_int32),
         ("block", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("kernel", C.c_int32),
+        ("unroll", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
 def make_opts(dt=0.001, cl2=9.0, box=None, precision="fp64", method="auto", lanes=0,
-              block=0) -> ForceOpts:
+              block=0, kernel=0, unroll=0) -> ForceOpts:
     o = ForceOpts()
     o.dt, o.cl2 = float(dt), float(cl2)
     if box is not None:
@@ -68,6 +70,7 @@ def make_opts(dt=0.001, cl2=9.0, box=None, precision="fp64", method="auto", lane
     o.precision = _PRECISION[precision] if isinstance(precision, str) else int(precision)
     o.method = _METHOD[method] if isinstance(method, str) else int(method)
     o.lanes, o.block = int(lanes), int(block)
+    o.kernel, o.unroll = int(kernel), int(unroll)
     return o
 
 

@@ -150,15 +150,22 @@ Periodic make_periodic(const lj_force_opts* o) {
 }
 
 // Default lanes per i-particle: chosen from the average row length so that a
-// group takes 4-8 strided steps per row.
-int default_lanes(int precision, int method, int64_t entries, int n) {
-  (void)precision;
+// group takes a few strided steps per row (kernel 2 moves `unroll` entries
+// per lane and step, so it uses narrower groups).
+int default_lanes(int precision, int method, int kernel, int64_t entries, int n) {
   (void)method;
   const double avg = n > 0 ? (double)entries / n : 0.0;
+  if (kernel == 2 && precision == LJ_PREC_MIXED) return avg <= 48 ? 2 : (avg <= 96 ? 4 : 8);
   if (avg <= 12) return 2;
   if (avg <= 24) return 4;
   if (avg <= 96) return 8;
   return 16;
+}
+
+int default_kernel(int precision, int method) {
+  (void)precision;
+  (void)method;
+  return 1;
 }
 
 int copy_in(lj_ctx* ctx, int32_t* dst, const int32_t* src, size_t count, int where) {
@@ -305,10 +312,16 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
   L.cl2 = o->cl2;
   L.precision = o->precision;
   L.method = method;
-  L.lanes = o->lanes ? o->lanes : default_lanes(o->precision, method, l.entries, l.n);
+  L.kernel = o->kernel ? o->kernel : default_kernel(o->precision, method);
+  if (L.kernel == 2 && method == LJ_METHOD_SCATTER_HALF) L.kernel = 1;  // no compacted scatter
+  L.unroll = o->unroll ? o->unroll : 4;
+  if (L.kernel == 2 && !(L.unroll == 2 || L.unroll == 4 || L.unroll == 8))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be 2, 4 or 8");
+  L.lanes = o->lanes ? o->lanes : default_lanes(o->precision, method, L.kernel, l.entries, l.n);
   L.block = o->block ? o->block : 128;
   if (n == 0) return LJ_OK;
-  if (o->precision == LJ_PREC_MIXED) {
+  const bool fixed = o->precision == LJ_PREC_MIXED || L.kernel == 2;
+  if (fixed) {
     LJ_CUDA(ctx, ctx->qfix.ensure((size_t)n), "alloc");
     L.qfix = ctx->qfix.ptr;
     double max_abs = 0.0;
@@ -322,7 +335,7 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
         return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "non-finite position");
     }
     make_fixed_frame(L, max_abs);
-    if (method == LJ_METHOD_SCATTER_HALF) {
+    if (o->precision == LJ_PREC_MIXED && method == LJ_METHOD_SCATTER_HALF) {
       LJ_CUDA(ctx, ctx->fscratch.ensure(3 * (size_t)n), "alloc");
       L.fscratch = ctx->fscratch.ptr;
     }
@@ -608,6 +621,7 @@ int lj_force_csr_fp64_aos(const double* q, double* p, int32_t n, double dt, doub
   L.method = kind == LJ_LIST_FULL ? LJ_METHOD_GATHER_FULL : LJ_METHOD_SCATTER_HALF;
   L.lanes = 8;
   L.block = 128;
+  L.kernel = 1;
   return launch_force(L, static_cast<cudaStream_t>(stream)) == cudaSuccess ? LJ_OK
                                                                           : LJ_ERR_CUDA;
 }

@@ -341,6 +341,153 @@ __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const C
     kick_p<SOA>(P, i, widen_f32(hx + lx), widen_f32(hy + ly), widen_f32(hz + lz), K.fscale);
 }
 
+// Unrolled mixed gather (kernel 2).  The row loop runs to the longest row of
+// the warp, so every lane takes part in every iteration (no divergence, warp
+// votes are safe); each lane issues U independent index loads and U position
+// gathers before any arithmetic, which keeps U x 32 gathers in flight per
+// warp.  Pairs outside the cutoff are masked with a select, not a branch.  The
+// U terms of one step are summed in FP32 and the step sum enters the Kahan
+// accumulator, so compensation costs 12/U operations per pair.
+template <int G, int U, bool PBC, bool SOA, bool ANISO>
+__global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const Csr C,
+                                                        const int4* __restrict__ qfix,
+                                                        const MixedConsts K) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / G;
+  const int lane = t & (G - 1);
+  const bool valid = i < C.n;
+  int cnt = 0, k0 = 0;
+  int4 xi = make_int4(0, 0, 0, 0);
+  if (valid) {
+    cnt = __ldg(C.np + i);
+    k0 = __ldg(C.ptr + i);
+    xi = __ldg(qfix + i);
+  }
+  int cmax = cnt;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
+  KahanF ax, ay, az;
+  ax.init();
+  ay.init();
+  az.init();
+  for (int base = 0; base < cmax; base += G * U) {
+    int jj[U];
+    bool ok[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = base + lane + u * G;
+      ok[u] = k < cnt;
+      jj[u] = ok[u] ? __ldg(C.list + k0 + k) : 0;
+    }
+    int4 xj[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    unsigned border = 0u;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
+      const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+      const bool in = ok[u] && r2 <= K.cl2_lo;
+      if (ok[u] && r2 > K.cl2_lo && r2 <= K.cl2_hi) border |= 1u << u;
+      float df = df_mixed<ANISO>(r2, K);
+      df = in ? df : 0.0f;
+      sx = fmaf(df, d.x, sx);
+      sy = fmaf(df, d.y, sy);
+      sz = fmaf(df, d.z, sz);
+    }
+    if (__any_sync(kFullMask, border != 0u)) {
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (!(border & (1u << u))) continue;
+        const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, jj[u]), K.f64);
+        if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
+        const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
+        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+        const float df = df_mixed<ANISO>(r2, K);
+        sx = fmaf(df, d.x, sx);
+        sy = fmaf(df, d.y, sy);
+        sz = fmaf(df, d.z, sz);
+      }
+    }
+    ax.add(sx);
+    ay.add(sy);
+    az.add(sz);
+  }
+  float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
+  if (G > 1) {
+    group_reduce_comp<G>(hx, lx);
+    group_reduce_comp<G>(hy, ly);
+    group_reduce_comp<G>(hz, lz);
+  }
+  if (valid && lane == 0)
+    kick_p<SOA>(P, i, widen_f32(hx + lx), widen_f32(hy + ly), widen_f32(hz + lz), K.fscale);
+}
+
+// Compacted FP64 gather (kernel 2).  One warp per row.  Candidates are
+// screened in FP32 from the fixed-point image (cheap), the survivors (inside
+// the cutoff or within 4e-6 of it) are queued in shared memory, and the FP64
+// arithmetic runs on full batches of 32 queued pairs, so the FP64 pipe --
+// the bottleneck of this path on GB300 -- does not idle on pairs beyond the
+// cutoff or on the ragged end of a strided row.  The exact FP64 mask is
+// applied to every queued pair.
+constexpr int kCompactWarps = 4;
+
+template <bool PBC, bool SOA>
+__device__ __forceinline__ void fp64_pair_acc(const Particles& P, const double3& qi, int j,
+                                              const Fp64Consts& k, double& fx, double& fy,
+                                              double& fz) {
+  const double3 d = sep_fp64<PBC>(qi, load_q<SOA>(P, j), k);
+  const double r2 = r2_fp64(d);
+  if (beyond_cutoff(r2, k.cl2_bits)) return;
+  const double df = df_fp64(r2, k);
+  fx = fma(df, d.x, fx);
+  fy = fma(df, d.y, fy);
+  fz = fma(df, d.z, fz);
+}
+
+template <bool PBC, bool SOA, bool ANISO>
+__global__ void __launch_bounds__(32 * kCompactWarps) k_gather_fp64_c(
+    const Particles P, const Csr C, const int4* __restrict__ qfix, const MixedConsts K) {
+  __shared__ int queue[kCompactWarps][64];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kCompactWarps + w;
+  if (i >= C.n) return;  // warp-uniform
+  int* q = queue[w];
+  const int cnt = __ldg(C.np + i), k0 = __ldg(C.ptr + i);
+  const int4 xi = __ldg(qfix + i);
+  const double3 qi = load_q<SOA>(P, i);
+  const unsigned lt = (1u << lane) - 1u;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  int qn = 0;
+  for (int base = 0; base < cnt; base += 32) {
+    const int k = base + lane;
+    bool cand = false;
+    int j = 0;
+    if (k < cnt) {
+      j = __ldg(C.list + k0 + k);
+      const float3 d = sep_mixed<ANISO>(xi, __ldg(qfix + j), K);
+      cand = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x)) <= K.cl2_hi;
+    }
+    const unsigned b = __ballot_sync(kFullMask, cand);
+    if (cand) q[qn + __popc(b & lt)] = j;
+    qn += __popc(b);
+    __syncwarp();
+    if (qn >= 32) {
+      fp64_pair_acc<PBC, SOA>(P, qi, q[lane], K.f64, fx, fy, fz);
+      __syncwarp();
+      if (lane < qn - 32) q[lane] = q[lane + 32];
+      qn -= 32;
+      __syncwarp();
+    }
+  }
+  if (lane < qn) fp64_pair_acc<PBC, SOA>(P, qi, q[lane], K.f64, fx, fy, fz);
+  fx = group_reduce_fp64<32>(fx);
+  fy = group_reduce_fp64<32>(fy);
+  fz = group_reduce_fp64<32>(fz);
+  if (lane == 0) add_p<SOA>(P, i, fx, fy, fz);
+}
+
 // Mixed scatter: FP32 partial forces per particle in a scratch array
 // (compensation lost on the j side), then one FP64 kick per particle.
 template <int G, bool PBC, bool SOA, bool ANISO>
@@ -525,9 +672,22 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
   const long long threads = (long long)n * L.lanes;
   const int blocks = (int)((threads + block - 1) / block);
   const bool pbc = L.box.on != 0, soa = L.part.soa != 0;
+  const bool gather = L.method == LJ_METHOD_GATHER_FULL;
   if (L.precision == LJ_PREC_FP64) {
+    if (gather && L.kernel == 2) {
+      const MixedConsts K = make_mixed_consts(L);
+      const int cb = (n + kCompactWarps - 1) / kCompactWarps;
+      return dispatch_bools(pbc, soa, [&](auto P, auto S) {
+        if (L.aniso)
+          k_gather_fp64_c<P.value, S.value, true>
+              <<<cb, 32 * kCompactWarps, 0, s>>>(L.part, L.csr, L.qfix, K);
+        else
+          k_gather_fp64_c<P.value, S.value, false>
+              <<<cb, 32 * kCompactWarps, 0, s>>>(L.part, L.csr, L.qfix, K);
+        return cudaGetLastError();
+      });
+    }
     const Fp64Consts K = make_fp64_consts(L.box, L.dt, L.cl2);
-    const bool gather = L.method == LJ_METHOD_GATHER_FULL;
     return dispatch_lanes(L.lanes, [&](auto g) {
       return dispatch_bools(pbc, soa, [&](auto P, auto S) {
         constexpr int G = decltype(g)::value;
@@ -540,7 +700,29 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
     });
   }
   const MixedConsts K = make_mixed_consts(L);
-  const bool gather = L.method == LJ_METHOD_GATHER_FULL;
+  if (gather && L.kernel == 2) {
+    auto launch_u = [&](auto u) -> cudaError_t {
+      constexpr int U = decltype(u)::value;
+      return dispatch_lanes(L.lanes, [&](auto g) {
+        return dispatch_bools(pbc, soa, [&](auto P, auto S) {
+          constexpr int G = decltype(g)::value;
+          if (L.aniso)
+            k_gather_mixed_u<G, U, P.value, S.value, true>
+                <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, K);
+          else
+            k_gather_mixed_u<G, U, P.value, S.value, false>
+                <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, K);
+          return cudaGetLastError();
+        });
+      });
+    };
+    switch (L.unroll) {
+      case 2: return launch_u(std::integral_constant<int, 2>{});
+      case 4: return launch_u(std::integral_constant<int, 4>{});
+      case 8: return launch_u(std::integral_constant<int, 8>{});
+      default: return cudaErrorInvalidValue;
+    }
+  }
   if (!gather) {
     cudaError_t e = cudaMemsetAsync(L.fscratch, 0, sizeof(float) * 3 * (size_t)n, s);
     if (e != cudaSuccess) return e;

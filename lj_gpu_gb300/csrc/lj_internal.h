@@ -48,6 +48,8 @@ struct ForceLaunch {
   int method;      // LJ_METHOD_GATHER_FULL / LJ_METHOD_SCATTER_HALF (resolved)
   int lanes;       // 1..32
   int block;       // threads per block
+  int kernel;      // 1: simple strided, 2: unrolled (mixed) / compacted (FP64)
+  int unroll;      // entries in flight per lane (kernel 2, mixed)
   // mixed precision only
   int4* qfix;      // n entries, written by the fixed-image pass
   float* fscratch; // 3 n floats (scatter-half mixed only)

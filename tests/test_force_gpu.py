@@ -47,14 +47,15 @@ def system(name):
     return q, box, half
 
 
-def run_engine(engine, q, half, box, precision, method, layout, calls, dt, lanes=0, ctx=None):
+def run_engine(engine, q, half, box, precision, method, layout, calls, dt, lanes=0, ctx=None,
+               kernel=0, unroll=0):
     own = ctx is None
     ctx = ctx or engine.Context(0)
     try:
         npp, ptr, lst = half
         ctx.set_list_csr(dev(npp), dev(ptr), dev(lst), kind="half")
         opts = engine.make_opts(dt=dt, cl2=9.0, box=box, precision=precision, method=method,
-                                lanes=lanes)
+                                lanes=lanes, kernel=kernel, unroll=unroll)
         if layout == "aos":
             qd, pd = dev(q), dev(np.zeros_like(q))
             for _ in range(calls):
@@ -78,13 +79,13 @@ def oracle_p(q, half, box, calls, dt):
 
 
 @pytest.mark.parametrize("name", list(SYSTEMS))
-@pytest.mark.parametrize("method", ["scatter", "gather"])
+@pytest.mark.parametrize("method,kernel", [("scatter", 1), ("gather", 1), ("gather", 2)])
 @pytest.mark.parametrize("layout", ["aos", "soa"])
-def test_fp64_matches_oracle(engine, name, method, layout):
+def test_fp64_matches_oracle(engine, name, method, kernel, layout):
     q, box, half = system(name)
     dt = 0.001 if box is None else 0.005
     ref = oracle_p(q, half, box, 10, dt)
-    got = run_engine(engine, q, half, box, "fp64", method, layout, 10, dt)
+    got = run_engine(engine, q, half, box, "fp64", method, layout, 10, dt, kernel=kernel)
     e = ol.rel_errors(got, ref)
     assert e["max_rel"] <= FP64_TOL, e
 
@@ -99,25 +100,28 @@ def test_fp64_every_lane_width(engine, lanes):
 
 
 @pytest.mark.parametrize("name", list(SYSTEMS))
-@pytest.mark.parametrize("method", ["gather", "scatter"])
+@pytest.mark.parametrize("method,kernel", [("gather", 1), ("gather", 2), ("scatter", 1)])
 @pytest.mark.parametrize("layout", ["aos", "soa"])
-def test_mixed_error_bounds(engine, name, method, layout):
+def test_mixed_error_bounds(engine, name, method, kernel, layout):
     q, box, half = system(name)
     dt = 0.005
     ref = oracle_p(q, half, box, 1, dt)
-    got = run_engine(engine, q, half, box, "mixed", method, layout, 1, dt)
+    got = run_engine(engine, q, half, box, "mixed", method, layout, 1, dt, kernel=kernel)
     e = ol.rel_errors(got, ref)
     for k, tol in MIXED_TOL.items():
         assert e[k] <= tol, (k, e)
 
 
-@pytest.mark.parametrize("lanes", [1, 4, 8, 16, 32])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32])
 def test_mixed_every_lane_width(engine, lanes):
     q, box, half = system("pbc_rho1")
     ref = oracle_p(q, half, box, 1, 0.005)
-    got = run_engine(engine, q, half, box, "mixed", "gather", "aos", 1, 0.005, lanes=lanes)
-    e = ol.rel_errors(got, ref)
-    assert e["max_rel_rms"] <= MIXED_TOL["max_rel_rms"], e
+    for kernel, unrolls in ((1, [0]), (2, [2, 4, 8])):
+        for unroll in unrolls:
+            got = run_engine(engine, q, half, box, "mixed", "gather", "aos", 1, 0.005, lanes=lanes,
+                             kernel=kernel, unroll=unroll)
+            e = ol.rel_errors(got, ref)
+            assert e["max_rel_rms"] <= MIXED_TOL["max_rel_rms"], (kernel, unroll, e)
 
 
 def test_mixed_anisotropic_box(engine):
@@ -140,8 +144,8 @@ def test_cutoff_boundary_pairs_follow_fp64_mask(engine):
     """Isolated pairs at r2 within a few ulp of CL2: the mixed mask must be the
     FP64 mask (a toggled pair would change F by |f(rc)| ~ 1e-2, i.e. 100 %)."""
     rng = np.random.default_rng(1)
-    g = 8  # 8^3 pair sites 9 apart: only the planted pairs interact
-    centres = np.stack(np.meshgrid(*[np.arange(g) * 9.0] * 3, indexing="ij"), -1).reshape(-1, 3)
+    g = 8  # 8^3 pair sites 12 apart: only the planted pairs interact
+    centres = np.stack(np.meshgrid(*[np.arange(g) * 12.0] * 3, indexing="ij"), -1).reshape(-1, 3)
     m = centres.shape[0]
     dirs = rng.normal(size=(m, 3))
     dirs /= np.linalg.norm(dirs, axis=1)[:, None]
@@ -154,10 +158,12 @@ def test_cutoff_boundary_pairs_follow_fp64_mask(engine):
     ref64 = run_engine(engine, q, half, None, "fp64", "gather", "aos", 1, 0.005)
     inside = np.linalg.norm(ref64[:, :3], axis=1) > 0
     assert 0 < inside.sum() < 2 * m  # both sides of the surface are exercised
-    for method in ("gather", "scatter"):
-        got = run_engine(engine, q, half, None, "mixed", method, "aos", 1, 0.005)
+    for method, kernel in (("gather", 1), ("gather", 2), ("scatter", 1)):
+        got = run_engine(engine, q, half, None, "mixed", method, "aos", 1, 0.005, kernel=kernel)
         assert np.array_equal(np.linalg.norm(got[:, :3], axis=1) > 0, inside), method
         assert ol.rel_errors(got, ref64)["max_rel"] <= 1e-5, method
+    got64c = run_engine(engine, q, half, None, "fp64", "gather", "aos", 1, 0.005, kernel=2)
+    assert ol.rel_errors(got64c, ref64)["max_rel"] <= FP64_TOL
 
 
 def test_stateless_drop_in(engine):
@@ -277,8 +283,8 @@ def test_edge_cases(engine):
     half = (npp, ptr, lst)
     ref = oracle_p(q, half, None, 1, 0.001)
     for prec in ("fp64", "mixed"):
-        for method in ("scatter", "gather"):
-            got = run_engine(engine, q, half, None, prec, method, "aos", 1, 0.001)
+        for method, kernel in (("scatter", 1), ("gather", 1), ("gather", 2)):
+            got = run_engine(engine, q, half, None, prec, method, "aos", 1, 0.001, kernel=kernel)
             e = ol.rel_errors(got, ref)
             if prec == "fp64":
                 assert e["max_rel"] <= FP64_TOL, (method, e)
