@@ -149,6 +149,25 @@ int lj_force_pairs_fp64_aos(const double* q, double* p, int32_t n, double dt, do
                             const int32_t* i_particles, const int32_t* j_particles,
                             int64_t n_pairs, const double* box, void* stream);
 
+/* Mixed-precision force call over a FULL CSR list that allocates nothing
+ * (no cudaMalloc, no cudaFree, no allocating library call).  This entry point
+ * has no counterpart in the reference.  It exists for callers that cannot
+ * allocate device memory: hosts that own every allocation through their own
+ * pool, real-time loops where an allocation's implicit synchronisation is not
+ * allowed, plugin hosts that forbid it.  Its scratch, the fixed-point
+ * position image, lives in one static device array sized for at most
+ * LJ_NOALLOC_MAX_PARTICLES particles (16 MiB held by every GPU that loads the
+ * library); larger n returns LJ_ERR_INVALID_ARGUMENT.  Every call shares that
+ * array, so calls that overlap on the GPU race: order them.  The first call on
+ * a device looks up the array's device address; make it before any stream
+ * capture.  Open boundaries (box == NULL) synchronise the stream once per
+ * call to read the coordinate extent.  Same arithmetic as lj_force_aos with
+ * LJ_PREC_MIXED and LJ_METHOD_GATHER_FULL. */
+#define LJ_NOALLOC_MAX_PARTICLES 1048576
+int lj_force_mixed_noalloc_aos(const double* q, double* p, int32_t n, double dt, double cl2,
+                               const int32_t* sorted_list, const int32_t* number_of_partners,
+                               const int32_t* pointer, const double* box, void* stream);
+
 /* ---- system set-up (host memory, no GPU needed) -------------------------- */
 /* The reference's init() (cpu_ref/force_aos.cpp:142-169, add_particle :43-51):
  * FCC cells of side (4/density)^(1/3), floor(box_len / side) cells per axis,

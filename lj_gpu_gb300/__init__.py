@@ -105,7 +105,11 @@ _SIGNATURES = {
                               C.POINTER(C.c_double)]),
     "lj_init_momenta": (C.c_int, [_P, C.c_int32, C.c_double, C.c_uint64]),
     "lj_list_build": (C.c_int, [_P, _P, C.c_int32, C.c_double, _P, C.c_int32]),
+    "lj_force_mixed_noalloc_aos": (C.c_int, [_P, _P, C.c_int32, C.c_double, C.c_double, _P,
+                                             _P, _P, _P, _P]),
 }
+
+NOALLOC_MAX_PARTICLES = 1 << 20
 
 EXPORTED = tuple(_SIGNATURES)
 
@@ -315,6 +319,21 @@ def force_csr_fp64_aos(q, p, dt, cl2, sorted_list, number_of_partners, pointer, 
                                      stream)
     if st != LJ_OK:
         raise LJError(st, "lj_force_csr_fp64_aos")
+
+
+def force_mixed_noalloc_aos(q, p, dt, cl2, sorted_list, number_of_partners, pointer, box=None,
+                            stream=0):
+    """Mixed-precision gather over a full list with no allocation by the
+    engine: for callers that cannot allocate device memory.  Its scratch is a
+    static device array for at most NOALLOC_MAX_PARTICLES particles, shared by
+    every call (calls that overlap on the GPU race)."""
+    bx = _box3(box)
+    st = lib().lj_force_mixed_noalloc_aos(ptr(q), ptr(p), q.shape[0], float(dt), float(cl2),
+                                          ptr(sorted_list), ptr(number_of_partners),
+                                          ptr(pointer), C.cast(bx, C.c_void_p) if bx else None,
+                                          stream)
+    if st != LJ_OK:
+        raise LJError(st, "lj_force_mixed_noalloc_aos")
 
 
 def force_pairs_fp64_aos(q, p, dt, cl2, i_particles, j_particles, box=None, stream=0):
