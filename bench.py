@@ -172,9 +172,22 @@ def profiled_traffic(name):
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_call:"):
+        if line.startswith("traffic_bytes_per_launch:"):
             return float(line.split(":")[1].split()[0])
     return None
+
+
+# FP64 add / FMA issue rate measured on this machine's GB300 (one op per lane):
+# 503 G/s, i.e. ~1.0 TFLOP/s counting an FMA as two
+FP64_PEAK_OPS = 503e9
+
+
+def pair_kernel_bytes(method, layout, P, N):
+    """Compulsory bytes of the pair kernel alone: list indices, the 16-byte
+    fixed-point image read once, number_of_partners + pointer, p read +
+    written (AoS: a 32-byte record)."""
+    per_n = (16 + 8 + 64) if layout == "aos" else (16 + 8 + 48)
+    return (8 if method == "gather" else 4) * P + per_n * N
 
 
 def algorithmic_bytes(method, layout, P, N):
@@ -237,8 +250,9 @@ def run_ours(args, dist):
         ms = [a.elapsed_time(b) for a, b in ev]
         return sum(ms)
 
-    variants = [(p, m, l) for p in ("mixed", "fp64") for m in ("gather", "scatter")
-                for l in ("aos", "soa")]
+    variants = [("mixed", "gather", "aos"), ("mixed", "gather", "soa"),
+                ("mixed", "scatter", "aos"), ("fp64", "scatter", "aos"),
+                ("fp64", "scatter", "soa"), ("fp64", "gather", "aos")]
     results = {}
     clocks = None
     for v in variants:
@@ -259,6 +273,17 @@ def run_ours(args, dist):
                     key=lambda k: results[k]["gpairs"])
     head = results[best_mixed]
     prec, method, layout = best_mixed.split("/")
+
+    # pair-kernel time of the headline variant (engine-side CUDA events
+    # between the position-image pass and the pair kernel)
+    def stage_times(variant, steps):
+        ctx.set_timing(True)
+        time_variant(*variant.split("/"), steps, 0)
+        t = ctx.get_timing()
+        ctx.set_timing(False)
+        return t[0] / t[3], t[1] / t[3]
+    t_image_ms, t_pair_ms = stage_times(best_mixed, args.steps)
+    t_image64_ms, t_pair64_ms = stage_times(best_fp64, max(3, min(args.steps, 20)))
 
     # e2e: the reference's measure() through the C ABI with pinned host buffers
     e2e = None
@@ -286,17 +311,30 @@ def run_ours(args, dist):
                "ms_per_step": t_step * 1e3}
 
     hbm, peak_kind = peaks()
-    alg = algorithmic_bytes(method, layout, P, N)
-    achieved = alg / head["s_per_call"] / 1e9
+    alg = pair_kernel_bytes(method, layout, P, N)
+    achieved = alg / (t_pair_ms * 1e-3) / 1e9
     traffic = profiled_traffic("force_mixed_gather_aos_108k_rho0.5.txt")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                "algorithmic_bytes_per_call": alg,
-                "kernel": f"force call {best_mixed} (fixed-image pass + pair kernel)"}
+                "kernel": f"pair kernel of {best_mixed} (k_gather_mixed_u)",
+                "algorithmic_bytes_per_launch": alg,
+                "kernel_ms": t_pair_ms, "position_image_ms": t_image_ms,
+                "force_call_bytes": algorithmic_bytes(method, layout, P, N),
+                "force_call_frac": algorithmic_bytes(method, layout, P, N)
+                / head["s_per_call"] / 1e9 / hbm}
     fp = results[best_fp64]
-    fp_alg = algorithmic_bytes(best_fp64.split("/")[1], best_fp64.split("/")[2], P, N)
+    fp_m, fp_l = best_fp64.split("/")[1], best_fp64.split("/")[2]
+    # FP64 arithmetic per pair inside the cutoff (scatter): 20 FP64 ops; the
+    # inside fraction of a search-radius list is (rc / rs)^3 for a uniform
+    # density
+    inside = (RC / RS) ** 3
+    dp_ops = P * inside * (20 if fp_m == "scatter" else 34)
     fp64 = {"value": fp["gpairs"], "variant": best_fp64, "ms_per_call": fp["s_per_call"] * 1e3,
-            "hbm_frac": fp_alg / fp["s_per_call"] / 1e9 / hbm,
+            "pair_kernel_ms": t_pair64_ms,
+            "hbm_frac": algorithmic_bytes(fp_m, fp_l, P, N) / fp["s_per_call"] / 1e9 / hbm,
+            "fp64_ops_per_call": dp_ops,
+            "fp64_pipe_frac": dp_ops / (t_pair64_ms * 1e-3) / FP64_PEAK_OPS,
+            "fp64_peak_ops_per_s": FP64_PEAK_OPS,
             "mixed_over_fp64": head["gpairs"] / fp["gpairs"]}
 
     cpu = None
@@ -317,6 +355,7 @@ def run_ours(args, dist):
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64": fp64,
         "variants": {k: round(v["gpairs"], 3) for k, v in results.items()},
         "clocks": clocks, "gpu_launches": 2 * args.steps,
+        "gpu_launches_note": "headline timed region: position-image pass + pair kernel per step",
     }
     ctx.close()
     return line

@@ -92,6 +92,14 @@ void lj_ctx_destroy(lj_ctx* ctx);
 const char* lj_ctx_last_error(const lj_ctx* ctx);
 /* stream used by every later call on ctx (cudaStream_t as void*) */
 int lj_ctx_set_stream(lj_ctx* ctx, void* stream);
+/* Per-stage device timing of force calls (the reference times with
+ * gettimeofday around 100 calls, cuda/force_cuda.cu:330-341; this records
+ * CUDA events around the engine's own launches).  on = 1 enables and resets
+ * the sums, 0 disables. */
+int lj_ctx_set_timing(lj_ctx* ctx, int32_t on);
+/* ms[0]: position-image passes, ms[1]: pair kernels, ms[2]: both, summed
+ * over *calls force calls since the last reset (synchronises). */
+int lj_ctx_get_timing(lj_ctx* ctx, double* ms, int64_t* calls);
 
 /* ---- neighbour lists ---------------------------------------------------- */
 /* Installs an i-sorted CSR list for n particles (replaces the reference's

@@ -85,6 +85,8 @@ _SIGNATURES = {
     "lj_ctx_destroy": (None, [_P]),
     "lj_ctx_last_error": (C.c_char_p, [_P]),
     "lj_ctx_set_stream": (C.c_int, [_P, _P]),
+    "lj_ctx_set_timing": (C.c_int, [_P, C.c_int32]),
+    "lj_ctx_get_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "lj_list_set_csr": (C.c_int, [_P, C.c_int32, _P, _P, _P, C.c_int64, C.c_int32, C.c_int32]),
     "lj_list_set_pairs": (C.c_int, [_P, C.c_int32, _P, _P, C.c_int64, C.c_int32]),
     "lj_list_get_csr": (C.c_int, [_P, C.c_int32, _P, _P, _P, C.c_int64,
@@ -200,6 +202,16 @@ class Context:
     def set_stream(self, stream):
         s = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream or 0)
         self._check(lib().lj_ctx_set_stream(self._h, s), "set_stream")
+
+    def set_timing(self, on=True):
+        self._check(lib().lj_ctx_set_timing(self._h, 1 if on else 0), "set_timing")
+
+    def get_timing(self):
+        """(ms position-image passes, ms pair kernels, ms both, calls) since reset."""
+        ms = (C.c_double * 3)()
+        calls = C.c_int64()
+        self._check(lib().lj_ctx_get_timing(self._h, ms, C.byref(calls)), "get_timing")
+        return ms[0], ms[1], ms[2], calls.value
 
     def set_list_csr(self, number_of_partners, pointer, sorted_list, kind="half", n=None):
         _check_contig(number_of_partners, pointer, sorted_list)

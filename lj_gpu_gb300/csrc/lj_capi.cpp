@@ -86,6 +86,12 @@ struct lj_ctx {
   DevBuf<int4> b_cq;
   DevBuf<unsigned long long> b_minmax;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  // per-stage timing (lj_ctx_set_timing): event triples around force calls
+  bool timing = false;
+  std::vector<cudaEvent_t> tev;  // pool, 3 per recorded call
+  size_t tev_used = 0;
+  double t_ms[3] = {0, 0, 0};
+  int64_t t_calls = 0;
 };
 
 namespace {
@@ -149,13 +155,14 @@ Periodic make_periodic(const lj_force_opts* o) {
   return b;
 }
 
-// Default lanes per i-particle: chosen from the average row length so that a
-// group takes a few strided steps per row (kernel 2 moves `unroll` entries
-// per lane and step, so it uses narrower groups).
+// Defaults measured on GB300 (108,000 particles, rho = 0.5 and 1.0, cold L2):
+//   mixed gather  : kernel 2, 4 lanes per row, 4 entries per lane in flight
+//   FP64 scatter  : kernel 2 (compacted, RED on both ends)
+//   FP64 gather   : kernel 2 (compacted, one warp per row)
 int default_lanes(int precision, int method, int kernel, int64_t entries, int n) {
-  (void)method;
   const double avg = n > 0 ? (double)entries / n : 0.0;
-  if (kernel == 2 && precision == LJ_PREC_MIXED) return avg <= 48 ? 2 : (avg <= 96 ? 4 : 8);
+  if (kernel == 2 && precision == LJ_PREC_MIXED) return avg <= 24 ? 2 : 4;
+  if (precision == LJ_PREC_FP64 && method == LJ_METHOD_SCATTER_HALF) return avg <= 12 ? 2 : 4;
   if (avg <= 12) return 2;
   if (avg <= 24) return 4;
   if (avg <= 96) return 8;
@@ -163,9 +170,8 @@ int default_lanes(int precision, int method, int kernel, int64_t entries, int n)
 }
 
 int default_kernel(int precision, int method) {
-  (void)precision;
-  (void)method;
-  return 1;
+  if (precision == LJ_PREC_MIXED) return method == LJ_METHOD_GATHER_FULL ? 2 : 1;
+  return 2;
 }
 
 int copy_in(lj_ctx* ctx, int32_t* dst, const int32_t* src, size_t count, int where) {
@@ -177,26 +183,6 @@ int copy_in(lj_ctx* ctx, int32_t* dst, const int32_t* src, size_t count, int whe
                           ctx->stream),
           "list copy");
   return LJ_OK;
-}
-
-// Validates the CSR in `l` on the device; synchronises.
-int validate(lj_ctx* ctx, const DevList& l) {
-  LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
-  const int32_t init[2] = {0, 0x7fffffff};
-  LJ_CUDA(ctx, cudaMemcpyAsync(ctx->err2.ptr, init, sizeof init, cudaMemcpyHostToDevice,
-                               ctx->stream), "err init");
-  LJ_CUDA(ctx, launch_validate_csr(l.csr(), ctx->err2.ptr, ctx->stream), "validate");
-  int32_t out[2];
-  LJ_CUDA(ctx, cudaMemcpyAsync(out, ctx->err2.ptr, sizeof out, cudaMemcpyDeviceToHost,
-                               ctx->stream), "err read");
-  LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "validate sync");
-  switch (out[0]) {
-    case 0: return LJ_OK;
-    case 1: return fail(ctx, LJ_ERR_BAD_LIST, "number_of_partners[%d] out of range", out[1]);
-    case 2: return fail(ctx, LJ_ERR_BAD_LIST, "pointer[%d] out of range", out[1]);
-    case 3: return fail(ctx, LJ_ERR_BAD_LIST, "row %d runs past the end of the list", out[1]);
-    default: return fail(ctx, LJ_ERR_BAD_LIST, "sorted_list[%d] out of range", out[1]);
-  }
 }
 
 // Builds ctx->full from ctx->half on the device.
@@ -239,19 +225,10 @@ int expand_full(lj_ctx* ctx) {
   return LJ_OK;
 }
 
-int row_max(lj_ctx* ctx, DevList& l) {
-  // max row of an installed list (reuses the offsets->ptr reduction path)
-  std::vector<int32_t> np((size_t)l.n);
-  if (l.n > 0)
-    LJ_CUDA(ctx, cudaMemcpyAsync(np.data(), l.np.ptr, sizeof(int32_t) * (size_t)l.n,
-                                 cudaMemcpyDeviceToHost, ctx->stream), "np read");
-  LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-  int m = 0;
-  for (int v : np) m = std::max(m, v);
-  l.max_row = m;
-  return LJ_OK;
-}
-
+// Copies a caller CSR into the context, validates it, and stores it compact:
+// rows in i order, contiguous, pointer[i] = sum of the earlier row lengths
+// (what sortpair produces).  Kernels that sweep several rows as one flat range
+// rely on that.
 int install_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ptr,
                 const int32_t* list, int64_t entries, int32_t kind, int32_t where) {
   DevList& l = kind == LJ_LIST_HALF ? ctx->half : ctx->full;
@@ -259,15 +236,52 @@ int install_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ptr,
   ctx->full.valid = false;
   LJ_CUDA(ctx, l.np.ensure((size_t)n), "alloc");
   LJ_CUDA(ctx, l.ptr.ensure((size_t)n), "alloc");
-  LJ_CUDA(ctx, l.list.ensure((size_t)entries), "alloc");
+  LJ_CUDA(ctx, ctx->tmp_i32a.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->tmp_i32b.ensure((size_t)entries), "alloc");
   int rc;
   if ((rc = copy_in(ctx, l.np.ptr, np, (size_t)n, where))) return rc;
-  if ((rc = copy_in(ctx, l.ptr.ptr, ptr, (size_t)n, where))) return rc;
-  if ((rc = copy_in(ctx, l.list.ptr, list, (size_t)entries, where))) return rc;
+  if ((rc = copy_in(ctx, ctx->tmp_i32a.ptr, ptr, (size_t)n, where))) return rc;
+  if ((rc = copy_in(ctx, ctx->tmp_i32b.ptr, list, (size_t)entries, where))) return rc;
+  // validation runs on the caller's layout, as check_loadedpair does
+  const Csr raw{n, entries, l.np.ptr, ctx->tmp_i32a.ptr, ctx->tmp_i32b.ptr};
+  {
+    LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
+    const int32_t init[2] = {0, 0x7fffffff};
+    LJ_CUDA(ctx, cudaMemcpyAsync(ctx->err2.ptr, init, sizeof init, cudaMemcpyHostToDevice,
+                                 ctx->stream), "err init");
+    LJ_CUDA(ctx, launch_validate_csr(raw, ctx->err2.ptr, ctx->stream), "validate");
+    int32_t out[2];
+    LJ_CUDA(ctx, cudaMemcpyAsync(out, ctx->err2.ptr, sizeof out, cudaMemcpyDeviceToHost,
+                                 ctx->stream), "err read");
+    LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "validate sync");
+    switch (out[0]) {
+      case 0: break;
+      case 1: return fail(ctx, LJ_ERR_BAD_LIST, "number_of_partners[%d] out of range", out[1]);
+      case 2: return fail(ctx, LJ_ERR_BAD_LIST, "pointer[%d] out of range", out[1]);
+      case 3: return fail(ctx, LJ_ERR_BAD_LIST, "row %d runs past the end of the list", out[1]);
+      default: return fail(ctx, LJ_ERR_BAD_LIST, "sorted_list[%d] out of range", out[1]);
+    }
+  }
+  LJ_CUDA(ctx, ctx->tmp_off.ensure((size_t)n + 1), "alloc");
+  LJ_CUDA(ctx, ctx->tmp_scan.ensure(scan_tmp_bytes(n)), "alloc");
+  LJ_CUDA(ctx, launch_scan_counts(l.np.ptr, n, ctx->tmp_off.ptr, ctx->tmp_scan.ptr,
+                                  ctx->tmp_scan.cap, ctx->stream), "scan");
+  int64_t total = 0;
+  LJ_CUDA(ctx, cudaMemcpyAsync(&total, ctx->tmp_off.ptr + n, sizeof total,
+                               cudaMemcpyDeviceToHost, ctx->stream), "total");
+  LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+  LJ_CUDA(ctx, l.list.ensure((size_t)std::max<int64_t>(total, 1)), "alloc");
+  LJ_CUDA(ctx, launch_compact_rows(l.np.ptr, ctx->tmp_i32a.ptr, ctx->tmp_i32b.ptr,
+                                   ctx->tmp_off.ptr, n, l.list.ptr, ctx->stream), "compact");
+  LJ_CUDA(ctx, launch_offsets_to_ptr(ctx->tmp_off.ptr, n, l.ptr.ptr, l.np.ptr, ctx->err2.ptr,
+                                     ctx->stream), "ptr");
+  int32_t mr = 0;
+  LJ_CUDA(ctx, cudaMemcpyAsync(&mr, ctx->err2.ptr, sizeof mr, cudaMemcpyDeviceToHost,
+                               ctx->stream), "max row");
+  LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
   l.n = n;
-  l.entries = entries;
-  if ((rc = validate(ctx, l))) return rc;
-  if ((rc = row_max(ctx, l))) return rc;
+  l.entries = total;
+  l.max_row = mr;
   l.valid = true;
   if (kind == LJ_LIST_HALF) {
     if ((rc = expand_full(ctx))) {
@@ -295,6 +309,20 @@ int resolve_method(lj_ctx* ctx, const lj_force_opts* o, int* method) {
   return LJ_OK;
 }
 
+// Three events per timed force call: before the position-image pass, before
+// the pair kernel, after it.
+cudaEvent_t* timing_slot(lj_ctx* ctx) {
+  if (!ctx->timing) return nullptr;
+  while (ctx->tev.size() < ctx->tev_used + 3) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    ctx->tev.push_back(e);
+  }
+  cudaEvent_t* s = ctx->tev.data() + ctx->tev_used;
+  ctx->tev_used += 3;
+  return s;
+}
+
 int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts* o) {
   int rc = check_opts(ctx, o);
   if (rc) return rc;
@@ -313,14 +341,18 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
   L.precision = o->precision;
   L.method = method;
   L.kernel = o->kernel ? o->kernel : default_kernel(o->precision, method);
-  if (L.kernel == 2 && method == LJ_METHOD_SCATTER_HALF) L.kernel = 1;  // no compacted scatter
+  // the mixed path has no compacted scatter (FP32 atomics lose to the gather)
+  if (L.kernel == 2 && method == LJ_METHOD_SCATTER_HALF && o->precision == LJ_PREC_MIXED)
+    L.kernel = 1;
   L.unroll = o->unroll ? o->unroll : 4;
-  if (L.kernel == 2 && !(L.unroll == 2 || L.unroll == 4 || L.unroll == 8))
-    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be 2, 4 or 8");
+  if (L.kernel == 2 && !(L.unroll == 1 || L.unroll == 2 || L.unroll == 4 || L.unroll == 8))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be 1, 2, 4 or 8");
   L.lanes = o->lanes ? o->lanes : default_lanes(o->precision, method, L.kernel, l.entries, l.n);
   L.block = o->block ? o->block : 128;
   if (n == 0) return LJ_OK;
   const bool fixed = o->precision == LJ_PREC_MIXED || L.kernel == 2;
+  cudaEvent_t* tv = timing_slot(ctx);
+  if (tv) LJ_CUDA(ctx, cudaEventRecord(tv[0], ctx->stream), "event");
   if (fixed) {
     LJ_CUDA(ctx, ctx->qfix.ensure((size_t)n), "alloc");
     L.qfix = ctx->qfix.ptr;
@@ -341,7 +373,9 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
     }
     LJ_CUDA(ctx, launch_fixed_image(L, ctx->stream), "fixed image");
   }
+  if (tv) LJ_CUDA(ctx, cudaEventRecord(tv[1], ctx->stream), "event");
   LJ_CUDA(ctx, launch_force(L, ctx->stream), "force launch");
+  if (tv) LJ_CUDA(ctx, cudaEventRecord(tv[2], ctx->stream), "event");
   return LJ_OK;
 }
 
@@ -403,10 +437,45 @@ void lj_ctx_destroy(lj_ctx* ctx) {
   else cudaDeviceSynchronize();
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : ctx->tev) cudaEventDestroy(e);
   delete ctx;
 }
 
 const char* lj_ctx_last_error(const lj_ctx* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int lj_ctx_set_timing(lj_ctx* ctx, int32_t on) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  if (ctx->tev_used) cudaStreamSynchronize(ctx->stream);
+  ctx->timing = on != 0;
+  ctx->tev_used = 0;
+  ctx->t_ms[0] = ctx->t_ms[1] = ctx->t_ms[2] = 0.0;
+  ctx->t_calls = 0;
+  return LJ_OK;
+}
+
+int lj_ctx_get_timing(lj_ctx* ctx, double* ms, int64_t* calls) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  for (size_t k = 0; k + 2 < ctx->tev_used; k += 3) {
+    LJ_CUDA(ctx, cudaEventSynchronize(ctx->tev[k + 2]), "event sync");
+    float a = 0.f, b = 0.f;
+    LJ_CUDA(ctx, cudaEventElapsedTime(&a, ctx->tev[k], ctx->tev[k + 1]), "elapsed");
+    LJ_CUDA(ctx, cudaEventElapsedTime(&b, ctx->tev[k + 1], ctx->tev[k + 2]), "elapsed");
+    ctx->t_ms[0] += a;
+    ctx->t_ms[1] += b;
+    ctx->t_ms[2] += a + b;
+    ctx->t_calls++;
+  }
+  ctx->tev_used = 0;
+  if (ms) {
+    ms[0] = ctx->t_ms[0];
+    ms[1] = ctx->t_ms[1];
+    ms[2] = ctx->t_ms[2];
+  }
+  if (calls) *calls = ctx->t_calls;
+  return LJ_OK;
+}
 
 int lj_ctx_set_stream(lj_ctx* ctx, void* stream) {
   if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
@@ -432,9 +501,21 @@ int lj_list_set_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* pt
   ctx->list_from_host = where == LJ_WHERE_HOST;
   ctx->host_kind = kind;
   if (ctx->list_from_host) {
-    ctx->h_np.assign(np, np + n);
-    ctx->h_ptr.assign(ptr, ptr + n);
-    ctx->h_list.assign(list, list + entries);
+    // the compact form actually installed, re-uploaded by lj_measure_aos
+    const DevList& l = kind == LJ_LIST_HALF ? ctx->half : ctx->full;
+    ctx->h_np.resize((size_t)n);
+    ctx->h_ptr.resize((size_t)n);
+    ctx->h_list.resize((size_t)l.entries);
+    if (n > 0) {
+      LJ_CUDA(ctx, cudaMemcpy(ctx->h_np.data(), l.np.ptr, sizeof(int32_t) * (size_t)n,
+                              cudaMemcpyDeviceToHost), "copy");
+      LJ_CUDA(ctx, cudaMemcpy(ctx->h_ptr.data(), l.ptr.ptr, sizeof(int32_t) * (size_t)n,
+                              cudaMemcpyDeviceToHost), "copy");
+    }
+    if (l.entries > 0)
+      LJ_CUDA(ctx, cudaMemcpy(ctx->h_list.data(), l.list.ptr,
+                              sizeof(int32_t) * (size_t)l.entries, cudaMemcpyDeviceToHost),
+              "copy");
   } else {
     ctx->h_np.clear();
     ctx->h_ptr.clear();

@@ -34,12 +34,17 @@ __device__ __forceinline__ bool dlt_neg(double x, long long ybits) {
   return (unsigned long long)dbits(x) > (0x8000000000000000ull | (unsigned long long)ybits);
 }
 
-// Minimum-image shift of one FP64 component; exactly `d > L/2 ? d - L :
-// d < -L/2 ? d + L : d` with the comparisons done on bit patterns.
+// Minimum-image shift of one FP64 component: `d > L/2 ? d - L : d < -L/2 ?
+// d + L : d`.  The comparisons run on bit patterns and the shift (0, -L or +L)
+// is selected with integer moves, so exactly one FP64 add is issued (two
+// predicated adds would both occupy the FP64 pipe).  d + (-L) is bitwise
+// d - L, so the result equals the branchy form.
 __device__ __forceinline__ double min_image_fp64(double d, double len, long long half_bits) {
-  if (dgt_pos(d, half_bits)) d -= len;
-  else if (dlt_neg(d, half_bits)) d += len;
-  return d;
+  const long long lb = dbits(len);
+  long long sb = 0;  // +0.0
+  if (dgt_pos(d, half_bits)) sb = lb ^ (long long)0x8000000000000000ull;
+  if (dlt_neg(d, half_bits)) sb = lb;
+  return d + __longlong_as_double(sb);
 }
 
 // 1/r2 in FP64.  The seed is the MUFU FP32 reciprocal of the top 20 mantissa

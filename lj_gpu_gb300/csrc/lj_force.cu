@@ -488,6 +488,81 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_gather_fp64_c(
   if (lane == 0) add_p<SOA>(P, i, fx, fy, fz);
 }
 
+// Compacted FP64 scatter over the half list (kernel 2).  A warp owns 32
+// consecutive rows; their entries are contiguous (the context keeps a compact
+// CSR), so the warp sweeps them flat, 32 entries per step, each lane finding
+// its entry's row by a shuffle binary search over the rows' start offsets.
+// Candidates are screened in FP32 from the fixed-point image; survivors are
+// queued as (i, j) in shared memory and the FP64 arithmetic runs on full
+// batches of 32.  Both ends are updated with RED.F64 (p_i += f, p_j -= f), so
+// a batch may span rows and no lane waits for a row to end.
+constexpr int kScatterWarps = 4;
+
+template <bool PBC, bool SOA>
+__device__ __forceinline__ void fp64_pair_red(const Particles& P, int i, int j,
+                                              const Fp64Consts& k) {
+  const double3 d = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, j), k);
+  const double r2 = r2_fp64(d);
+  if (beyond_cutoff(r2, k.cl2_bits)) return;
+  const double df = df_fp64(r2, k);
+  const double fx = df * d.x, fy = df * d.y, fz = df * d.z;
+  red_p<SOA>(P, i, fx, fy, fz);
+  red_p<SOA>(P, j, flip_sign(fx), flip_sign(fy), flip_sign(fz));
+}
+
+template <bool PBC, bool SOA, bool ANISO>
+__global__ void __launch_bounds__(32 * kScatterWarps) k_scatter_fp64_c(
+    const Particles P, const Csr C, const int4* __restrict__ qfix, const MixedConsts K) {
+  __shared__ int2 queue[kScatterWarps][64];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r0 = (blockIdx.x * kScatterWarps + w) * 32;
+  if (r0 >= C.n) return;  // warp-uniform
+  const int nrows = min(32, C.n - r0);
+  int2* q = queue[w];
+  // start offset of row r0 + lane (rows past the end start at e1)
+  const int my_start = lane < nrows ? __ldg(C.ptr + r0 + lane) : 0x7fffffff;
+  const int e0 = __shfl_sync(kFullMask, my_start, 0);
+  const int last = nrows - 1;
+  const int e1 = __shfl_sync(kFullMask, my_start, last) + __ldg(C.np + r0 + last);
+  const unsigned lt = (1u << lane) - 1u;
+  int qn = 0;
+  for (int base = e0; base < e1; base += 32) {
+    const int k = base + lane;
+    // row of entry k: the largest r with start(r) <= k (all lanes search, so
+    // every shuffle is executed by the full warp; r + step stays below 32)
+    int r = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int s = __shfl_sync(kFullMask, my_start, r + step);
+      if (s <= k) r += step;
+    }
+    bool cand = false;
+    const int i = r0 + r;
+    int j = 0;
+    if (k < e1) {
+      j = __ldg(C.list + k);
+      const float3 d = sep_mixed<ANISO>(__ldg(qfix + i), __ldg(qfix + j), K);
+      cand = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x)) <= K.cl2_hi;
+    }
+    const unsigned b = __ballot_sync(kFullMask, cand);
+    if (cand) q[qn + __popc(b & lt)] = make_int2(i, j);
+    qn += __popc(b);
+    __syncwarp();
+    if (qn >= 32) {
+      const int2 e = q[lane];
+      fp64_pair_red<PBC, SOA>(P, e.x, e.y, K.f64);
+      __syncwarp();
+      if (lane < qn - 32) q[lane] = q[lane + 32];
+      qn -= 32;
+      __syncwarp();
+    }
+  }
+  if (lane < qn) {
+    const int2 e = q[lane];
+    fp64_pair_red<PBC, SOA>(P, e.x, e.y, K.f64);
+  }
+}
+
 // Mixed scatter: FP32 partial forces per particle in a scratch array
 // (compensation lost on the j side), then one FP64 kick per particle.
 template <int G, bool PBC, bool SOA, bool ANISO>
@@ -674,6 +749,19 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
   const bool pbc = L.box.on != 0, soa = L.part.soa != 0;
   const bool gather = L.method == LJ_METHOD_GATHER_FULL;
   if (L.precision == LJ_PREC_FP64) {
+    if (!gather && L.kernel == 2) {
+      const MixedConsts K = make_mixed_consts(L);
+      const int cb = (n + 32 * kScatterWarps - 1) / (32 * kScatterWarps);
+      return dispatch_bools(pbc, soa, [&](auto P, auto S) {
+        if (L.aniso)
+          k_scatter_fp64_c<P.value, S.value, true>
+              <<<cb, 32 * kScatterWarps, 0, s>>>(L.part, L.csr, L.qfix, K);
+        else
+          k_scatter_fp64_c<P.value, S.value, false>
+              <<<cb, 32 * kScatterWarps, 0, s>>>(L.part, L.csr, L.qfix, K);
+        return cudaGetLastError();
+      });
+    }
     if (gather && L.kernel == 2) {
       const MixedConsts K = make_mixed_consts(L);
       const int cb = (n + kCompactWarps - 1) / kCompactWarps;
@@ -717,6 +805,7 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
       });
     };
     switch (L.unroll) {
+      case 1: return launch_u(std::integral_constant<int, 1>{});
       case 2: return launch_u(std::integral_constant<int, 2>{});
       case 4: return launch_u(std::integral_constant<int, 4>{});
       case 8: return launch_u(std::integral_constant<int, 8>{});

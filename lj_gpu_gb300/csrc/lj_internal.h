@@ -86,6 +86,9 @@ cudaError_t launch_full_from_half_fill(const Csr& half, const int64_t* off, int3
 // Rows [off[i], off[i+1]) of `in` sorted ascending (stable) into `out`.
 cudaError_t launch_sort_rows_into(const int64_t* off, int n, const int32_t* in, int32_t* out,
                                   cudaStream_t s);
+// Compact copy of CSR rows: out[off[i] + m] = in[ptr[i] + m], m < np[i].
+cudaError_t launch_compact_rows(const int32_t* np, const int32_t* ptr, const int32_t* in,
+                                const int64_t* off, int n, int32_t* out, cudaStream_t s);
 cudaError_t launch_offsets_to_ptr(const int64_t* off, int n, int32_t* ptr, int32_t* np,
                                   int32_t* max_row, cudaStream_t s);
 // (i, j) pairs with non-decreasing i into CSR rows: counts per i.

@@ -174,6 +174,19 @@ __global__ void k_pairs_count(const int32_t* ip, int64_t npairs, int n, int32_t*
   }
 }
 
+// out[off[i] + m] = in[ptr[i] + m] for m < np[i]: a compact, contiguous CSR
+__global__ void k_compact_rows(const int32_t* __restrict__ np, const int32_t* __restrict__ ptr,
+                               const int32_t* __restrict__ in, const int64_t* __restrict__ off,
+                               int n, int32_t* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nwarps) {
+    const int c = np[i], a = ptr[i];
+    const int64_t b = off[i];
+    for (int m = lane; m < c; m += 32) out[b + m] = in[a + m];
+  }
+}
+
 int grid_for(int64_t work, int block) {
   int64_t g = (work + block - 1) / block;
   if (g < 1) g = 1;
@@ -226,6 +239,12 @@ cudaError_t launch_full_from_half_fill(const Csr& half, const int64_t* off, int3
 cudaError_t launch_sort_rows_into(const int64_t* off, int n, const int32_t* in, int32_t* out,
                                   cudaStream_t s) {
   if (n > 0) k_sort_rows<<<grid_for((int64_t)n * 32, 256), 256, 0, s>>>(off, n, in, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compact_rows(const int32_t* np, const int32_t* ptr, const int32_t* in,
+                                const int64_t* off, int n, int32_t* out, cudaStream_t s) {
+  if (n > 0) k_compact_rows<<<grid_for((int64_t)n * 32, 256), 256, 0, s>>>(np, ptr, in, off, n, out);
   return cudaGetLastError();
 }
 

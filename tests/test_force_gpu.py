@@ -79,7 +79,8 @@ def oracle_p(q, half, box, calls, dt):
 
 
 @pytest.mark.parametrize("name", list(SYSTEMS))
-@pytest.mark.parametrize("method,kernel", [("scatter", 1), ("gather", 1), ("gather", 2)])
+@pytest.mark.parametrize("method,kernel", [("scatter", 1), ("scatter", 2), ("gather", 1),
+                                           ("gather", 2)])
 @pytest.mark.parametrize("layout", ["aos", "soa"])
 def test_fp64_matches_oracle(engine, name, method, kernel, layout):
     q, box, half = system(name)
@@ -162,8 +163,9 @@ def test_cutoff_boundary_pairs_follow_fp64_mask(engine):
         got = run_engine(engine, q, half, None, "mixed", method, "aos", 1, 0.005, kernel=kernel)
         assert np.array_equal(np.linalg.norm(got[:, :3], axis=1) > 0, inside), method
         assert ol.rel_errors(got, ref64)["max_rel"] <= 1e-5, method
-    got64c = run_engine(engine, q, half, None, "fp64", "gather", "aos", 1, 0.005, kernel=2)
-    assert ol.rel_errors(got64c, ref64)["max_rel"] <= FP64_TOL
+    for method in ("gather", "scatter"):
+        got64c = run_engine(engine, q, half, None, "fp64", method, "aos", 1, 0.005, kernel=2)
+        assert ol.rel_errors(got64c, ref64)["max_rel"] <= FP64_TOL, method
 
 
 def test_stateless_drop_in(engine):
@@ -283,7 +285,7 @@ def test_edge_cases(engine):
     half = (npp, ptr, lst)
     ref = oracle_p(q, half, None, 1, 0.001)
     for prec in ("fp64", "mixed"):
-        for method, kernel in (("scatter", 1), ("gather", 1), ("gather", 2)):
+        for method, kernel in (("scatter", 1), ("scatter", 2), ("gather", 1), ("gather", 2)):
             got = run_engine(engine, q, half, None, prec, method, "aos", 1, 0.001, kernel=kernel)
             e = ol.rel_errors(got, ref)
             if prec == "fp64":
@@ -339,4 +341,32 @@ def test_device_list_build_large_periodic(engine):
         ctx.build_list(dev(q), 3.3, box=L)
         got = ctx.get_list_csr("half")
         for a, b in zip(got, half):
+            assert np.array_equal(a, b)
+
+
+def test_non_compact_list_layout(engine):
+    """Rows stored out of order with gaps between them (a valid CSR that is not
+    compact): every kernel sees the same pairs as with the compact list."""
+    q, box, half = system("pbc_rho0.5")
+    npp, ptr, lst = half
+    n = len(npp)
+    rng = np.random.default_rng(8)
+    order = rng.permutation(n)
+    gap = 3
+    new_ptr = np.zeros(n, np.int32)
+    chunks, pos = [], 0
+    for i in order:
+        new_ptr[i] = pos
+        chunks.append(lst[ptr[i]:ptr[i] + npp[i]])
+        chunks.append(np.full(gap, -7 % n, np.int32))  # junk between rows
+        pos += npp[i] + gap
+    big = np.concatenate(chunks).astype(np.int32)
+    ref = oracle_p(q, half, box, 1, 0.005)
+    for method, kernel in (("scatter", 1), ("scatter", 2), ("gather", 1), ("gather", 2)):
+        got = run_engine(engine, q, (npp, new_ptr, big), box, "fp64", method, "aos", 1, 0.005,
+                         kernel=kernel)
+        assert ol.rel_errors(got, ref)["max_rel"] <= FP64_TOL, (method, kernel)
+    with engine.Context(0) as ctx:
+        ctx.set_list_csr(dev(npp), dev(new_ptr), dev(big))
+        for a, b in zip(ctx.get_list_csr("half"), half):
             assert np.array_equal(a, b)
