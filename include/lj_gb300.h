@@ -207,6 +207,44 @@ enum { LJ_BUILD_HALF = 1, LJ_BUILD_FULL = 2 };
 int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double search_radius,
                   const double* box, int32_t kinds);
 
+/* ---- molecular dynamics (project extension) ------------------------------- */
+/* The reference never integrates: its 100 calls re-kick p from a fixed q
+ * (cpu_ref/force_aos.cpp:592-601).  lj_md_run advances q and p with velocity
+ * Verlet (m = 1) in a periodic box, using the force path above as the kick,
+ * with on-device neighbour rebuilds whenever a particle has moved more than
+ * skin/2 since the last build. */
+typedef struct lj_md_params {
+  double dt;              /* time step */
+  double rc;              /* cutoff; list radius = rc + skin */
+  double skin;            /* Verlet skin */
+  double box[3];          /* periodic box lengths (each > 2 (rc + skin)) */
+  int32_t precision;      /* LJ_PREC_MIXED (gather) or LJ_PREC_FP64 (scatter) */
+  int32_t record_every;   /* energies every k steps (0: at 0 and at the end) */
+  int32_t graph_steps;    /* steps per captured CUDA graph (0: 20, 1: no graph) */
+  int32_t reserved[5];
+} lj_md_params;
+
+typedef struct lj_md_record {
+  int64_t step;
+  double kinetic;    /* sum p^2 / 2 (FP64) */
+  double potential;  /* sum over pairs r <= rc of 4 (r^-12 - r^-6), unshifted */
+} lj_md_record;
+
+typedef struct lj_md_stats {
+  int64_t steps;
+  int64_t rebuilds;       /* list builds after the initial one */
+  double ms_total;        /* device time of the whole run */
+  int64_t list_capacity;  /* entries reserved for the list */
+} lj_md_stats;
+
+/* q, p: AoS device arrays (modified in place; p must hold the initial
+ * momenta, e.g. from lj_init_momenta).  records may be NULL.  Positions are
+ * wrapped into [0, L).  LJ_ERR_LIST_OVERFLOW if a rebuild would exceed the
+ * list capacity (q, p are then partially advanced). */
+int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_params* params,
+              int32_t nsteps, lj_md_record* records, int32_t max_records, int32_t* n_records,
+              lj_md_stats* stats);
+
 /* ---- host-buffer call (the reference's measure(), force_cuda.cu:319-342) - */
 /* Uploads q and p from host memory, runs `calls` force calls on the installed
  * list, downloads p, and synchronises.  If the list was installed from host

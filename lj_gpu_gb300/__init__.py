@@ -74,6 +74,33 @@ def make_opts(dt=0.001, cl2=9.0, box=None, precision="fp64", method="auto", lane
     return o
 
 
+class MdParams(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double), ("rc", C.c_double), ("skin", C.c_double), ("box", C.c_double * 3),
+        ("precision", C.c_int32), ("record_every", C.c_int32), ("graph_steps", C.c_int32),
+        ("reserved", C.c_int32 * 5),
+    ]
+
+
+class MdRecord(C.Structure):
+    _fields_ = [("step", C.c_int64), ("kinetic", C.c_double), ("potential", C.c_double)]
+
+
+class MdStats(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("rebuilds", C.c_int64), ("ms_total", C.c_double),
+                ("list_capacity", C.c_int64)]
+
+
+def make_md_params(dt, rc, skin, box, precision="mixed", record_every=0, graph_steps=0):
+    m = MdParams()
+    m.dt, m.rc, m.skin = float(dt), float(rc), float(skin)
+    b = [float(box)] * 3 if isinstance(box, (int, float)) else [float(v) for v in box]
+    m.box[0], m.box[1], m.box[2] = b
+    m.precision = _PRECISION[precision] if isinstance(precision, str) else int(precision)
+    m.record_every, m.graph_steps = int(record_every), int(graph_steps)
+    return m
+
+
 _lib: Optional[C.CDLL] = None
 
 _P = C.c_void_p
@@ -107,6 +134,9 @@ _SIGNATURES = {
                               C.POINTER(C.c_double)]),
     "lj_init_momenta": (C.c_int, [_P, C.c_int32, C.c_double, C.c_uint64]),
     "lj_list_build": (C.c_int, [_P, _P, C.c_int32, C.c_double, _P, C.c_int32]),
+    "lj_md_run": (C.c_int, [_P, _P, _P, C.c_int32, C.POINTER(MdParams), C.c_int32,
+                            C.POINTER(MdRecord), C.c_int32, C.POINTER(C.c_int32),
+                            C.POINTER(MdStats)]),
     "lj_force_mixed_noalloc_aos": (C.c_int, [_P, _P, C.c_int32, C.c_double, C.c_double, _P,
                                              _P, _P, _P, _P]),
 }
@@ -265,6 +295,20 @@ class Context:
         st = lib().lj_force_soa(self._h, ptr(qx), ptr(qy), ptr(qz), ptr(px), ptr(py), ptr(pz),
                                 n, C.byref(opts))
         self._check(st, "force_soa")
+
+    def md_run(self, q, p, params: MdParams, nsteps, max_records=64):
+        """Velocity Verlet on device AoS q, p (in place); returns (records, stats)
+        with records a list of (step, kinetic, potential)."""
+        _check_contig(q, p)
+        recs = (MdRecord * max(1, max_records))()
+        nrec = C.c_int32()
+        st = MdStats()
+        s = lib().lj_md_run(self._h, ptr(q), ptr(p), q.shape[0], C.byref(params), int(nsteps),
+                            recs, max_records, C.byref(nrec), C.byref(st))
+        self._check(s, "md_run")
+        return ([(recs[k].step, recs[k].kinetic, recs[k].potential) for k in range(nrec.value)],
+                {"steps": st.steps, "rebuilds": st.rebuilds, "ms_total": st.ms_total,
+                 "list_capacity": st.list_capacity})
 
     def measure_aos(self, q_host, p_host, opts: ForceOpts, calls=100):
         """The reference's measure(): H2D, `calls` force calls, D2H; returns

@@ -1,0 +1,96 @@
+// lj_ctx.h -- definition of the opaque lj_ctx and its device buffers
+// (shared by the C-ABI translation units).  Not part of the public interface.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "lj_gb300.h"
+#include "lj_internal.h"
+
+namespace ljg {
+
+// Grow-only device buffer.
+template <typename T>
+struct DevBuf {
+  T* ptr = nullptr;
+  size_t cap = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+  cudaError_t ensure(size_t count) {
+    if (count <= cap && ptr) return cudaSuccess;
+    release();
+    const size_t c = count > 0 ? count : 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&ptr), c * sizeof(T));
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      return e;
+    }
+    cap = c;
+    return cudaSuccess;
+  }
+};
+
+struct DevList {
+  DevBuf<int32_t> np, ptr, list;
+  int n = 0;
+  int64_t entries = 0;
+  int max_row = 0;
+  bool valid = false;
+  Csr csr() const { return Csr{n, entries, np.ptr, ptr.ptr, list.ptr}; }
+};
+
+struct MdState;  // lj_md.cu
+void md_state_delete(MdState* m);
+struct MdStateDeleter {
+  void operator()(MdState* m) const { md_state_delete(m); }
+};
+
+}  // namespace ljg
+
+struct lj_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  ljg::DevList half, full;
+  // host copies when the list came from host memory (re-uploaded by measure)
+  bool list_from_host = false;
+  int32_t host_kind = LJ_LIST_HALF;
+  std::vector<int32_t> h_np, h_ptr, h_list;
+  // scratch
+  ljg::DevBuf<int4> qfix;
+  ljg::DevBuf<float> fscratch;
+  ljg::DevBuf<double> maxabs;
+  ljg::DevBuf<int32_t> err2;
+  ljg::DevBuf<int32_t> tmp_i32a, tmp_i32b;
+  ljg::DevBuf<int64_t> tmp_off;
+  ljg::DevBuf<unsigned char> tmp_scan;
+  ljg::DevBuf<double> mq, mp;  // device q / p for lj_measure_aos
+  // neighbour build
+  ljg::DevBuf<int32_t> b_cell, b_count, b_cursor, b_order, b_cnt_half, b_cnt_full;
+  ljg::DevBuf<int64_t> b_start, b_off_half, b_off_full;
+  ljg::DevBuf<int4> b_cq;
+  ljg::DevBuf<unsigned long long> b_minmax;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  // per-stage timing (lj_ctx_set_timing): event triples around force calls
+  bool timing = false;
+  std::vector<cudaEvent_t> tev;  // pool, 3 per recorded call
+  size_t tev_used = 0;
+  double t_ms[3] = {0, 0, 0};
+  int64_t t_calls = 0;
+  // molecular dynamics state (lj_md_run)
+  std::unique_ptr<ljg::MdState, ljg::MdStateDeleter> md;
+};
+
+// Error reporting shared by the C-ABI translation units.
+int lj_fail(lj_ctx* ctx, int code, const char* fmt, ...);

@@ -76,8 +76,11 @@ cudaError_t launch_max_abs(const Particles& part, int n, double* out, cudaStream
 // index (the smallest is kept).
 cudaError_t launch_validate_csr(const Csr& c, int32_t* err, cudaStream_t s);
 // Exclusive scan of n int32 counts into out[0..n] (out[n] = total, int64).
+// Kernels that take `guard` do nothing while *guard == 0 (nullptr: always run).
+cudaError_t launch_zero_i32(int32_t* p, int64_t count, const int32_t* guard, cudaStream_t s);
 cudaError_t launch_scan_counts(const int32_t* counts, int n, int64_t* out, void* tmp,
-                               size_t tmp_bytes, cudaStream_t s);
+                               size_t tmp_bytes, cudaStream_t s,
+                               const int32_t* guard = nullptr);
 size_t scan_tmp_bytes(int n);
 // Full list from a half list: counts, offsets, fill, per-row sort.
 cudaError_t launch_full_from_half_count(const Csr& half, int32_t* deg, cudaStream_t s);
@@ -85,12 +88,13 @@ cudaError_t launch_full_from_half_fill(const Csr& half, const int64_t* off, int3
                                        int32_t* full_list, cudaStream_t s);
 // Rows [off[i], off[i+1]) of `in` sorted ascending (stable) into `out`.
 cudaError_t launch_sort_rows_into(const int64_t* off, int n, const int32_t* in, int32_t* out,
-                                  cudaStream_t s);
+                                  cudaStream_t s, const int32_t* guard = nullptr);
 // Compact copy of CSR rows: out[off[i] + m] = in[ptr[i] + m], m < np[i].
 cudaError_t launch_compact_rows(const int32_t* np, const int32_t* ptr, const int32_t* in,
                                 const int64_t* off, int n, int32_t* out, cudaStream_t s);
 cudaError_t launch_offsets_to_ptr(const int64_t* off, int n, int32_t* ptr, int32_t* np,
-                                  int32_t* max_row, cudaStream_t s);
+                                  int32_t* max_row, cudaStream_t s,
+                                  const int32_t* guard = nullptr);
 // (i, j) pairs with non-decreasing i into CSR rows: counts per i.
 cudaError_t launch_pairs_count(const int32_t* ip, int64_t npairs, int n, int32_t* cnt,
                                int32_t* err, cudaStream_t s);

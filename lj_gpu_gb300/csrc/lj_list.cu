@@ -17,6 +17,20 @@ constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
+// Kernels that may sit in a captured graph take an optional guard: when it
+// is non-null and *guard == 0 the kernel does nothing (fixed-shape rebuilds
+// of the MD loop run only on the steps that need them).
+__device__ __forceinline__ bool guarded_off(const int32_t* guard) {
+  return guard && *(volatile const int32_t*)guard == 0;
+}
+
+__global__ void k_zero_i32(int32_t* p, int64_t count, const int32_t* guard) {
+  if (guarded_off(guard)) return;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count;
+       k += (int64_t)gridDim.x * blockDim.x)
+    p[k] = 0;
+}
+
 __device__ __forceinline__ void report(int32_t* err, int code, int32_t index) {
   atomicMax(err + 0, code);
   atomicMin(err + 1, index);
@@ -63,7 +77,9 @@ __device__ int64_t block_scan_incl(int64_t v, int64_t* warp_tot) {
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int32_t* in, int n,
-                                                            int64_t* tile_sum) {
+                                                            int64_t* tile_sum,
+                                                            const int32_t* guard) {
+  if (guarded_off(guard)) return;
   __shared__ int64_t wt[32];
   const int64_t base = (int64_t)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
   int64_t s = 0;
@@ -74,7 +90,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int32_t* in, 
 }
 
 // exclusive scan of the tile sums in place (one block, serial over chunks)
-__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(int64_t* tile_sum, int nt) {
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(int64_t* tile_sum, int nt,
+                                                                const int32_t* guard) {
+  if (guarded_off(guard)) return;
   __shared__ int64_t wt[32];
   __shared__ int64_t carry;
   if (threadIdx.x == 0) carry = 0;
@@ -93,7 +111,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(int64_t* tile_s
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int32_t* in, int n,
                                                             const int64_t* tile_off,
-                                                            int64_t* out) {
+                                                            int64_t* out, const int32_t* guard) {
+  if (guarded_off(guard)) return;
   __shared__ int64_t wt[32];
   const int64_t base = (int64_t)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
   int32_t v[kScanItems];
@@ -128,7 +147,9 @@ __global__ void k_fill_full(Csr half, const int64_t* off, int32_t* cursor, int32
 }
 
 // one warp per row: stable rank sort, O(len^2 / 32) compares per lane
-__global__ void k_sort_rows(const int64_t* off, int n, const int32_t* in, int32_t* out) {
+__global__ void k_sort_rows(const int64_t* off, int n, const int32_t* in, int32_t* out,
+                            const int32_t* guard) {
+  if (guarded_off(guard)) return;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -148,7 +169,8 @@ __global__ void k_sort_rows(const int64_t* off, int n, const int32_t* in, int32_
 }
 
 __global__ void k_offsets_to_ptr(const int64_t* off, int n, int32_t* ptr, int32_t* np,
-                                 int32_t* max_row) {
+                                 int32_t* max_row, const int32_t* guard) {
+  if (guarded_off(guard)) return;
   int m = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     ptr[i] = (int32_t)off[i];
@@ -207,15 +229,23 @@ size_t scan_tmp_bytes(int n) {
   return sizeof(int64_t) * (size_t)(tiles > 0 ? tiles : 1);
 }
 
+cudaError_t launch_zero_i32(int32_t* p, int64_t count, const int32_t* guard, cudaStream_t s) {
+  if (count > 0) k_zero_i32<<<grid_for(count, 256), 256, 0, s>>>(p, count, guard);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_scan_counts(const int32_t* counts, int n, int64_t* out, void* tmp,
-                               size_t tmp_bytes, cudaStream_t s) {
-  if (n == 0) return cudaMemsetAsync(out, 0, sizeof(int64_t), s);
+                               size_t tmp_bytes, cudaStream_t s, const int32_t* guard) {
+  if (n == 0) {
+    if (guard) return cudaErrorInvalidValue;  // guarded scans need n > 0
+    return cudaMemsetAsync(out, 0, sizeof(int64_t), s);
+  }
   const int tiles = (n + kScanTile - 1) / kScanTile;
   if (tmp_bytes < sizeof(int64_t) * (size_t)tiles) return cudaErrorInvalidValue;
   auto* ts = static_cast<int64_t*>(tmp);
-  k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(counts, n, ts);
-  k_scan_tile_sums<<<1, kScanThreads, 0, s>>>(ts, tiles);
-  k_scan_apply<<<tiles, kScanThreads, 0, s>>>(counts, n, ts, out);
+  k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(counts, n, ts, guard);
+  k_scan_tile_sums<<<1, kScanThreads, 0, s>>>(ts, tiles, guard);
+  k_scan_apply<<<tiles, kScanThreads, 0, s>>>(counts, n, ts, out, guard);
   return cudaGetLastError();
 }
 
@@ -237,8 +267,9 @@ cudaError_t launch_full_from_half_fill(const Csr& half, const int64_t* off, int3
 }
 
 cudaError_t launch_sort_rows_into(const int64_t* off, int n, const int32_t* in, int32_t* out,
-                                  cudaStream_t s) {
-  if (n > 0) k_sort_rows<<<grid_for((int64_t)n * 32, 256), 256, 0, s>>>(off, n, in, out);
+                                  cudaStream_t s, const int32_t* guard) {
+  if (n > 0)
+    k_sort_rows<<<grid_for((int64_t)n * 32, 256), 256, 0, s>>>(off, n, in, out, guard);
   return cudaGetLastError();
 }
 
@@ -249,10 +280,12 @@ cudaError_t launch_compact_rows(const int32_t* np, const int32_t* ptr, const int
 }
 
 cudaError_t launch_offsets_to_ptr(const int64_t* off, int n, int32_t* ptr, int32_t* np,
-                                  int32_t* max_row, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(max_row, 0, sizeof(int32_t), s);
+                                  int32_t* max_row, cudaStream_t s, const int32_t* guard) {
+  cudaError_t e = guard ? launch_zero_i32(max_row, 1, guard, s)
+                        : cudaMemsetAsync(max_row, 0, sizeof(int32_t), s);
   if (e != cudaSuccess) return e;
-  if (n > 0) k_offsets_to_ptr<<<grid_for(n, 256), 256, 0, s>>>(off, n, ptr, np, max_row);
+  if (n > 0)
+    k_offsets_to_ptr<<<grid_for(n, 256), 256, 0, s>>>(off, n, ptr, np, max_row, guard);
   return cudaGetLastError();
 }
 

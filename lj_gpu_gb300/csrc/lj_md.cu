@@ -1,0 +1,496 @@
+// lj_md.cu -- velocity-Verlet molecular dynamics around the force path.
+//
+// The reference never integrates (its 100 "steps" re-kick p from a fixed q,
+// cpu_ref/force_aos.cpp:592-601); this loop is the benchmark spec's extension.
+//
+// One step (m = 1, force routine = kick p += F dt):
+//   drift   q += p dt, wrap into [0, L), fixed-point image of q, and the
+//           displacement against the image at the last list build; any
+//           particle beyond skin/2 raises the rebuild flag        (k_md_drift)
+//   rebuild fixed-shape, flag-guarded kernels: cell binning, counting sort,
+//           count walk, row scan, capacity check, fill walk, row sort,
+//           offsets; they do nothing on steps that need no rebuild
+//   kick    the mixed gather (or FP64 compacted scatter) with dt
+// Half kicks of consecutive steps are merged into one full kick; they are
+// split only where synchronous momenta are needed (energy records and the
+// end), so a run of S steps costs S + 1 + records force calls.  Steps between
+// records run as CUDA graph launches of `graph_steps` captured steps.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "lj_ctx.h"
+#include "lj_nlist.h"
+
+namespace ljg {
+namespace {
+
+enum { F_REBUILD = 0, F_FILL = 1, F_OVERFLOW = 2, F_COUNT = 3, F_MAXROW = 4, F_WORDS = 8 };
+
+__device__ __forceinline__ double wrap_box(double x, double len) {
+  // single shift into [0, len), selected on bit patterns: one FP64 add
+  long long sb = 0;
+  if (!(x < len) && x == x) sb = __double_as_longlong(-len);
+  if (x < 0.0) sb = __double_as_longlong(len);
+  double y = x + __longlong_as_double(sb);
+  if (y >= len) y = 0.0;  // -tiny + len rounds up to len
+  return y;
+}
+
+__global__ void __launch_bounds__(256) k_md_drift(double* __restrict__ q,
+                                                  const double* __restrict__ p, int n, double dt,
+                                                  double lx, double ly, double lz, FixedAxis ax,
+                                                  FixedAxis ay, FixedAxis az,
+                                                  int4* __restrict__ qfix,
+                                                  const int4* __restrict__ qref, float ux,
+                                                  float uy, float uz, float half_skin2,
+                                                  int32_t* __restrict__ flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double* qi = q + 4 * (size_t)i;
+  const double* pi = p + 4 * (size_t)i;
+  const double2 pxy = *reinterpret_cast<const double2*>(pi);
+  const double pz = pi[2];
+  double2 xy = *reinterpret_cast<double2*>(qi);
+  double z = qi[2];
+  xy.x = wrap_box(fma(pxy.x, dt, xy.x), lx);
+  xy.y = wrap_box(fma(pxy.y, dt, xy.y), ly);
+  z = wrap_box(fma(pz, dt, z), lz);
+  *reinterpret_cast<double2*>(qi) = xy;
+  qi[2] = z;
+  const int4 x = make_int4(to_fixed(xy.x, ax), to_fixed(xy.y, ay), to_fixed(z, az), 0);
+  qfix[i] = x;
+  const int4 r = qref[i];
+  const float dx = (float)wrap_sub(x.x, r.x) * ux, dy = (float)wrap_sub(x.y, r.y) * uy,
+              dz = (float)wrap_sub(x.z, r.z) * uz;
+  if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) > half_skin2) flags[F_REBUILD] = 1;
+}
+
+// After the row scan: fill only if the list fits the capacity, else flag.
+__global__ void k_md_capacity(const int64_t* __restrict__ off_end, int64_t cap,
+                              int32_t* __restrict__ flags) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (!flags[F_REBUILD]) return;
+  if (*off_end <= cap) {
+    flags[F_FILL] = 1;
+  } else {
+    flags[F_OVERFLOW] = 1;
+    flags[F_FILL] = 0;
+  }
+}
+
+__global__ void k_md_copy_ref(const int4* __restrict__ qfix, int4* __restrict__ qref, int n,
+                              const int32_t* __restrict__ flags) {
+  if (!flags[F_FILL]) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) qref[i] = qfix[i];
+}
+
+__global__ void k_md_finish(int32_t* flags) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (flags[F_FILL]) flags[F_COUNT] += 1;
+  flags[F_REBUILD] = 0;
+  flags[F_FILL] = 0;
+}
+
+__global__ void k_md_set(int32_t* flags, int word, int value) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) flags[word] = value;
+}
+
+// Potential energy sum over pairs j > i of 4 (r^-12 - r^-6) for r2 <= cl2.
+// Mixed: FP32 pair math from the fixed-point image, Kahan per thread, FP64
+// across threads.  FP64: the FP64 kernels' arithmetic.
+template <bool FP64>
+__global__ void __launch_bounds__(256) k_md_potential(const double* __restrict__ q,
+                                                      const int4* __restrict__ qfix, Csr c,
+                                                      double lx, double ly, double lz,
+                                                      float k_hi, float k_lo, float cl2u_lo,
+                                                      float cl2u_hi, double cl2,
+                                                      double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double u = 0.0;
+  if (i < c.n) {
+    const int cnt = c.np[i], k0 = c.ptr[i];
+    const double* qi = q + 4 * (size_t)i;
+    const double len[3] = {lx, ly, lz};
+    long long hb[3];
+    for (int d = 0; d < 3; d++) hb[d] = __double_as_longlong(0.5 * len[d]);
+    float s = 0.f, comp = 0.f;
+    const int4 xi = qfix[i];
+    for (int m = 0; m < cnt; m++) {
+      const int j = c.list[k0 + m];
+      if (j <= i) continue;
+      const double* qj = q + 4 * (size_t)j;
+      if (FP64) {
+        double d[3];
+        for (int x = 0; x < 3; x++) d[x] = min_image_fp64(qj[x] - qi[x], len[x], hb[x]);
+        const double r2 = fma(d[2], d[2], fma(d[1], d[1], d[0] * d[0]));
+        if (r2 > cl2) continue;
+        const double ir6 = 1.0 / (r2 * r2 * r2);
+        u += 4.0 * ir6 * (ir6 - 1.0);
+      } else {
+        const int4 xj = qfix[j];
+        const float dx = (float)wrap_sub(xj.x, xi.x), dy = (float)wrap_sub(xj.y, xi.y),
+                    dz = (float)wrap_sub(xj.z, xi.z);
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        bool in = r2 <= cl2u_lo;
+        if (!in && r2 <= cl2u_hi) {
+          double d[3];
+          for (int x = 0; x < 3; x++) d[x] = min_image_fp64(qj[x] - qi[x], len[x], hb[x]);
+          in = !(fma(d[2], d[2], fma(d[1], d[1], d[0] * d[0])) > cl2);
+        }
+        if (!in) continue;
+        float inv = 1.0f / r2;
+        inv = fmaf(inv, k_hi, inv * k_lo);
+        const float ir6 = inv * inv * inv;
+        const float e = 4.0f * ir6 * (ir6 - 1.0f);
+        const float y = e - comp;
+        const float t = s + y;
+        comp = (t - s) - y;
+        s = t;
+      }
+    }
+    if (!FP64) u = (double)s - (double)comp;
+  }
+  for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(0xffffffffu, u, o);
+  if ((threadIdx.x & 31) == 0 && u != 0.0) atomicAdd(out, u);
+}
+
+__global__ void __launch_bounds__(256) k_md_kinetic(const double* __restrict__ p, int n,
+                                                    double* __restrict__ out) {
+  double k = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double* b = p + 4 * (size_t)i;
+    k += 0.5 * (b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+  }
+  for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, k);
+}
+
+int grid1(int64_t n, int b) { return (int)std::max<int64_t>(1, (n + b - 1) / b); }
+
+}  // namespace
+
+struct MdState {
+  int n = 0;
+  int64_t cap = 0;
+  CellGrid grid{};
+  ForceLaunch kick_full{}, kick_half{};
+  BuildArgs build{};
+  DevBuf<int4> qfix, qref, cq;
+  DevBuf<int32_t> flags, cell, count, cursor, order, cnt, np, ptr, list, tmp_list;
+  DevBuf<int64_t> start, off;
+  DevBuf<unsigned char> scan_tmp;
+  DevBuf<double> energy;
+  cudaStream_t own_stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  ~MdState() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+};
+
+void md_state_delete(MdState* m) { delete m; }
+
+}  // namespace ljg
+
+using namespace ljg;
+
+namespace {
+
+#define MD_CUDA(ctx, call, what)                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return lj_fail(ctx, e_ == cudaErrorMemoryAllocation ? LJ_ERR_OUT_OF_MEMORY : LJ_ERR_CUDA, \
+                     "%s: %s", what, cudaGetErrorString(e_));                           \
+  } while (0)
+
+// The fixed-shape rebuild sequence (guarded by flags[F_REBUILD]).
+cudaError_t md_rebuild(MdState& m, cudaStream_t s) {
+  const int32_t* g = m.flags.ptr + F_REBUILD;
+  const int32_t* gf = m.flags.ptr + F_FILL;
+  cudaError_t e;
+  if ((e = launch_bin(m.build.q, m.n, m.grid, m.cell.ptr, m.count.ptr, s, g))) return e;
+  if ((e = launch_scan_counts(m.count.ptr, m.grid.ncells, m.start.ptr, m.scan_tmp.ptr,
+                              m.scan_tmp.cap, s, g)))
+    return e;
+  if ((e = launch_place(m.cell.ptr, m.n, m.start.ptr, m.cursor.ptr, m.grid.ncells, m.qfix.ptr,
+                        m.order.ptr, m.cq.ptr, s, g)))
+    return e;
+  if ((e = launch_walk(m.build, false, s, g))) return e;
+  if ((e = launch_scan_counts(m.cnt.ptr, m.n, m.off.ptr, m.scan_tmp.ptr, m.scan_tmp.cap, s, g)))
+    return e;
+  k_md_capacity<<<1, 32, 0, s>>>(m.off.ptr + m.n, m.cap, m.flags.ptr);
+  if ((e = launch_walk(m.build, true, s, gf))) return e;
+  if ((e = launch_sort_rows_into(m.off.ptr, m.n, m.tmp_list.ptr, m.list.ptr, s, gf))) return e;
+  if ((e = launch_offsets_to_ptr(m.off.ptr, m.n, m.ptr.ptr, m.np.ptr, m.flags.ptr + F_MAXROW, s,
+                                 gf)))
+    return e;
+  k_md_copy_ref<<<grid1(m.n, 256), 256, 0, s>>>(m.qfix.ptr, m.qref.ptr, m.n, m.flags.ptr);
+  k_md_finish<<<1, 32, 0, s>>>(m.flags.ptr);
+  return cudaGetLastError();
+}
+
+struct DriftArgs {
+  double* q;
+  const double* p;
+  double dt;
+  double len[3];
+  float unit[3];
+  float half_skin2;
+};
+
+cudaError_t md_step(MdState& m, const DriftArgs& d, const ForceLaunch& kick, cudaStream_t s) {
+  k_md_drift<<<grid1(m.n, 256), 256, 0, s>>>(
+      d.q, d.p, m.n, d.dt, d.len[0], d.len[1], d.len[2], kick.axis[0], kick.axis[1],
+      kick.axis[2], m.qfix.ptr, m.qref.ptr, d.unit[0], d.unit[1], d.unit[2], d.half_skin2,
+      m.flags.ptr);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if ((e = md_rebuild(m, s))) return e;
+  return launch_force(kick, s);
+}
+
+}  // namespace
+
+extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_params* prm,
+                         int32_t nsteps, lj_md_record* records, int32_t max_records,
+                         int32_t* n_records, lj_md_stats* stats) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (n_records) *n_records = 0;
+  if (!prm || n < 1 || nsteps < 0 || !q || !p)
+    return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "bad MD arguments");
+  if ((reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(p)) & 15u)
+    return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "q and p must be 16-byte aligned");
+  if (!(prm->dt > 0.0) || !(prm->rc > 0.0) || !(prm->skin >= 0.0))
+    return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "dt, rc must be > 0 and skin >= 0");
+  if (prm->precision != LJ_PREC_MIXED && prm->precision != LJ_PREC_FP64)
+    return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown precision");
+  const double rs = prm->rc + prm->skin;
+  for (int d = 0; d < 3; d++)
+    if (!(prm->box[d] > 2.0 * rs))
+      return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT,
+                     "box must exceed twice the list radius (minimum image)");
+  if (cudaSetDevice(ctx->device) != cudaSuccess)
+    return lj_fail(ctx, LJ_ERR_CUDA, "set device");
+  if (!ctx->md) ctx->md.reset(new MdState());
+  MdState& m = *ctx->md;
+  cudaStream_t s = ctx->stream;
+  if (!s) {
+    // graphs cannot be captured on the legacy stream: run on our own stream,
+    // ordered after everything the caller queued on the legacy stream
+    if (!m.own_stream) MD_CUDA(ctx, cudaStreamCreateWithFlags(&m.own_stream, cudaStreamNonBlocking),
+                               "stream");
+    MD_CUDA(ctx, cudaStreamSynchronize(nullptr), "sync");
+    s = m.own_stream;
+  }
+  const bool mixed = prm->precision == LJ_PREC_MIXED;
+
+  // ---- buffers and constants -------------------------------------------
+  m.n = n;
+  const double vol = prm->box[0] * prm->box[1] * prm->box[2];
+  const double per = 4.18879 * rs * rs * rs * (n / vol);  // full-list partners / particle
+  const int64_t want = (int64_t)std::ceil(n * per * (mixed ? 1.0 : 0.5) * 1.6) + 4096;
+  if (want > 0x7fffffffll)
+    return lj_fail(ctx, LJ_ERR_UNSUPPORTED, "neighbour list would exceed 2^31 entries");
+  m.cap = std::max<int64_t>(m.cap, want);
+  for (int d = 0; d < 3; d++) {
+    m.grid.nc[d] = std::max(1, std::min(1024, (int)std::floor(prm->box[d] / rs)));
+    m.grid.lo[d] = 0.0;
+    m.grid.inv_w[d] = m.grid.nc[d] / prm->box[d];
+  }
+  m.grid.ncells = m.grid.nc[0] * m.grid.nc[1] * m.grid.nc[2];
+  m.grid.periodic = 1;
+  MD_CUDA(ctx, m.qfix.ensure(n), "alloc");
+  MD_CUDA(ctx, m.qref.ensure(n), "alloc");
+  MD_CUDA(ctx, m.cq.ensure(n), "alloc");
+  MD_CUDA(ctx, m.flags.ensure(F_WORDS), "alloc");
+  MD_CUDA(ctx, m.cell.ensure(n), "alloc");
+  MD_CUDA(ctx, m.order.ensure(n), "alloc");
+  MD_CUDA(ctx, m.cnt.ensure(n), "alloc");
+  MD_CUDA(ctx, m.np.ensure(n), "alloc");
+  MD_CUDA(ctx, m.ptr.ensure(n), "alloc");
+  MD_CUDA(ctx, m.count.ensure(m.grid.ncells), "alloc");
+  MD_CUDA(ctx, m.cursor.ensure(m.grid.ncells), "alloc");
+  MD_CUDA(ctx, m.start.ensure((size_t)m.grid.ncells + 1), "alloc");
+  MD_CUDA(ctx, m.off.ensure((size_t)n + 1), "alloc");
+  MD_CUDA(ctx, m.scan_tmp.ensure(scan_tmp_bytes(std::max(n, m.grid.ncells))), "alloc");
+  MD_CUDA(ctx, m.list.ensure((size_t)m.cap), "alloc");
+  MD_CUDA(ctx, m.tmp_list.ensure((size_t)m.cap), "alloc");
+  MD_CUDA(ctx, m.energy.ensure(2), "alloc");
+  MD_CUDA(ctx, cudaMemsetAsync(m.flags.ptr, 0, sizeof(int32_t) * F_WORDS, s), "memset");
+
+  ForceLaunch K{};
+  K.part.soa = 0;
+  K.part.q = q;
+  K.part.p = p;
+  K.csr = Csr{n, m.cap, m.np.ptr, m.ptr.ptr, m.list.ptr};
+  K.box.on = 1;
+  for (int d = 0; d < 3; d++) {
+    K.box.len[d] = prm->box[d];
+    K.box.half[d] = 0.5 * prm->box[d];
+  }
+  K.cl2 = prm->rc * prm->rc;
+  K.precision = prm->precision;
+  K.method = mixed ? LJ_METHOD_GATHER_FULL : LJ_METHOD_SCATTER_HALF;
+  K.kernel = 2;
+  K.unroll = 4;
+  K.lanes = mixed ? 4 : 4;
+  K.block = 128;
+  K.qfix = m.qfix.ptr;
+  make_fixed_frame(K, 0.0);
+  ForceLaunch Kfull = K, Khalf = K;
+  Kfull.dt = prm->dt;
+  Khalf.dt = 0.5 * prm->dt;
+
+  BuildArgs& b = m.build;
+  b = BuildArgs{};
+  b.q = q;
+  b.n = n;
+  b.grid = m.grid;
+  b.search = rs;
+  for (int d = 0; d < 3; d++) {
+    b.box[d] = prm->box[d];
+    b.unit[d] = K.unit[d];
+  }
+  b.aniso = K.aniso;
+  b.start = m.start.ptr;
+  b.order = m.order.ptr;
+  b.cq = m.cq.ptr;
+  b.cell = m.cell.ptr;
+  b.want_half = mixed ? 0 : 1;
+  b.want_full = mixed ? 1 : 0;
+  b.cnt_half = b.cnt_full = m.cnt.ptr;
+  b.off_half = b.off_full = m.off.ptr;
+  b.out_half = b.out_full = m.tmp_list.ptr;
+
+  DriftArgs D{};
+  D.q = q;
+  D.p = p;
+  D.dt = prm->dt;
+  for (int d = 0; d < 3; d++) {
+    D.len[d] = prm->box[d];
+    D.unit[d] = (float)K.unit[d];
+  }
+  D.half_skin2 = (float)(0.25 * prm->skin * prm->skin);
+
+  cudaEvent_t t0, t1;
+  MD_CUDA(ctx, cudaEventCreate(&t0), "event");
+  MD_CUDA(ctx, cudaEventCreate(&t1), "event");
+  struct EvGuard {
+    cudaEvent_t a, b;
+    ~EvGuard() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } evg{t0, t1};
+  MD_CUDA(ctx, cudaEventRecord(t0, s), "event");
+
+  // ---- initial image and list ----------------------------------------------
+  MD_CUDA(ctx, launch_fixed_image(K, s), "image");
+  k_md_set<<<1, 32, 0, s>>>(m.flags.ptr, F_REBUILD, 1);
+  MD_CUDA(ctx, md_rebuild(m, s), "initial build");
+
+  int32_t nrec = 0;
+  auto read_flags = [&](int32_t* f) -> int {
+    MD_CUDA(ctx, cudaMemcpyAsync(f, m.flags.ptr, sizeof(int32_t) * F_WORDS,
+                                 cudaMemcpyDeviceToHost, s), "flags");
+    MD_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+    return LJ_OK;
+  };
+  auto record = [&](int64_t step) -> int {
+    if (!records || nrec >= max_records) return LJ_OK;
+    MD_CUDA(ctx, cudaMemsetAsync(m.energy.ptr, 0, 2 * sizeof(double), s), "memset");
+    const double u2 = K.unit[0] * K.unit[0];
+    const double cl2u = K.cl2 / u2;
+    const float khi = (float)(1.0 / u2), klo = (float)(1.0 / u2 - (double)khi);
+    const Csr c{n, 0, m.np.ptr, m.ptr.ptr, m.list.ptr};
+    if (mixed && !K.aniso)
+      k_md_potential<false><<<grid1(n, 256), 256, 0, s>>>(
+          q, m.qfix.ptr, c, K.box.len[0], K.box.len[1], K.box.len[2], khi, klo,
+          (float)(cl2u * (1 - 4e-6)), (float)(cl2u * (1 + 4e-6)), K.cl2, m.energy.ptr + 1);
+    else
+      k_md_potential<true><<<grid1(n, 256), 256, 0, s>>>(
+          q, m.qfix.ptr, c, K.box.len[0], K.box.len[1], K.box.len[2], 0.f, 0.f, 0.f, 0.f, K.cl2,
+          m.energy.ptr + 1);
+    k_md_kinetic<<<std::min(grid1(n, 256), 1024), 256, 0, s>>>(p, n, m.energy.ptr);
+    double e[2];
+    MD_CUDA(ctx, cudaGetLastError(), "energy");
+    MD_CUDA(ctx, cudaMemcpyAsync(e, m.energy.ptr, sizeof e, cudaMemcpyDeviceToHost, s), "energy");
+    MD_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+    records[nrec].step = step;
+    records[nrec].kinetic = e[0];
+    records[nrec].potential = e[1];
+    nrec++;
+    return LJ_OK;
+  };
+
+  int32_t f[F_WORDS];
+  int rc;
+  if ((rc = read_flags(f))) return rc;
+  if (f[F_OVERFLOW]) return lj_fail(ctx, LJ_ERR_LIST_OVERFLOW, "initial list exceeds capacity");
+  if ((rc = record(0))) return rc;
+
+  // ---- graph of `graph_steps` plain steps ----------------------------------
+  const int gsteps = prm->graph_steps > 0 ? prm->graph_steps : 20;
+  if (m.graph) {
+    cudaGraphExecDestroy(m.graph);
+    m.graph = nullptr;
+  }
+  if (gsteps > 1) {
+    cudaGraph_t g = nullptr;
+    MD_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
+    cudaError_t ce = cudaSuccess;
+    for (int k = 0; k < gsteps && ce == cudaSuccess; k++) ce = md_step(m, D, Kfull, s);
+    cudaError_t ee = cudaStreamEndCapture(s, &g);
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return lj_fail(ctx, LJ_ERR_CUDA, "graph capture: %s",
+                     cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+    }
+    ce = cudaGraphInstantiate(&m.graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return lj_fail(ctx, LJ_ERR_CUDA, "graph instantiate");
+    m.graph_steps = gsteps;
+  }
+
+  // ---- integrate -------------------------------------------------------------
+  const int every = prm->record_every > 0 ? prm->record_every : nsteps;
+  if (nsteps > 0) MD_CUDA(ctx, launch_force(Khalf, s), "kick");  // p(1/2)
+  int64_t step = 0;
+  while (step < nsteps) {
+    int64_t stop = std::min<int64_t>(nsteps, (step / every + 1) * every);
+    int64_t plain = stop - step - 1;
+    while (m.graph && plain >= m.graph_steps) {
+      MD_CUDA(ctx, cudaGraphLaunch(m.graph, s), "graph launch");
+      plain -= m.graph_steps;
+    }
+    for (; plain > 0; plain--) MD_CUDA(ctx, md_step(m, D, Kfull, s), "step");
+    MD_CUDA(ctx, md_step(m, D, Khalf, s), "step");  // p(stop), synchronous
+    if ((rc = read_flags(f))) return rc;
+    if (f[F_OVERFLOW])
+      return lj_fail(ctx, LJ_ERR_LIST_OVERFLOW,
+                     "neighbour list exceeded its capacity of %lld entries",
+                     (long long)m.cap);
+    if (stop % every == 0 || stop == nsteps)
+      if ((rc = record(stop))) return rc;
+    if (stop < nsteps) MD_CUDA(ctx, launch_force(Khalf, s), "kick");
+    step = stop;
+  }
+  MD_CUDA(ctx, cudaEventRecord(t1, s), "event");
+  if ((rc = read_flags(f))) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, t0, t1);
+  if (stats) {
+    stats->steps = nsteps;
+    stats->rebuilds = f[F_COUNT];
+    stats->ms_total = ms;
+    stats->list_capacity = m.cap;
+  }
+  if (n_records) *n_records = nrec;
+  if (!ctx->stream) MD_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+  return LJ_OK;
+}

@@ -27,8 +27,13 @@ __device__ __forceinline__ int wrap_cell(int c, int nc) {
   return c < 0 ? c + nc : c;
 }
 
+__device__ __forceinline__ bool off_guard(const int32_t* guard) {
+  return guard && *(volatile const int32_t*)guard == 0;
+}
+
 __global__ void k_bin(const double* __restrict__ q, int n, CellGrid g, int32_t* __restrict__ cell,
-                      int32_t* __restrict__ count) {
+                      int32_t* __restrict__ count, const int32_t* guard) {
+  if (off_guard(guard)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* b = q + 4 * (size_t)i;
@@ -47,7 +52,9 @@ __global__ void k_bin(const double* __restrict__ q, int n, CellGrid g, int32_t* 
 
 __global__ void k_place(const int32_t* __restrict__ cell, int n, const int64_t* __restrict__ start,
                         int32_t* __restrict__ cursor, const int4* __restrict__ qfix,
-                        int32_t* __restrict__ order, int4* __restrict__ cq) {
+                        int32_t* __restrict__ order, int4* __restrict__ cq,
+                        const int32_t* guard) {
+  if (off_guard(guard)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int c = cell[i];
@@ -138,7 +145,9 @@ __global__ void __launch_bounds__(128) k_walk(const double* __restrict__ q, int 
                                               const int64_t* __restrict__ off_half,
                                               const int64_t* __restrict__ off_full,
                                               int32_t* __restrict__ out_half,
-                                              int32_t* __restrict__ out_full) {
+                                              int32_t* __restrict__ out_full,
+                                              const int32_t* guard) {
+  if (off_guard(guard)) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const int i = order[s];
@@ -221,22 +230,25 @@ cudaError_t launch_minmax(const double* q, int n, unsigned long long* out6, cuda
 }
 
 cudaError_t launch_bin(const double* q, int n, const CellGrid& g, int32_t* cell, int32_t* count,
-                       cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int32_t) * (size_t)g.ncells, s);
+                       cudaStream_t s, const int32_t* guard) {
+  cudaError_t e = guard ? launch_zero_i32(count, g.ncells, guard, s)
+                        : cudaMemsetAsync(count, 0, sizeof(int32_t) * (size_t)g.ncells, s);
   if (e != cudaSuccess || n == 0) return e;
-  k_bin<<<grid_of(n, 256, 0), 256, 0, s>>>(q, n, g, cell, count);
+  k_bin<<<grid_of(n, 256, 0), 256, 0, s>>>(q, n, g, cell, count, guard);
   return cudaGetLastError();
 }
 
 cudaError_t launch_place(const int32_t* cell, int n, const int64_t* start, int32_t* cursor,
-                         int ncells, const int4* qfix, int32_t* order, int4* cq, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncells, s);
+                         int ncells, const int4* qfix, int32_t* order, int4* cq, cudaStream_t s,
+                         const int32_t* guard) {
+  cudaError_t e = guard ? launch_zero_i32(cursor, ncells, guard, s)
+                        : cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncells, s);
   if (e != cudaSuccess || n == 0) return e;
-  k_place<<<grid_of(n, 256, 0), 256, 0, s>>>(cell, n, start, cursor, qfix, order, cq);
+  k_place<<<grid_of(n, 256, 0), 256, 0, s>>>(cell, n, start, cursor, qfix, order, cq, guard);
   return cudaGetLastError();
 }
 
-cudaError_t launch_walk(const BuildArgs& a, bool fill, cudaStream_t s) {
+cudaError_t launch_walk(const BuildArgs& a, bool fill, cudaStream_t s, const int32_t* guard) {
   if (a.n == 0) return cudaSuccess;
   BuildConsts k{};
   const double u2 = a.aniso ? 1.0 : a.unit[0] * a.unit[0];
@@ -259,11 +271,11 @@ cudaError_t launch_walk(const BuildArgs& a, bool fill, cudaStream_t s) {
   if (fill)
     k_walk<true><<<blocks, 128, 0, s>>>(a.q, a.n, a.grid, a.start, a.order, a.cq, a.cell, k,
                                         a.want_half, a.want_full, nullptr, nullptr, a.off_half,
-                                        a.off_full, a.out_half, a.out_full);
+                                        a.off_full, a.out_half, a.out_full, guard);
   else
     k_walk<false><<<blocks, 128, 0, s>>>(a.q, a.n, a.grid, a.start, a.order, a.cq, a.cell, k,
                                          a.want_half, a.want_full, a.cnt_half, a.cnt_full,
-                                         nullptr, nullptr, nullptr, nullptr);
+                                         nullptr, nullptr, nullptr, nullptr, guard);
   return cudaGetLastError();
 }
 

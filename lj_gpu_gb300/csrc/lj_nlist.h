@@ -5,6 +5,8 @@
 #include <cstring>
 #include <cuda_runtime.h>
 
+#include "lj_internal.h"
+
 namespace ljg {
 
 struct CellGrid {
@@ -38,10 +40,13 @@ struct BuildArgs {
 
 double key_to_double(unsigned long long k);
 cudaError_t launch_minmax(const double* q, int n, unsigned long long* out6, cudaStream_t s);
+// `guard` (optional): the kernels do nothing while *guard == 0.
 cudaError_t launch_bin(const double* q, int n, const CellGrid& g, int32_t* cell, int32_t* count,
-                       cudaStream_t s);
+                       cudaStream_t s, const int32_t* guard = nullptr);
 cudaError_t launch_place(const int32_t* cell, int n, const int64_t* start, int32_t* cursor,
-                         int ncells, const int4* qfix, int32_t* order, int4* cq, cudaStream_t s);
-cudaError_t launch_walk(const BuildArgs& a, bool fill, cudaStream_t s);
+                         int ncells, const int4* qfix, int32_t* order, int4* cq, cudaStream_t s,
+                         const int32_t* guard = nullptr);
+cudaError_t launch_walk(const BuildArgs& a, bool fill, cudaStream_t s,
+                        const int32_t* guard = nullptr);
 
 }  // namespace ljg

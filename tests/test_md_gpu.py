@@ -1,0 +1,108 @@
+"""Velocity-Verlet MD on the GPU against an FP64 oracle integration.
+
+The reference has no integrator; the oracle composes its restated force
+routine (cpu_ref/force_aos.cpp:192-224) into velocity Verlet: kick dt/2,
+drift, kick dt/2, with the list rebuilt from scratch every step.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def oracle_vv(q, p, L, rc, dt, steps):
+    q, p = q.copy(), p.copy()
+    O = ol.oracle()
+    box = np.array([L, L, L])
+    for _ in range(steps):
+        half = ol.build_list(q, rc + 0.2, box=L)
+        ol.force_sorted_aos(q, p, *half, cl2=rc * rc, dt=0.5 * dt, box=L)
+        O.lj_or_drift(q, p, q.shape[0], dt, box.ctypes.data)
+        half = ol.build_list(q, rc + 0.2, box=L)
+        ol.force_sorted_aos(q, p, *half, cl2=rc * rc, dt=0.5 * dt, box=L)
+    return q, p
+
+
+def periodic_diff(a, b, L):
+    d = a[:, :3] - b[:, :3]
+    return d - L * np.round(d / L)
+
+
+@pytest.mark.parametrize("graph_steps", [1, 8])
+def test_fp64_md_matches_oracle_velocity_verlet(engine, graph_steps):
+    q, L = ol.init_fcc_periodic(5, 0.8, 0.05, seed=12)  # 500 particles, L = claimed
+    p = engine.init_momenta(q.shape[0], 1.0, seed=4)
+    rc, skin, dt, steps = 2.5, 0.3, 0.005, 60
+    qd, pd = _dev(q), _dev(p)
+    prm = engine.make_md_params(dt, rc, skin, L, precision="fp64", record_every=20,
+                                graph_steps=graph_steps)
+    with engine.Context(0) as ctx:
+        recs, stats = ctx.md_run(qd, pd, prm, steps)
+    import torch
+    torch.cuda.synchronize()
+    qg, pg = qd.cpu().numpy(), pd.cpu().numpy()
+    qo, po = oracle_vv(q, p, L, rc, dt, steps)
+    assert np.abs(periodic_diff(qg, qo, L)).max() < 1e-11
+    e = ol.rel_errors(pg, po)
+    assert e["max_rel_rms"] < 1e-10, e
+    assert [r[0] for r in recs] == [0, 20, 40, 60]
+    assert stats["steps"] == steps and stats["rebuilds"] >= 1
+    # energies of the FP64 run against the oracle's at the end
+    half = ol.build_list(qo, rc, box=L)
+    u = ol.potential_half(qo, *half, cl2=rc * rc, box=L)
+    k = ol.oracle().lj_or_kinetic(po, po.shape[0])
+    assert abs(recs[-1][2] - u) <= 1e-9 * abs(u) and abs(recs[-1][1] - k) <= 1e-9 * abs(k)
+
+
+def test_mixed_md_tracks_fp64_and_conserves(engine):
+    q, L = ol.init_fcc_periodic(6, 1.0, 0.05, seed=21)  # 864 particles
+    p = engine.init_momenta(q.shape[0], 1.0, seed=9)
+    rc, skin, dt = 2.5, 0.3, 0.005
+    out = {}
+    for prec in ("fp64", "mixed"):
+        qd, pd = _dev(q), _dev(p)
+        prm = engine.make_md_params(dt, rc, skin, L, precision=prec, record_every=50)
+        with engine.Context(0) as ctx:
+            recs, stats = ctx.md_run(qd, pd, prm, 200)
+        import torch
+        torch.cuda.synchronize()
+        out[prec] = (qd.cpu().numpy(), pd.cpu().numpy(), recs, stats)
+    qf, pf, rf, _ = out["fp64"]
+    qm, pm, rm, sm = out["mixed"]
+    # short trajectories stay together (chaos has not amplified FP32 errors yet)
+    assert np.abs(periodic_diff(qm, qf, L)).max() < 1e-5
+    # total momentum: the FP64 scatter applies +f and -f (zero to rounding);
+    # the mixed gather evaluates f_ij and f_ji separately in FP32, so the sum
+    # drifts at the FP32 rounding level of the forces
+    assert np.abs(out["fp64"][1][:, :3].sum(axis=0)).max() < 1e-11
+    assert np.abs(pm[:, :3].sum(axis=0)).max() < 1e-4
+    # the cut (unshifted, as in the reference) potential jumps by |4(rc^-12 -
+    # rc^-6)| ~ 0.016 whenever a pair crosses rc, so the total energy is not a
+    # constant of this model; the mixed run must reproduce the FP64 energies
+    e0 = rf[0][1] + rf[0][2]
+    assert [r[0] for r in rm] == [r[0] for r in rf]
+    for a, b in zip(rm, rf):
+        assert abs((a[1] + a[2]) - (b[1] + b[2])) <= 1e-5 * abs(e0), (a, b)
+        assert abs(a[2] - b[2]) <= 1e-5 * abs(b[2]), (a, b)
+    assert sm["rebuilds"] >= 2
+
+
+def test_md_list_overflow_is_reported(engine):
+    # 500 particles packed into a corner of a large box: the capacity estimate
+    # from the mean density is far too small, and the run must say so
+    q, _ = ol.init_fcc_periodic(5, 1.0, 0.05, seed=3)
+    L = 40.0
+    p = np.zeros_like(q)
+    qd, pd = _dev(q), _dev(p)
+    prm = engine.make_md_params(0.005, 2.5, 0.3, L, precision="mixed")
+    with engine.Context(0) as ctx:
+        with pytest.raises(engine.LJError) as e:
+            ctx.md_run(qd, pd, prm, 5)
+        assert e.value.status == engine.LJ_ERR_LIST_OVERFLOW
