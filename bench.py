@@ -55,6 +55,12 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="rho0.5_108k",
+                    choices=["rho0.5_108k", "rho1_108k", "precision_1m", "large_8m"],
+                    help="rho0.5_108k: the headline force benchmark; rho1_108k: the same at "
+                         "rho = 1; precision_1m: 1,000,188-particle mixed MD with force "
+                         "errors against FP64 every 100 steps; large_8m: 8,001,504-particle "
+                         "MD, mixed and FP64 back to back")
     return ap.parse_args()
 
 
@@ -200,7 +206,7 @@ def algorithmic_bytes(method, layout, P, N):
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
-def run_ours(args, dist):
+def run_ours(args, dist, density=DENSITY):
     import torch
     import lj_gpu_gb300 as lj
     from lj_gpu_gb300 import _build
@@ -209,7 +215,7 @@ def run_ours(args, dist):
     dev = torch.device("cuda", dist.local)
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
-    q, L = lj.init_fcc(NCELL, DENSITY, JITTER, SEED)
+    q, L = lj.init_fcc(NCELL, density, JITTER, SEED)
     N = q.shape[0]
     qd = torch.from_numpy(q).to(dev)
     qs = [torch.from_numpy(np.ascontiguousarray(q[:, d])).to(dev) for d in range(3)]
@@ -339,7 +345,7 @@ def run_ours(args, dist):
 
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(q, L, P, sample_calls=5)
+        cpu = cpu_baseline(q, L, P, sample_calls=5 if density <= 0.5 else 2)
 
     line = {
         "metric": METRIC, "value": dist.world * P / head["s_per_call"] / 1e9, "unit": UNIT,
@@ -347,7 +353,8 @@ def run_ours(args, dist):
         "ms_per_step": head["s_per_call"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math, f64 q/p",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "N": N, "pairs_half": P, "pairs_full": P_full,
+        "config": {"workload": WORKLOAD.replace("rho=0.5", f"rho={density}").replace(
+                       "L=60", f"L={L:.4g}"), "N": N, "pairs_half": P, "pairs_full": P_full,
                    "max_row_half": max_half, "max_row_full": max_full, "box": L,
                    "variant": best_mixed, "step": "one force call",
                    "l2": "flushed before every timed call (512 MiB write)",
@@ -359,6 +366,111 @@ def run_ours(args, dist):
     }
     ctx.close()
     return line
+
+
+# ---------------------------------------------------------------------------
+# MD workloads
+# ---------------------------------------------------------------------------
+def force_errors(torch, lj, L, qd, rs=RS):
+    """Mixed vs FP64 forces of the engine on the same positions (the FP64 path
+    is held to 1e-12 of the oracle by the parity tests)."""
+    ctx = lj.Context(qd.device.index or 0, stream=torch.cuda.current_stream())
+    ctx.build_list(qd, rs, box=L)
+    out = {}
+    for prec in ("mixed", "fp64"):
+        p = torch.zeros_like(qd)
+        ctx.force_aos(qd, p, lj.make_opts(dt=1.0, cl2=RC * RC, box=L, precision=prec))
+        out[prec] = p[:, :3]
+    torch.cuda.synchronize()
+    d = torch.linalg.norm(out["mixed"] - out["fp64"], dim=1)
+    r = torch.linalg.norm(out["fp64"], dim=1)
+    rms = torch.sqrt(torch.mean(r * r))
+    per = d / r
+    ctx.close()
+    return {"max_rel": float(per.max()), "rms_rel": float(torch.sqrt(torch.mean(per * per))),
+            "max_rel_rms": float(d.max() / rms), "global_rel": float(torch.linalg.norm(d) /
+                                                                     torch.linalg.norm(r))}
+
+
+def run_precision(args, dist):
+    """1,000,188 particles (FCC 63^3 x 4), rho = 1, rc 3.0, skin 0.3, MB momenta
+    at T* = 1, 1,000 mixed velocity-Verlet steps at dt = 0.005."""
+    import torch
+    import lj_gpu_gb300 as lj
+    from lj_gpu_gb300 import _build
+    _build.build()
+    dev = torch.device("cuda", dist.local)
+    torch.cuda.set_device(dev)
+    q, L = lj.init_fcc(63, 1.0, JITTER, SEED)
+    N = q.shape[0]
+    p = lj.init_momenta(N, 1.0, SEED + 1)
+    qd, pd = torch.from_numpy(q).to(dev), torch.from_numpy(p).to(dev)
+    errors = [dict(step=0, **force_errors(torch, lj, L, qd))]
+    ctx = lj.Context(dist.local, stream=torch.cuda.current_stream())
+    prm = lj.make_md_params(DT, RC, RS - RC, L, precision="mixed", record_every=100)
+    records, ms, rebuilds = [], 0.0, 0
+    for seg in range(10):
+        recs, st = ctx.md_run(qd, pd, prm, 100)
+        ms += st["ms_total"]
+        rebuilds += st["rebuilds"]
+        records += [(r[0] + 100 * seg, r[1], r[2]) for r in recs if seg == 0 or r[0] > 0]
+        errors.append(dict(step=100 * (seg + 1), **force_errors(torch, lj, L, qd)))
+    e0 = records[0][1] + records[0][2]
+    drift = max(abs(r[1] + r[2] - e0) for r in records) / abs(e0)
+    ctx.close()
+    return {"metric": "mixed-precision MD force error vs FP64 and energy drift",
+            "workload": "precision_1m", "N": N, "box": L, "steps": 1000, "dt": DT,
+            "ms_per_step": ms / 1000, "rebuilds": rebuilds,
+            "max_rel_rms_force_error": max(e["max_rel_rms"] for e in errors),
+            "global_rel_force_error": max(e["global_rel"] for e in errors),
+            "force_errors": errors, "energy_drift_rel": drift,
+            "energies": [{"step": r[0], "kinetic": r[1], "potential": r[2]} for r in records],
+            "note": "the cut, unshifted potential (the reference's) jumps when pairs cross "
+                    "rc, so total energy drifts in FP64 too; force errors are against the "
+                    "engine's FP64 path on the same positions"}
+
+
+def run_large(args, dist):
+    """8,001,504 particles (FCC 126^3 x 4), rho = 1, rc 3.0, skin 0.3, MB
+    momenta at T* = 1, 500 steps at dt = 0.005 with a rebuild every 20 steps,
+    mixed then FP64 from the same initial state."""
+    import torch
+    import lj_gpu_gb300 as lj
+    from lj_gpu_gb300 import _build
+    _build.build()
+    dev = torch.device("cuda", dist.local)
+    torch.cuda.set_device(dev)
+    steps = 500 if args.steps >= 100 else args.steps
+    q, L = lj.init_fcc(126, 1.0, JITTER, SEED)
+    N = q.shape[0]
+    p = lj.init_momenta(N, 1.0, SEED + 1)
+    hbm, _ = peaks()
+    out = {"metric": "MD ns/step and HBM GB/s, mixed vs FP64", "workload": "large_8m", "N": N,
+           "box": L, "steps": steps, "dt": DT, "rebuild_every": 20}
+    for prec in ("mixed", "fp64"):
+        qd, pd = torch.from_numpy(q).to(dev), torch.from_numpy(p).to(dev)
+        ctx = lj.Context(dist.local, stream=torch.cuda.current_stream())
+        prm = lj.make_md_params(DT, RC, RS - RC, L, precision=prec, record_every=steps,
+                                rebuild_every=20)
+        recs, st = ctx.md_run(qd, pd, prm, steps)
+        ctx.build_list(qd, RS, box=L, kinds=("half",))
+        _, P, _ = ctx.list_info("half")
+        ctx.close()
+        ms = st["ms_total"] / steps
+        # per step: force call (gather 8P + 104N, scatter 4P + 104N), drift
+        # (q r/w, p read, image write, reference image read: 112N), rebuild
+        # list write amortised over 20 steps
+        fbytes = (8 * P if prec == "mixed" else 4 * P) + 104 * N
+        step_bytes = fbytes + 112 * N + (8 * P if prec == "mixed" else 4 * P) / 20
+        out[prec] = {"ms_per_step": ms, "ns_per_step_per_particle": ms * 1e6 / N,
+                     "gpairs": P / (ms * 1e-3) / 1e9, "hbm_gbs": step_bytes / (ms * 1e-3) / 1e9,
+                     "hbm_frac": step_bytes / (ms * 1e-3) / 1e9 / hbm,
+                     "rebuilds": st["rebuilds"], "pairs_half": P,
+                     "energy_first_last": [recs[0][1] + recs[0][2], recs[-1][1] + recs[-1][2]]}
+        del qd, pd
+        torch.cuda.empty_cache()
+    out["mixed_over_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -425,7 +537,12 @@ def main():
         line = run_reference(args, dist)
     else:
         dist = Dist("nccl")
-        line = run_ours(args, dist)
+        if args.workload == "precision_1m":
+            line = run_precision(args, dist)
+        elif args.workload == "large_8m":
+            line = run_large(args, dist)
+        else:
+            line = run_ours(args, dist, 1.0 if args.workload == "rho1_108k" else DENSITY)
     if dist.rank == 0 and line is not None:
         print(json.dumps(line))
     dist.close()

@@ -221,7 +221,9 @@ typedef struct lj_md_params {
   int32_t precision;      /* LJ_PREC_MIXED (gather) or LJ_PREC_FP64 (scatter) */
   int32_t record_every;   /* energies every k steps (0: at 0 and at the end) */
   int32_t graph_steps;    /* steps per captured CUDA graph (0: 20, 1: no graph) */
-  int32_t reserved[5];
+  int32_t rebuild_every;  /* 0: rebuild when a particle moved > skin/2 since the
+                             last build; k > 0: also every k steps */
+  int32_t reserved[4];
 } lj_md_params;
 
 typedef struct lj_md_record {

@@ -78,7 +78,7 @@ class MdParams(C.Structure):
     _fields_ = [
         ("dt", C.c_double), ("rc", C.c_double), ("skin", C.c_double), ("box", C.c_double * 3),
         ("precision", C.c_int32), ("record_every", C.c_int32), ("graph_steps", C.c_int32),
-        ("reserved", C.c_int32 * 5),
+        ("rebuild_every", C.c_int32), ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -91,13 +91,15 @@ class MdStats(C.Structure):
                 ("list_capacity", C.c_int64)]
 
 
-def make_md_params(dt, rc, skin, box, precision="mixed", record_every=0, graph_steps=0):
+def make_md_params(dt, rc, skin, box, precision="mixed", record_every=0, graph_steps=0,
+                   rebuild_every=0):
     m = MdParams()
     m.dt, m.rc, m.skin = float(dt), float(rc), float(skin)
     b = [float(box)] * 3 if isinstance(box, (int, float)) else [float(v) for v in box]
     m.box[0], m.box[1], m.box[2] = b
     m.precision = _PRECISION[precision] if isinstance(precision, str) else int(precision)
     m.record_every, m.graph_steps = int(record_every), int(graph_steps)
+    m.rebuild_every = int(rebuild_every)
     return m
 
 

@@ -25,7 +25,15 @@
 namespace ljg {
 namespace {
 
-enum { F_REBUILD = 0, F_FILL = 1, F_OVERFLOW = 2, F_COUNT = 3, F_MAXROW = 4, F_WORDS = 8 };
+enum {
+  F_REBUILD = 0,  // a rebuild is due this step
+  F_FILL = 1,     // the rebuild fits the capacity (fill, sort, offsets run)
+  F_OVERFLOW = 2, // a rebuild did not fit
+  F_COUNT = 3,    // rebuilds done
+  F_MAXROW = 4,   // longest row of the last build
+  F_STEP = 5,     // steps taken (drives rebuild_every)
+  F_WORDS = 8
+};
 
 __device__ __forceinline__ double wrap_box(double x, double len) {
   // single shift into [0, len), selected on bit patterns: one FP64 add
@@ -44,8 +52,15 @@ __global__ void __launch_bounds__(256) k_md_drift(double* __restrict__ q,
                                                   int4* __restrict__ qfix,
                                                   const int4* __restrict__ qref, float ux,
                                                   float uy, float uz, float half_skin2,
+                                                  int rebuild_every,
                                                   int32_t* __restrict__ flags) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    // step counter; flags[F_STEP] is read by no other thread of this kernel
+    const int stepno = flags[F_STEP] + 1;
+    flags[F_STEP] = stepno;
+    if (rebuild_every > 0 && stepno % rebuild_every == 0) flags[F_REBUILD] = 1;
+  }
   if (i >= n) return;
   double* qi = q + 4 * (size_t)i;
   const double* pi = p + 4 * (size_t)i;
@@ -240,13 +255,14 @@ struct DriftArgs {
   double len[3];
   float unit[3];
   float half_skin2;
+  int rebuild_every;
 };
 
 cudaError_t md_step(MdState& m, const DriftArgs& d, const ForceLaunch& kick, cudaStream_t s) {
   k_md_drift<<<grid1(m.n, 256), 256, 0, s>>>(
       d.q, d.p, m.n, d.dt, d.len[0], d.len[1], d.len[2], kick.axis[0], kick.axis[1],
       kick.axis[2], m.qfix.ptr, m.qref.ptr, d.unit[0], d.unit[1], d.unit[2], d.half_skin2,
-      m.flags.ptr);
+      d.rebuild_every, m.flags.ptr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if ((e = md_rebuild(m, s))) return e;
@@ -293,7 +309,10 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   m.n = n;
   const double vol = prm->box[0] * prm->box[1] * prm->box[2];
   const double per = 4.18879 * rs * rs * rs * (n / vol);  // full-list partners / particle
-  const int64_t want = (int64_t)std::ceil(n * per * (mixed ? 1.0 : 0.5) * 1.6) + 4096;
+  // expected entries times a slack for density fluctuations (generous for
+  // small systems, 30 % above the mean for large ones)
+  const double slack = n < 100000 ? 1.6 : 1.3;
+  const int64_t want = (int64_t)std::ceil(n * per * (mixed ? 1.0 : 0.5) * slack) + 4096;
   if (want > 0x7fffffffll)
     return lj_fail(ctx, LJ_ERR_UNSUPPORTED, "neighbour list would exceed 2^31 entries");
   m.cap = std::max<int64_t>(m.cap, want);
@@ -376,6 +395,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     D.unit[d] = (float)K.unit[d];
   }
   D.half_skin2 = (float)(0.25 * prm->skin * prm->skin);
+  D.rebuild_every = prm->rebuild_every > 0 ? prm->rebuild_every : 0;
 
   cudaEvent_t t0, t1;
   MD_CUDA(ctx, cudaEventCreate(&t0), "event");
