@@ -754,6 +754,11 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
                                   ctx->tmp_scan.cap, s), "cell scan");
   LJ_CUDA(ctx, launch_place(ctx->b_cell.ptr, n, ctx->b_start.ptr, ctx->b_cursor.ptr, g.ncells,
                             ctx->qfix.ptr, ctx->b_order.ptr, ctx->b_cq.ptr, s), "place");
+  // per-cell ordering (deterministic walks)
+  LJ_CUDA(ctx, ctx->b_order2.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->b_cq2.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, launch_sort_cells(ctx->b_start.ptr, g.ncells, ctx->b_order.ptr, ctx->b_cq.ptr,
+                                 ctx->b_order2.ptr, ctx->b_cq2.ptr, s), "cell sort");
   BuildArgs a{};
   a.q = q;
   a.n = n;
@@ -765,63 +770,63 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
   }
   a.aniso = F.aniso;
   a.start = ctx->b_start.ptr;
-  a.order = ctx->b_order.ptr;
-  a.cq = ctx->b_cq.ptr;
+  a.order = ctx->b_order2.ptr;
+  a.cq = ctx->b_cq2.ptr;
   a.cell = ctx->b_cell.ptr;
-  a.want_half = want_half;
-  a.want_full = want_full;
-  LJ_CUDA(ctx, ctx->b_cnt_half.ensure((size_t)n), "alloc");
-  LJ_CUDA(ctx, ctx->b_cnt_full.ensure((size_t)n), "alloc");
-  LJ_CUDA(ctx, ctx->b_off_half.ensure((size_t)n + 1), "alloc");
-  LJ_CUDA(ctx, ctx->b_off_full.ensure((size_t)n + 1), "alloc");
-  a.cnt_half = ctx->b_cnt_half.ptr;
-  a.cnt_full = ctx->b_cnt_full.ptr;
-  LJ_CUDA(ctx, launch_walk(a, false, s), "count walk");
-  int64_t tot[2] = {0, 0};
+  // padded row length from the mean density of the occupied volume, doubled
+  // and rebuilt if any row does not fit
+  double vol = 1.0;
+  for (int d = 0; d < 3; d++) vol *= g.nc[d] / g.inv_w[d];
+  const double per = 4.18879 * rs * rs * rs * (std::max(n, 1) / std::max(vol, 1e-300));
+  int maxrow = std::max(32, ((int)std::ceil(per * 1.5) + 32 + 31) / 32 * 32);
   ctx->half.valid = false;
   ctx->full.valid = false;
-  for (int kind = 0; kind < 2; kind++) {
-    if (!(kind == 0 ? want_half : want_full)) continue;
-    int32_t* cnt = kind == 0 ? a.cnt_half : a.cnt_full;
-    int64_t* off = kind == 0 ? ctx->b_off_half.ptr : ctx->b_off_full.ptr;
-    LJ_CUDA(ctx, launch_scan_counts(cnt, n, off, ctx->tmp_scan.ptr, ctx->tmp_scan.cap, s),
-            "row scan");
-    LJ_CUDA(ctx, cudaMemcpyAsync(&tot[kind], off + n, sizeof(int64_t), cudaMemcpyDeviceToHost,
-                                 s), "total");
-  }
-  LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
-  for (int kind = 0; kind < 2; kind++)
-    if (tot[kind] > 0x7fffffffll)
-      return fail(ctx, LJ_ERR_LIST_OVERFLOW, "list would exceed 2^31-1 entries");
-  a.off_half = ctx->b_off_half.ptr;
-  a.off_full = ctx->b_off_full.ptr;
-  LJ_CUDA(ctx, ctx->tmp_i32a.ensure((size_t)std::max<int64_t>(tot[0], 1)), "alloc");
-  LJ_CUDA(ctx, ctx->tmp_i32b.ensure((size_t)std::max<int64_t>(tot[1], 1)), "alloc");
-  a.out_half = ctx->tmp_i32a.ptr;
-  a.out_full = ctx->tmp_i32b.ptr;
-  LJ_CUDA(ctx, launch_walk(a, true, s), "fill walk");
   LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
+  LJ_CUDA(ctx, ctx->b_cnt_half.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->b_off_half.ensure((size_t)n + 1), "alloc");
   for (int kind = 0; kind < 2; kind++) {
     if (!(kind == 0 ? want_half : want_full)) continue;
+    for (;;) {
+      if (maxrow > 1 << 20)
+        return fail(ctx, LJ_ERR_LIST_OVERFLOW, "a neighbour row exceeds 2^20 entries");
+      LJ_CUDA(ctx, ctx->tmp_i32a.ensure((size_t)n * maxrow), "alloc");
+      LJ_CUDA(ctx, cudaMemsetAsync(ctx->err2.ptr, 0, sizeof(int32_t), s), "memset");
+      LJ_CUDA(ctx, launch_build_rows(a, kind == 0, maxrow, ctx->tmp_i32a.ptr,
+                                     ctx->b_cnt_half.ptr, ctx->err2.ptr, s), "row build");
+      int32_t ovf = 0;
+      LJ_CUDA(ctx, cudaMemcpyAsync(&ovf, ctx->err2.ptr, sizeof ovf, cudaMemcpyDeviceToHost, s),
+              "read");
+      LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+      if (!ovf) break;
+      maxrow *= 2;
+    }
+    int64_t total = 0;
+    LJ_CUDA(ctx, launch_scan_counts(ctx->b_cnt_half.ptr, n, ctx->b_off_half.ptr, ctx->tmp_scan.ptr,
+                                    ctx->tmp_scan.cap, s), "row scan");
+    LJ_CUDA(ctx, cudaMemcpyAsync(&total, ctx->b_off_half.ptr + n, sizeof total,
+                                 cudaMemcpyDeviceToHost, s), "total");
+    LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+    if (total > 0x7fffffffll)
+      return fail(ctx, LJ_ERR_LIST_OVERFLOW, "list would exceed 2^31-1 entries");
     DevList& l = kind == 0 ? ctx->half : ctx->full;
-    const int64_t* off = kind == 0 ? a.off_half : a.off_full;
+    LJ_CUDA(ctx, ctx->tmp_i32b.ensure((size_t)std::max<int64_t>(total, 1)), "alloc");
+    LJ_CUDA(ctx, launch_compact_padded(ctx->b_cnt_half.ptr, ctx->tmp_i32a.ptr, maxrow,
+                                       ctx->b_off_half.ptr, n, ctx->tmp_i32b.ptr, s), "compact");
     LJ_CUDA(ctx, l.np.ensure((size_t)n), "alloc");
     LJ_CUDA(ctx, l.ptr.ensure((size_t)n), "alloc");
-    LJ_CUDA(ctx, l.list.ensure((size_t)std::max<int64_t>(tot[kind], 1)), "alloc");
-    LJ_CUDA(ctx, launch_sort_rows_into(off, n, kind == 0 ? a.out_half : a.out_full, l.list.ptr,
-                                       s), "row sort");
-    LJ_CUDA(ctx, launch_offsets_to_ptr(off, n, l.ptr.ptr, l.np.ptr, ctx->err2.ptr + kind, s),
-            "ptr");
-  }
-  int32_t mr[2] = {0, 0};
-  LJ_CUDA(ctx, cudaMemcpyAsync(mr, ctx->err2.ptr, sizeof mr, cudaMemcpyDeviceToHost, s), "read");
-  LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
-  for (int kind = 0; kind < 2; kind++) {
-    if (!(kind == 0 ? want_half : want_full)) continue;
-    DevList& l = kind == 0 ? ctx->half : ctx->full;
+    LJ_CUDA(ctx, l.list.ensure((size_t)std::max<int64_t>(total, 1)), "alloc");
+    // rows ascending in j, as makepair + sortpair produce them
+    LJ_CUDA(ctx, launch_sort_rows_into(ctx->b_off_half.ptr, n, ctx->tmp_i32b.ptr, l.list.ptr, s),
+            "row sort");
+    LJ_CUDA(ctx, launch_offsets_to_ptr(ctx->b_off_half.ptr, n, l.ptr.ptr, l.np.ptr,
+                                       ctx->err2.ptr + 1, s), "ptr");
+    int32_t mr = 0;
+    LJ_CUDA(ctx, cudaMemcpyAsync(&mr, ctx->err2.ptr + 1, sizeof mr, cudaMemcpyDeviceToHost, s),
+            "read");
+    LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
     l.n = n;
-    l.entries = tot[kind];
-    l.max_row = mr[kind];
+    l.entries = total;
+    l.max_row = mr;
     l.valid = true;
   }
   ctx->list_from_host = false;

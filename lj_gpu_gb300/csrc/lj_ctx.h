@@ -77,9 +77,10 @@ struct lj_ctx {
   ljg::DevBuf<unsigned char> tmp_scan;
   ljg::DevBuf<double> mq, mp;  // device q / p for lj_measure_aos
   // neighbour build
-  ljg::DevBuf<int32_t> b_cell, b_count, b_cursor, b_order, b_cnt_half, b_cnt_full;
-  ljg::DevBuf<int64_t> b_start, b_off_half, b_off_full;
-  ljg::DevBuf<int4> b_cq;
+  ljg::DevBuf<int32_t> b_cell, b_count, b_cursor, b_order, b_cnt_half;
+  ljg::DevBuf<int64_t> b_start, b_off_half;
+  ljg::DevBuf<int4> b_cq, b_cq2;
+  ljg::DevBuf<int32_t> b_order2;
   ljg::DevBuf<unsigned long long> b_minmax;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   // per-stage timing (lj_ctx_set_timing): event triples around force calls

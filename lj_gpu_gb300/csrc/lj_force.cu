@@ -348,6 +348,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const C
 // warp.  Pairs outside the cutoff are masked with a select, not a branch.  The
 // U terms of one step are summed in FP32 and the step sum enters the Kahan
 // accumulator, so compensation costs 12/U operations per pair.
+// Accepts padded rows (C.ptr == nullptr, row i at i * C.stride).
 template <int G, int U, bool PBC, bool SOA, bool ANISO>
 __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const Csr C,
                                                         const int4* __restrict__ qfix,
@@ -356,11 +357,12 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
   const int i = t / G;
   const int lane = t & (G - 1);
   const bool valid = i < C.n;
-  int cnt = 0, k0 = 0;
+  int cnt = 0;
+  int64_t k0 = 0;
   int4 xi = make_int4(0, 0, 0, 0);
   if (valid) {
     cnt = __ldg(C.np + i);
-    k0 = __ldg(C.ptr + i);
+    k0 = row_start(C, i);
     xi = __ldg(qfix + i);
   }
   int cmax = cnt;

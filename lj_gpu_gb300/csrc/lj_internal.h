@@ -22,14 +22,21 @@ struct Particles {
   double* pz;
 };
 
-// A device CSR list.
+// A device CSR list.  Rows start at ptr[i], or, when ptr is null, at
+// i * stride (padded rows with a 64-bit start; kernels that accept this say
+// so).
 struct Csr {
   int n;
   int64_t entries;
   const int32_t* np;
   const int32_t* ptr;
   const int32_t* list;
+  int64_t stride;
 };
+
+__device__ __forceinline__ int64_t row_start(const Csr& c, int i) {
+  return c.ptr ? (int64_t)__ldg(c.ptr + i) : (int64_t)i * c.stride;
+}
 
 struct Periodic {
   int on;

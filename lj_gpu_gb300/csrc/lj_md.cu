@@ -8,8 +8,9 @@
 //           displacement against the image at the last list build; any
 //           particle beyond skin/2 raises the rebuild flag        (k_md_drift)
 //   rebuild fixed-shape, flag-guarded kernels: cell binning, counting sort,
-//           count walk, row scan, capacity check, fill walk, row sort,
-//           offsets; they do nothing on steps that need no rebuild
+//           per-cell ordering, warp-cooperative row build into padded rows
+//           (+ compaction for the FP64 scatter); they do nothing on steps
+//           that need no rebuild
 //   kick    the mixed gather (or FP64 compacted scatter) with dt
 // Half kicks of consecutive steps are merged into one full kick; they are
 // split only where synchronous momenta are needed (energy records and the
@@ -81,31 +82,17 @@ __global__ void __launch_bounds__(256) k_md_drift(double* __restrict__ q,
   if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) > half_skin2) flags[F_REBUILD] = 1;
 }
 
-// After the row scan: fill only if the list fits the capacity, else flag.
-__global__ void k_md_capacity(const int64_t* __restrict__ off_end, int64_t cap,
-                              int32_t* __restrict__ flags) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  if (!flags[F_REBUILD]) return;
-  if (*off_end <= cap) {
-    flags[F_FILL] = 1;
-  } else {
-    flags[F_OVERFLOW] = 1;
-    flags[F_FILL] = 0;
-  }
-}
-
 __global__ void k_md_copy_ref(const int4* __restrict__ qfix, int4* __restrict__ qref, int n,
                               const int32_t* __restrict__ flags) {
-  if (!flags[F_FILL]) return;
+  if (!flags[F_REBUILD]) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) qref[i] = qfix[i];
 }
 
 __global__ void k_md_finish(int32_t* flags) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  if (flags[F_FILL]) flags[F_COUNT] += 1;
+  if (flags[F_REBUILD]) flags[F_COUNT] += 1;
   flags[F_REBUILD] = 0;
-  flags[F_FILL] = 0;
 }
 
 __global__ void k_md_set(int32_t* flags, int word, int value) {
@@ -125,7 +112,8 @@ __global__ void __launch_bounds__(256) k_md_potential(const double* __restrict__
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double u = 0.0;
   if (i < c.n) {
-    const int cnt = c.np[i], k0 = c.ptr[i];
+    const int cnt = c.np[i];
+    const int64_t k0 = row_start(c, i);
     const double* qi = q + 4 * (size_t)i;
     const double len[3] = {lx, ly, lz};
     long long hb[3];
@@ -192,8 +180,9 @@ struct MdState {
   CellGrid grid{};
   ForceLaunch kick_full{}, kick_half{};
   BuildArgs build{};
-  DevBuf<int4> qfix, qref, cq;
-  DevBuf<int32_t> flags, cell, count, cursor, order, cnt, np, ptr, list, tmp_list;
+  int maxrow = 0;
+  DevBuf<int4> qfix, qref, cq, cq2;
+  DevBuf<int32_t> flags, cell, count, cursor, order, order2, cnt, ptr, rows, list;
   DevBuf<int64_t> start, off;
   DevBuf<unsigned char> scan_tmp;
   DevBuf<double> energy;
@@ -222,10 +211,12 @@ namespace {
                      "%s: %s", what, cudaGetErrorString(e_));                           \
   } while (0)
 
-// The fixed-shape rebuild sequence (guarded by flags[F_REBUILD]).
-cudaError_t md_rebuild(MdState& m, cudaStream_t s) {
+// The fixed-shape rebuild sequence (guarded by flags[F_REBUILD]): bin, cell
+// offsets, placement, per-cell ordering, warp-cooperative row build into the
+// padded rows.  The mixed gather reads the padded rows directly; the FP64
+// scatter sweeps rows flat, so its rows are compacted (scan + copy).
+cudaError_t md_rebuild(MdState& m, bool compact, cudaStream_t s) {
   const int32_t* g = m.flags.ptr + F_REBUILD;
-  const int32_t* gf = m.flags.ptr + F_FILL;
   cudaError_t e;
   if ((e = launch_bin(m.build.q, m.n, m.grid, m.cell.ptr, m.count.ptr, s, g))) return e;
   if ((e = launch_scan_counts(m.count.ptr, m.grid.ncells, m.start.ptr, m.scan_tmp.ptr,
@@ -234,15 +225,22 @@ cudaError_t md_rebuild(MdState& m, cudaStream_t s) {
   if ((e = launch_place(m.cell.ptr, m.n, m.start.ptr, m.cursor.ptr, m.grid.ncells, m.qfix.ptr,
                         m.order.ptr, m.cq.ptr, s, g)))
     return e;
-  if ((e = launch_walk(m.build, false, s, g))) return e;
-  if ((e = launch_scan_counts(m.cnt.ptr, m.n, m.off.ptr, m.scan_tmp.ptr, m.scan_tmp.cap, s, g)))
+  if ((e = launch_sort_cells(m.start.ptr, m.grid.ncells, m.order.ptr, m.cq.ptr, m.order2.ptr,
+                             m.cq2.ptr, s, g)))
     return e;
-  k_md_capacity<<<1, 32, 0, s>>>(m.off.ptr + m.n, m.cap, m.flags.ptr);
-  if ((e = launch_walk(m.build, true, s, gf))) return e;
-  if ((e = launch_sort_rows_into(m.off.ptr, m.n, m.tmp_list.ptr, m.list.ptr, s, gf))) return e;
-  if ((e = launch_offsets_to_ptr(m.off.ptr, m.n, m.ptr.ptr, m.np.ptr, m.flags.ptr + F_MAXROW, s,
-                                 gf)))
+  if ((e = launch_build_rows(m.build, m.build.want_half != 0, m.maxrow, m.rows.ptr, m.cnt.ptr,
+                             m.flags.ptr + F_OVERFLOW, s, g)))
     return e;
+  if (compact) {
+    if ((e = launch_scan_counts(m.cnt.ptr, m.n, m.off.ptr, m.scan_tmp.ptr, m.scan_tmp.cap, s, g)))
+      return e;
+    if ((e = launch_compact_padded(m.cnt.ptr, m.rows.ptr, m.maxrow, m.off.ptr, m.n, m.list.ptr,
+                                   s, g)))
+      return e;
+    if ((e = launch_offsets_to_ptr(m.off.ptr, m.n, m.ptr.ptr, m.cnt.ptr, m.flags.ptr + F_MAXROW,
+                                   s, g)))
+      return e;
+  }
   k_md_copy_ref<<<grid1(m.n, 256), 256, 0, s>>>(m.qfix.ptr, m.qref.ptr, m.n, m.flags.ptr);
   k_md_finish<<<1, 32, 0, s>>>(m.flags.ptr);
   return cudaGetLastError();
@@ -265,7 +263,7 @@ cudaError_t md_step(MdState& m, const DriftArgs& d, const ForceLaunch& kick, cud
       d.rebuild_every, m.flags.ptr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  if ((e = md_rebuild(m, s))) return e;
+  if ((e = md_rebuild(m, kick.method == LJ_METHOD_SCATTER_HALF, s))) return e;
   return launch_force(kick, s);
 }
 
@@ -309,13 +307,11 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   m.n = n;
   const double vol = prm->box[0] * prm->box[1] * prm->box[2];
   const double per = 4.18879 * rs * rs * rs * (n / vol);  // full-list partners / particle
-  // expected entries times a slack for density fluctuations (generous for
-  // small systems, 30 % above the mean for large ones)
-  const double slack = n < 100000 ? 1.6 : 1.3;
-  const int64_t want = (int64_t)std::ceil(n * per * (mixed ? 1.0 : 0.5) * slack) + 4096;
-  if (want > 0x7fffffffll)
-    return lj_fail(ctx, LJ_ERR_UNSUPPORTED, "neighbour list would exceed 2^31 entries");
-  m.cap = std::max<int64_t>(m.cap, want);
+  // padded row length: the mean full row plus room for density fluctuations
+  m.maxrow = std::max(m.maxrow, ((int)std::ceil(per * 1.5) + 32 + 31) / 32 * 32);
+  m.cap = (int64_t)n * m.maxrow;
+  if (!mixed && per * 0.5 * n * 1.3 > 0x7fffffff)
+    return lj_fail(ctx, LJ_ERR_UNSUPPORTED, "compacted half list would exceed 2^31 entries");
   for (int d = 0; d < 3; d++) {
     m.grid.nc[d] = std::max(1, std::min(1024, (int)std::floor(prm->box[d] / rs)));
     m.grid.lo[d] = 0.0;
@@ -326,19 +322,22 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   MD_CUDA(ctx, m.qfix.ensure(n), "alloc");
   MD_CUDA(ctx, m.qref.ensure(n), "alloc");
   MD_CUDA(ctx, m.cq.ensure(n), "alloc");
+  MD_CUDA(ctx, m.cq2.ensure(n), "alloc");
   MD_CUDA(ctx, m.flags.ensure(F_WORDS), "alloc");
   MD_CUDA(ctx, m.cell.ensure(n), "alloc");
   MD_CUDA(ctx, m.order.ensure(n), "alloc");
+  MD_CUDA(ctx, m.order2.ensure(n), "alloc");
   MD_CUDA(ctx, m.cnt.ensure(n), "alloc");
-  MD_CUDA(ctx, m.np.ensure(n), "alloc");
   MD_CUDA(ctx, m.ptr.ensure(n), "alloc");
   MD_CUDA(ctx, m.count.ensure(m.grid.ncells), "alloc");
   MD_CUDA(ctx, m.cursor.ensure(m.grid.ncells), "alloc");
   MD_CUDA(ctx, m.start.ensure((size_t)m.grid.ncells + 1), "alloc");
   MD_CUDA(ctx, m.off.ensure((size_t)n + 1), "alloc");
   MD_CUDA(ctx, m.scan_tmp.ensure(scan_tmp_bytes(std::max(n, m.grid.ncells))), "alloc");
-  MD_CUDA(ctx, m.list.ensure((size_t)m.cap), "alloc");
-  MD_CUDA(ctx, m.tmp_list.ensure((size_t)m.cap), "alloc");
+  MD_CUDA(ctx, m.rows.ensure((size_t)m.cap), "alloc");
+  // the compacted half list holds about half of the padded capacity
+  const int64_t half_cap = std::min<int64_t>(m.cap, 0x7fffffffll);
+  if (!mixed) MD_CUDA(ctx, m.list.ensure((size_t)half_cap), "alloc");
   MD_CUDA(ctx, m.energy.ensure(2), "alloc");
   MD_CUDA(ctx, cudaMemsetAsync(m.flags.ptr, 0, sizeof(int32_t) * F_WORDS, s), "memset");
 
@@ -346,7 +345,10 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   K.part.soa = 0;
   K.part.q = q;
   K.part.p = p;
-  K.csr = Csr{n, m.cap, m.np.ptr, m.ptr.ptr, m.list.ptr};
+  // mixed: padded rows read in place (64-bit row starts i * maxrow); FP64:
+  // compacted rows with int32 offsets
+  K.csr = mixed ? Csr{n, m.cap, m.cnt.ptr, nullptr, m.rows.ptr, (int64_t)m.maxrow}
+                : Csr{n, m.cap, m.cnt.ptr, m.ptr.ptr, m.list.ptr, 0};
   K.box.on = 1;
   for (int d = 0; d < 3; d++) {
     K.box.len[d] = prm->box[d];
@@ -377,14 +379,11 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   }
   b.aniso = K.aniso;
   b.start = m.start.ptr;
-  b.order = m.order.ptr;
-  b.cq = m.cq.ptr;
+  b.order = m.order2.ptr;  // per-cell sorted order (k_sort_cells output)
+  b.cq = m.cq2.ptr;
   b.cell = m.cell.ptr;
   b.want_half = mixed ? 0 : 1;
   b.want_full = mixed ? 1 : 0;
-  b.cnt_half = b.cnt_full = m.cnt.ptr;
-  b.off_half = b.off_full = m.off.ptr;
-  b.out_half = b.out_full = m.tmp_list.ptr;
 
   DriftArgs D{};
   D.q = q;
@@ -412,7 +411,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   // ---- initial image and list ----------------------------------------------
   MD_CUDA(ctx, launch_fixed_image(K, s), "image");
   k_md_set<<<1, 32, 0, s>>>(m.flags.ptr, F_REBUILD, 1);
-  MD_CUDA(ctx, md_rebuild(m, s), "initial build");
+  MD_CUDA(ctx, md_rebuild(m, !mixed, s), "initial build");
 
   int32_t nrec = 0;
   auto read_flags = [&](int32_t* f) -> int {
@@ -427,7 +426,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     const double u2 = K.unit[0] * K.unit[0];
     const double cl2u = K.cl2 / u2;
     const float khi = (float)(1.0 / u2), klo = (float)(1.0 / u2 - (double)khi);
-    const Csr c{n, 0, m.np.ptr, m.ptr.ptr, m.list.ptr};
+    const Csr c = K.csr;
     if (mixed && !K.aniso)
       k_md_potential<false><<<grid1(n, 256), 256, 0, s>>>(
           q, m.qfix.ptr, c, K.box.len[0], K.box.len[1], K.box.len[2], khi, klo,
@@ -451,7 +450,8 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   int32_t f[F_WORDS];
   int rc;
   if ((rc = read_flags(f))) return rc;
-  if (f[F_OVERFLOW]) return lj_fail(ctx, LJ_ERR_LIST_OVERFLOW, "initial list exceeds capacity");
+  if (f[F_OVERFLOW])
+    return lj_fail(ctx, LJ_ERR_LIST_OVERFLOW, "a neighbour row exceeds %d entries", m.maxrow);
   if ((rc = record(0))) return rc;
 
   // ---- graph of `graph_steps` plain steps ----------------------------------
@@ -493,8 +493,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     if ((rc = read_flags(f))) return rc;
     if (f[F_OVERFLOW])
       return lj_fail(ctx, LJ_ERR_LIST_OVERFLOW,
-                     "neighbour list exceeded its capacity of %lld entries",
-                     (long long)m.cap);
+                     "a neighbour row exceeded its capacity of %d entries", m.maxrow);
     if (stop % every == 0 || stop == nsteps)
       if ((rc = record(stop))) return rc;
     if (stop < nsteps) MD_CUDA(ctx, launch_force(Khalf, s), "kick");

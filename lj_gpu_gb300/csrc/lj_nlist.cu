@@ -6,11 +6,11 @@
 //   1. bin:   cell of every particle (cell side >= search radius), counts
 //   2. sort:  counting sort of particle indices by cell; the fixed-point
 //             positions are gathered into cell order for coalesced reads
-//   3. count: per particle, candidates in the 27 surrounding cells that pass
-//             r2 < rs^2 (half: j > i, full: j != i)
-//   4. scan:  row offsets
-//   5. fill:  same walk, writing j
-//   6. sort rows ascending (rank sort), so the CSR equals the reference's
+//   3. order: the slots of every cell sorted by particle index (deterministic)
+//   4. rows:  one warp per cell walks the 27 surrounding cells and writes the
+//             j with r2 < rs^2 (half: j > i, full: j != i) into padded rows
+//   5. scan + compact into a CSR; rows sorted ascending (rank sort), so the
+//             CSR equals the reference's
 //
 // Membership is decided in FP32 from the exact int32 fixed-point separation;
 // candidates within a relative 4e-6 of the search sphere are re-decided in
@@ -131,55 +131,104 @@ __device__ __forceinline__ void for_neighbour_cells(int cid, const CellGrid& g, 
       }
 }
 
-// One thread per particle, in cell order (slot s), so neighbouring threads
-// read the same cells.  pass 0 counts, pass 1 writes.
-template <bool FILL>
-__global__ void __launch_bounds__(128) k_walk(const double* __restrict__ q, int n, CellGrid g,
-                                              const int64_t* __restrict__ start,
-                                              const int32_t* __restrict__ order,
-                                              const int4* __restrict__ cq,
-                                              const int32_t* __restrict__ cell, BuildConsts k,
-                                              int want_half, int want_full,
-                                              int32_t* __restrict__ cnt_half,
-                                              int32_t* __restrict__ cnt_full,
-                                              const int64_t* __restrict__ off_half,
-                                              const int64_t* __restrict__ off_full,
-                                              int32_t* __restrict__ out_half,
-                                              int32_t* __restrict__ out_full,
-                                              const int32_t* guard) {
+// Deterministic order inside every cell: the slots of cell c sorted by
+// particle index (one warp per cell, stable rank sort, out of place).  The
+// counting-sort placement before it uses atomics, so its order varies run to
+// run; this makes every later walk -- and every floating-point sum over a
+// row -- reproducible.
+__global__ void k_sort_cells(const int64_t* __restrict__ start, int ncells,
+                             const int32_t* __restrict__ order, const int4* __restrict__ cq,
+                             int32_t* __restrict__ order2, int4* __restrict__ cq2,
+                             const int32_t* guard) {
   if (off_guard(guard)) return;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const int i = order[s];
-  const int4 xi = cq[s];
-  int nh = 0, nf = 0;
-  int64_t wh = 0, wf = 0;
-  if (FILL) {
-    if (want_half) wh = off_half[i];
-    if (want_full) wf = off_full[i];
-  }
-  for_neighbour_cells(cell[i], g, [&](int c) {
-    const int b = (int)start[c], e = (int)start[c + 1];
-    for (int t = b; t < e; t++) {
-      const int j = order[t];
-      if (j == i) continue;
-      if (!want_full && j < i) continue;
-      if (!within(xi, cq[t], q, i, j, k)) continue;
-      if (want_full) {
-        if (FILL) out_full[wf + nf] = j;
-        nf++;
-      }
-      if (want_half && j > i) {
-        if (FILL) out_half[wh + nh] = j;
-        nh++;
-      }
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncells; c += nwarps) {
+    const int s0 = (int)start[c], s1 = (int)start[c + 1];
+    for (int a = s0 + lane; a < s1; a += 32) {
+      const int v = order[a];
+      int rank = 0;
+      for (int b = s0; b < s1; b++) rank += order[b] < v;  // indices are distinct
+      order2[s0 + rank] = v;
+      cq2[s0 + rank] = cq[a];
     }
-  });
-  if (!FILL) {
-    if (want_half) cnt_half[i] = nh;
-    if (want_full) cnt_full[i] = nf;
   }
 }
+
+// Warp-cooperative neighbour build into a padded row layout (row i at
+// i * maxrow, length cnt[i]).  One warp per cell: the lanes hold up to 32 of
+// the cell's particles; every neighbour cell is read 32 particles at a time
+// with coalesced loads and broadcast to all lanes by shuffles, so a candidate
+// costs shuffles and FP32/integer arithmetic instead of a scattered load.
+// Rows come out in cell-walk order (deterministic after k_sort_cells).  A row
+// longer than maxrow is truncated and raises *overflow.
+template <bool HALF>
+__global__ void __launch_bounds__(128) k_build_rows(const double* __restrict__ q, CellGrid g,
+                                                    const int64_t* __restrict__ start,
+                                                    const int32_t* __restrict__ order,
+                                                    const int4* __restrict__ cq, BuildConsts k,
+                                                    int maxrow, int32_t* __restrict__ rows,
+                                                    int32_t* __restrict__ cnt,
+                                                    int32_t* __restrict__ overflow,
+                                                    const int32_t* guard) {
+  if (off_guard(guard)) return;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < g.ncells; c += nwarps) {
+    const int s0 = (int)start[c], s1 = (int)start[c + 1];
+    for (int a = s0; a < s1; a += 32) {
+      const bool act = a + lane < s1;
+      const int i = act ? order[a + lane] : -1;
+      const int4 xi = act ? cq[a + lane] : make_int4(0, 0, 0, 0);
+      const size_t base = act ? (size_t)i * (size_t)maxrow : 0;
+      int count = 0;
+      for_neighbour_cells(c, g, [&](int c2) {
+        const int t0 = (int)start[c2], t1 = (int)start[c2 + 1];
+        for (int b = t0; b < t1; b += 32) {
+          int jl = -1;
+          int4 xl = make_int4(0, 0, 0, 0);
+          if (b + lane < t1) {
+            jl = order[b + lane];
+            xl = cq[b + lane];
+          }
+          const int m = min(32, t1 - b);
+          for (int kk = 0; kk < m; kk++) {
+            const int j = __shfl_sync(kFullMask, jl, kk);
+            int4 xj;
+            xj.x = __shfl_sync(kFullMask, xl.x, kk);
+            xj.y = __shfl_sync(kFullMask, xl.y, kk);
+            xj.z = __shfl_sync(kFullMask, xl.z, kk);
+            xj.w = 0;
+            if (act && j != i && (!HALF || j > i) && within(xi, xj, q, i, j, k)) {
+              if (count < maxrow) rows[base + count] = j;
+              count++;
+            }
+          }
+        }
+      });
+      if (act) {
+        cnt[i] = min(count, maxrow);
+        if (count > maxrow) atomicMax(overflow, 1);
+      }
+    }
+  }
+}
+
+// Compact copy of padded rows: out[off[i] + m] = rows[i * maxrow + m].
+__global__ void k_compact_padded(const int32_t* __restrict__ cnt, const int32_t* __restrict__ rows,
+                                 int maxrow, const int64_t* __restrict__ off, int n,
+                                 int32_t* __restrict__ out, const int32_t* guard) {
+  if (off_guard(guard)) return;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nwarps) {
+    const int c = cnt[i];
+    const size_t a = (size_t)i * (size_t)maxrow;
+    const int64_t b = off[i];
+    for (int m = lane; m < c; m += 32) out[b + m] = rows[a + m];
+  }
+}
+
 
 __global__ void k_minmax(const double* __restrict__ q, int n, unsigned long long* out) {
   // out[0..2]: max over +x (as ordered keys), out[3..5]: max over -x
@@ -248,8 +297,7 @@ cudaError_t launch_place(const int32_t* cell, int n, const int64_t* start, int32
   return cudaGetLastError();
 }
 
-cudaError_t launch_walk(const BuildArgs& a, bool fill, cudaStream_t s, const int32_t* guard) {
-  if (a.n == 0) return cudaSuccess;
+BuildConsts make_build_consts(const BuildArgs& a) {
   BuildConsts k{};
   const double u2 = a.aniso ? 1.0 : a.unit[0] * a.unit[0];
   const double sl2u = a.search * a.search / u2;
@@ -267,16 +315,41 @@ cudaError_t launch_walk(const BuildArgs& a, bool fill, cudaStream_t s, const int
   k.aniso = a.aniso;
   k.periodic = a.grid.periodic;
   k.sl2 = a.search * a.search;
-  const int blocks = grid_of(a.n, 128, 0);
-  if (fill)
-    k_walk<true><<<blocks, 128, 0, s>>>(a.q, a.n, a.grid, a.start, a.order, a.cq, a.cell, k,
-                                        a.want_half, a.want_full, nullptr, nullptr, a.off_half,
-                                        a.off_full, a.out_half, a.out_full, guard);
-  else
-    k_walk<false><<<blocks, 128, 0, s>>>(a.q, a.n, a.grid, a.start, a.order, a.cq, a.cell, k,
-                                         a.want_half, a.want_full, a.cnt_half, a.cnt_full,
-                                         nullptr, nullptr, nullptr, nullptr, guard);
+  return k;
+}
+
+
+cudaError_t launch_sort_cells(const int64_t* start, int ncells, const int32_t* order,
+                              const int4* cq, int32_t* order2, int4* cq2, cudaStream_t s,
+                              const int32_t* guard) {
+  k_sort_cells<<<grid_of((int64_t)ncells * 32, 256, 152 * 64), 256, 0, s>>>(
+      start, ncells, order, cq, order2, cq2, guard);
   return cudaGetLastError();
 }
+
+cudaError_t launch_build_rows(const BuildArgs& a, bool half, int maxrow, int32_t* rows,
+                              int32_t* cnt, int32_t* overflow, cudaStream_t s,
+                              const int32_t* guard) {
+  if (a.n == 0) return cudaSuccess;
+  const BuildConsts k = make_build_consts(a);
+  const int blocks = grid_of((int64_t)a.grid.ncells * 32, 128, 152 * 64);
+  if (half)
+    k_build_rows<true><<<blocks, 128, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, maxrow,
+                                              rows, cnt, overflow, guard);
+  else
+    k_build_rows<false><<<blocks, 128, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, maxrow,
+                                               rows, cnt, overflow, guard);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compact_padded(const int32_t* cnt, const int32_t* rows, int maxrow,
+                                  const int64_t* off, int n, int32_t* out, cudaStream_t s,
+                                  const int32_t* guard) {
+  if (n > 0)
+    k_compact_padded<<<grid_of((int64_t)n * 32, 256, 152 * 64), 256, 0, s>>>(
+        cnt, rows, maxrow, off, n, out, guard);
+  return cudaGetLastError();
+}
+
 
 }  // namespace ljg

@@ -30,12 +30,6 @@ struct BuildArgs {
   const int4* cq;
   const int32_t* cell;
   int want_half, want_full;
-  int32_t* cnt_half;
-  int32_t* cnt_full;
-  const int64_t* off_half;
-  const int64_t* off_full;
-  int32_t* out_half;
-  int32_t* out_full;
 };
 
 double key_to_double(unsigned long long k);
@@ -46,7 +40,18 @@ cudaError_t launch_bin(const double* q, int n, const CellGrid& g, int32_t* cell,
 cudaError_t launch_place(const int32_t* cell, int n, const int64_t* start, int32_t* cursor,
                          int ncells, const int4* qfix, int32_t* order, int4* cq, cudaStream_t s,
                          const int32_t* guard = nullptr);
-cudaError_t launch_walk(const BuildArgs& a, bool fill, cudaStream_t s,
-                        const int32_t* guard = nullptr);
+
+// Sorts the slots of every cell by particle index (out of place).
+cudaError_t launch_sort_cells(const int64_t* start, int ncells, const int32_t* order,
+                              const int4* cq, int32_t* order2, int4* cq2, cudaStream_t s,
+                              const int32_t* guard = nullptr);
+// Warp-cooperative build into padded rows (row i at i * maxrow, cnt[i]
+// entries; half: j > i only).  Rows longer than maxrow set *overflow.
+cudaError_t launch_build_rows(const BuildArgs& a, bool half, int maxrow, int32_t* rows,
+                              int32_t* cnt, int32_t* overflow, cudaStream_t s,
+                              const int32_t* guard = nullptr);
+cudaError_t launch_compact_padded(const int32_t* cnt, const int32_t* rows, int maxrow,
+                                  const int64_t* off, int n, int32_t* out, cudaStream_t s,
+                                  const int32_t* guard = nullptr);
 
 }  // namespace ljg
