@@ -56,11 +56,13 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="rho0.5_108k",
-                    choices=["rho0.5_108k", "rho1_108k", "precision_1m", "large_8m"],
+                    choices=["rho0.5_108k", "rho1_108k", "precision_1m", "large_8m",
+                             "batch_512"],
                     help="rho0.5_108k: the headline force benchmark; rho1_108k: the same at "
                          "rho = 1; precision_1m: 1,000,188-particle mixed MD with force "
                          "errors against FP64 every 100 steps; large_8m: 8,001,504-particle "
-                         "MD, mixed and FP64 back to back")
+                         "MD, mixed and FP64 back to back; batch_512: 512 replicas of "
+                         "uneven N in one mixed MD loop")
     return ap.parse_args()
 
 
@@ -256,14 +258,23 @@ def run_ours(args, dist, density=DENSITY):
         ms = [a.elapsed_time(b) for a, b in ev]
         return sum(ms)
 
-    variants = [("mixed", "gather", "aos"), ("mixed", "gather", "soa"),
-                ("mixed", "scatter", "aos"), ("fp64", "scatter", "aos"),
+    # the engine's autotuner picks the launch shape of the AoS calls that
+    # leave the launch fields at their defaults ("auto" below)
+    tuned = {}
+    for prec in ("mixed", "fp64"):
+        best, ms_t = ctx.autotune(qd, lj.make_opts(dt=DT, cl2=RC * RC, box=L, precision=prec),
+                                  reps=5)
+        tuned[prec] = {"method": {1: "gather", 2: "scatter"}[best.method], "kernel": best.kernel,
+                       "lanes": best.lanes, "unroll": best.unroll, "block": best.block,
+                       "ms_warm": ms_t}
+    variants = [("mixed", "auto", "aos"), ("mixed", "gather", "soa"),
+                ("mixed", "scatter", "aos"), ("fp64", "auto", "aos"),
                 ("fp64", "scatter", "soa"), ("fp64", "gather", "aos")]
     results = {}
     clocks = None
     for v in variants:
         steps = args.steps if v[0] == "mixed" else max(3, min(args.steps, 20))
-        if v == ("mixed", "gather", "aos"):
+        if v == ("mixed", "auto", "aos"):
             with ClockSampler(dist.local) as cs:
                 ms = time_variant(*v, steps, args.warmup)
             clocks = cs.summary()
@@ -279,6 +290,8 @@ def run_ours(args, dist, density=DENSITY):
                     key=lambda k: results[k]["gpairs"])
     head = results[best_mixed]
     prec, method, layout = best_mixed.split("/")
+    if method == "auto":
+        method = tuned[prec]["method"]
 
     # pair-kernel time of the headline variant (engine-side CUDA events
     # between the position-image pass and the pair kernel)
@@ -322,7 +335,7 @@ def run_ours(args, dist, density=DENSITY):
     traffic = profiled_traffic("force_mixed_gather_aos_108k_rho0.5.txt")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                "kernel": f"pair kernel of {best_mixed} (k_gather_mixed_u)",
+                "kernel": f"pair kernel of {best_mixed}, shape {tuned['mixed']}",
                 "algorithmic_bytes_per_launch": alg,
                 "kernel_ms": t_pair_ms, "position_image_ms": t_image_ms,
                 "force_call_bytes": algorithmic_bytes(method, layout, P, N),
@@ -330,6 +343,8 @@ def run_ours(args, dist, density=DENSITY):
                 / head["s_per_call"] / 1e9 / hbm}
     fp = results[best_fp64]
     fp_m, fp_l = best_fp64.split("/")[1], best_fp64.split("/")[2]
+    if fp_m == "auto":
+        fp_m = tuned["fp64"]["method"]
     # FP64 arithmetic per pair inside the cutoff (scatter): 20 FP64 ops; the
     # inside fraction of a search-radius list is (rc / rs)^3 for a uniform
     # density
@@ -361,6 +376,7 @@ def run_ours(args, dist, density=DENSITY):
                    "list_build_s": t_build, "parallelism": f"replicas x{dist.world}"},
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64": fp64,
         "variants": {k: round(v["gpairs"], 3) for k, v in results.items()},
+        "autotuned": tuned,
         "clocks": clocks, "gpu_launches": 2 * args.steps,
         "gpu_launches_note": "headline timed region: position-image pass + pair kernel per step",
     }
@@ -473,6 +489,59 @@ def run_large(args, dist):
     return out
 
 
+def run_batch(args, dist):
+    """512 replicas, N log-uniform in [256, 16384] (seeded) -> n = round((N/4)^(1/3))
+    FCC cells, rho from {0.5, 0.8, 1.0}, rc 2.5, skin 0.3, MB momenta at T* = 1,
+    1,000 mixed velocity-Verlet steps at dt = 0.005 in one batched loop."""
+    import torch
+    import lj_gpu_gb300 as lj
+    from lj_gpu_gb300 import _build
+    _build.build()
+    dev = torch.device("cuda", dist.local)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(SEED)
+    steps = 1000 if args.steps >= 100 else args.steps
+    qs, ps, boxes, offs, specs = [], [], [], [0], []
+    for r in range(512):
+        ndraw = float(np.exp(rng.uniform(np.log(256), np.log(16384))))
+        nc = int(round((ndraw / 4) ** (1 / 3)))
+        rho = float(rng.choice([0.5, 0.8, 1.0]))
+        q, L = lj.init_fcc(nc, rho, JITTER, SEED + 1000 + r)
+        p = lj.init_momenta(q.shape[0], 1.0, SEED + 5000 + r)
+        qs.append(q)
+        ps.append(p)
+        boxes.append([L, L, L])
+        offs.append(offs[-1] + q.shape[0])
+        specs.append((nc, rho))
+    q, p = np.concatenate(qs), np.concatenate(ps)
+    qd, pd = torch.from_numpy(q).to(dev), torch.from_numpy(p).to(dev)
+    prm = lj.make_md_params(DT, 2.5, 0.3, 1.0, precision="mixed", record_every=steps)
+    ctx = lj.Context(dist.local, stream=torch.cuda.current_stream())
+    en, st, shapes = ctx.batch_run(qd, pd, np.array(offs, np.int32), np.array(boxes), prm, steps)
+    ctx.close()
+    # half-list pairs within rc + skin per replica, counted once on the device
+    pairs = 0
+    ctx = lj.Context(dist.local, stream=torch.cuda.current_stream())
+    for r in range(512):
+        a, b = offs[r], offs[r + 1]
+        ctx.build_list(qd[a:b].contiguous(), 2.8, box=boxes[r], kinds=("half",))
+        pairs += ctx.list_info("half")[1]
+    ctx.close()
+    e0 = en[0, :, 0] + en[0, :, 1]
+    e1 = en[-1, :, 0] + en[-1, :, 1]
+    ms = st["ms_total"] / steps
+    return {"metric": "batched MD G pair-interactions/s (mixed)", "workload": "batch_512",
+            "replicas": 512, "N_total": int(q.shape[0]), "N_min": int(min(np.diff(offs))),
+            "N_max": int(max(np.diff(offs))), "steps": steps, "ms_per_step": ms,
+            "gpairs": pairs / (ms * 1e-3) / 1e9, "pairs_half_within_list_radius": int(pairs),
+            "rebuilds": st["rebuilds"],
+            "size_classes": [{"rows": int(s[0]), "lanes": int(s[1]), "entries_in_flight": int(s[2])}
+                             for s in shapes if s[0] > 0],
+            "energy_change_rel_max": float(np.max(np.abs(e1 - e0) / np.abs(e0))),
+            "note": "graph-captured step chunks with flag-guarded on-device rebuilds; per-class "
+                    "gather shapes timed at start-up"}
+
+
 # ---------------------------------------------------------------------------
 # CPU legs (oracle: the reference's algorithm restated in C)
 # ---------------------------------------------------------------------------
@@ -541,6 +610,8 @@ def main():
             line = run_precision(args, dist)
         elif args.workload == "large_8m":
             line = run_large(args, dist)
+        elif args.workload == "batch_512":
+            line = run_batch(args, dist)
         else:
             line = run_ours(args, dist, 1.0 if args.workload == "rho1_108k" else DENSITY)
     if dist.rank == 0 and line is not None:

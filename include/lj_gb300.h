@@ -247,6 +247,35 @@ int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_params* 
               int32_t nsteps, lj_md_record* records, int32_t max_records, int32_t* n_records,
               lj_md_stats* stats);
 
+/* ---- replica batches (project extension) --------------------------------- */
+/* Many independent periodic systems of uneven size in one velocity-Verlet
+ * loop (mixed precision): q, p hold the replicas back to back (AoS device
+ * arrays of n_total particles); replica r owns particles
+ * [offsets[r], offsets[r+1]) (host array of n_replicas + 1) in the cubic box
+ * boxes[3 r .. 3 r + 2] (host).  params->box is ignored.  Every stage runs
+ * once over the whole batch; the rows are split into size classes by their
+ * expected length and each class's gather launch shape is timed and chosen at
+ * start-up.  energies (host, may be NULL): per record, per replica,
+ * (kinetic, potential).  class_shapes (host, may be NULL, 9 ints): per class
+ * (rows, lanes, entries in flight).  The reference has no batching. */
+int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total, int32_t n_replicas,
+                 const int32_t* offsets, const double* boxes, const lj_md_params* params,
+                 int32_t nsteps, double* energies, int32_t max_records, int32_t* n_records,
+                 lj_md_stats* stats, int32_t* class_shapes);
+
+/* ---- autotuner ------------------------------------------------------------ */
+/* Times candidate launch shapes of one force call (method gather/scatter,
+ * kernel generation, lanes per row, entries in flight, block size) on the
+ * installed list and the device AoS positions q, `reps` calls each, and
+ * returns the fastest in *best (the other fields are copied from *opts).
+ * The caller's momenta are not touched (a scratch array is used).  The
+ * winner is remembered: later calls with the same precision and boundary
+ * kind that leave method = AUTO and every launch field 0 use it, until the
+ * list changes.  The reference picks its kernel and THREAD_BLOCK by hand
+ * (cuda/force_cuda.cu:45,378-383). */
+int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts* opts,
+                    int32_t reps, lj_force_opts* best, double* ms_best);
+
 /* ---- host-buffer call (the reference's measure(), force_cuda.cu:319-342) - */
 /* Uploads q and p from host memory, runs `calls` force calls on the installed
  * list, downloads p, and synchronises.  If the list was installed from host

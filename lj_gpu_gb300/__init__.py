@@ -136,6 +136,11 @@ _SIGNATURES = {
                               C.POINTER(C.c_double)]),
     "lj_init_momenta": (C.c_int, [_P, C.c_int32, C.c_double, C.c_uint64]),
     "lj_list_build": (C.c_int, [_P, _P, C.c_int32, C.c_double, _P, C.c_int32]),
+    "lj_batch_run": (C.c_int, [_P, _P, _P, C.c_int32, C.c_int32, _P, _P, C.POINTER(MdParams),
+                               C.c_int32, _P, C.c_int32, C.POINTER(C.c_int32),
+                               C.POINTER(MdStats), _P]),
+    "lj_autotune_aos": (C.c_int, [_P, _P, C.c_int32, C.POINTER(ForceOpts), C.c_int32,
+                                  C.POINTER(ForceOpts), C.POINTER(C.c_double)]),
     "lj_md_run": (C.c_int, [_P, _P, _P, C.c_int32, C.POINTER(MdParams), C.c_int32,
                             C.POINTER(MdRecord), C.c_int32, C.POINTER(C.c_int32),
                             C.POINTER(MdStats)]),
@@ -298,6 +303,15 @@ class Context:
                                 n, C.byref(opts))
         self._check(st, "force_soa")
 
+    def autotune(self, q, opts: ForceOpts, reps=5):
+        """Fastest launch shape for the installed list; returns (opts, ms per call)."""
+        _check_contig(q)
+        best = ForceOpts()
+        ms = C.c_double()
+        self._check(lib().lj_autotune_aos(self._h, ptr(q), q.shape[0], C.byref(opts), reps,
+                                          C.byref(best), C.byref(ms)), "autotune")
+        return best, ms.value
+
     def md_run(self, q, p, params: MdParams, nsteps, max_records=64):
         """Velocity Verlet on device AoS q, p (in place); returns (records, stats)
         with records a list of (step, kinetic, potential)."""
@@ -311,6 +325,25 @@ class Context:
         return ([(recs[k].step, recs[k].kinetic, recs[k].potential) for k in range(nrec.value)],
                 {"steps": st.steps, "rebuilds": st.rebuilds, "ms_total": st.ms_total,
                  "list_capacity": st.list_capacity})
+
+    def batch_run(self, q, p, offsets, boxes, params: MdParams, nsteps, max_records=16):
+        """Replica batch (see lj_batch_run).  offsets: n_replicas + 1 ints, boxes:
+        (n_replicas, 3).  Returns (energies[rec, replica, (K, U)], stats, shapes)."""
+        import numpy as np
+        _check_contig(q, p)
+        offs = np.ascontiguousarray(offsets, np.int32)
+        bx = np.ascontiguousarray(boxes, np.float64)
+        R = len(offs) - 1
+        en = np.zeros((max(1, max_records), R, 2))
+        nrec = C.c_int32()
+        st = MdStats()
+        shapes = np.zeros(9, np.int32)
+        s = lib().lj_batch_run(self._h, ptr(q), ptr(p), q.shape[0], R, ptr(offs), ptr(bx),
+                               C.byref(params), int(nsteps), ptr(en), max_records,
+                               C.byref(nrec), C.byref(st), ptr(shapes))
+        self._check(s, "batch_run")
+        return (en[:nrec.value], {"steps": st.steps, "rebuilds": st.rebuilds,
+                                  "ms_total": st.ms_total}, shapes.reshape(3, 3))
 
     def measure_aos(self, q_host, p_host, opts: ForceOpts, calls=100):
         """The reference's measure(): H2D, `calls` force calls, D2H; returns

@@ -268,9 +268,33 @@ cudaEvent_t* timing_slot(lj_ctx* ctx) {
   return s;
 }
 
-int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts* o) {
-  int rc = check_opts(ctx, o);
+// A configuration chosen by lj_autotune_aos replaces the engine defaults when
+// the caller leaves method (AUTO) and every launch field at zero, for the
+// same precision, layout, boundary kind and list.
+const lj_force_opts* apply_tuned(lj_ctx* ctx, const lj_force_opts* o, int soa,
+                                 lj_force_opts* scratch) {
+  if (o->method != LJ_METHOD_AUTO || o->kernel || o->lanes || o->unroll || o->block) return o;
+  for (const auto& t : ctx->tuned) {
+    if (t.precision == o->precision && t.soa == soa && t.periodic == (o->periodic != 0) &&
+        t.entries_half == ctx->half.entries && t.entries_full == ctx->full.entries &&
+        t.n == (ctx->full.valid ? ctx->full.n : ctx->half.n)) {
+      *scratch = *o;
+      scratch->method = t.method;
+      scratch->kernel = t.kernel;
+      scratch->lanes = t.lanes;
+      scratch->unroll = t.unroll;
+      scratch->block = t.block;
+      return scratch;
+    }
+  }
+  return o;
+}
+
+int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts* o_in) {
+  int rc = check_opts(ctx, o_in);
   if (rc) return rc;
+  lj_force_opts tuned_opts;
+  const lj_force_opts* o = apply_tuned(ctx, o_in, part.soa, &tuned_opts);
   int method;
   if ((rc = resolve_method(ctx, o, &method))) return rc;
   const DevList& l = method == LJ_METHOD_SCATTER_HALF ? ctx->half : ctx->full;
@@ -833,6 +857,103 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
   ctx->h_np.clear();
   ctx->h_ptr.clear();
   ctx->h_list.clear();
+  return LJ_OK;
+}
+
+int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts* opts,
+                    int32_t reps, lj_force_opts* best, double* ms_best) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (!best || reps < 1) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "best is NULL or reps < 1");
+  int rc = check_opts(ctx, opts);
+  if (rc) return rc;
+  if (n < 1 || !q || !aligned16(q)) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "bad q or n");
+  if (!ctx->half.valid && !ctx->full.valid) return fail(ctx, LJ_ERR_NO_LIST, "no list installed");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  LJ_CUDA(ctx, ctx->tune_p.ensure(4 * (size_t)n), "alloc");
+  // candidate launch shapes
+  struct Cand { int method, kernel, lanes, unroll, block; };
+  std::vector<Cand> cands;
+  const bool mixed = opts->precision == LJ_PREC_MIXED;
+  const bool try_gather = ctx->full.valid && opts->method != LJ_METHOD_SCATTER_HALF;
+  const bool try_scatter = ctx->half.valid && opts->method != LJ_METHOD_GATHER_FULL;
+  for (int block : {128, 256}) {
+    if (try_gather) {
+      if (mixed) {
+        for (int g : {2, 4, 8})
+          for (int u : {2, 4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 2, g, u, block});
+        for (int g : {4, 8, 16}) cands.push_back({LJ_METHOD_GATHER_FULL, 1, g, 0, block});
+      } else {
+        if (block == 128) cands.push_back({LJ_METHOD_GATHER_FULL, 2, 0, 0, 128});
+        for (int g : {4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 1, g, 0, block});
+      }
+    }
+    if (try_scatter) {
+      if (!mixed && block == 128) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, 0, 0, 128});
+      for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_SCATTER_HALF, 1, g, 0, block});
+    }
+  }
+  if (cands.empty()) return fail(ctx, LJ_ERR_NO_LIST, "no list for the requested method");
+  Particles part{};
+  part.q = q;
+  part.p = ctx->tune_p.ptr;
+  const bool was_timing = ctx->timing;
+  ctx->timing = false;
+  double best_ms = 1e300;
+  Cand win = cands[0];
+  for (const Cand& c : cands) {
+    lj_force_opts o = *opts;
+    o.method = c.method;
+    o.kernel = c.kernel;
+    o.lanes = c.lanes;
+    o.unroll = c.unroll;
+    o.block = c.block;
+    if ((rc = run_force(ctx, part, n, &o))) {  // warm-up (and validity)
+      ctx->timing = was_timing;
+      return rc;
+    }
+    LJ_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream), "event");
+    for (int r = 0; r < reps; r++)
+      if ((rc = run_force(ctx, part, n, &o))) {
+        ctx->timing = was_timing;
+        return rc;
+      }
+    LJ_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream), "event");
+    LJ_CUDA(ctx, cudaEventSynchronize(ctx->ev[1]), "sync");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    if (ms / reps < best_ms) {
+      best_ms = ms / reps;
+      win = c;
+    }
+  }
+  ctx->timing = was_timing;
+  *best = *opts;
+  best->method = win.method;
+  best->kernel = win.kernel;
+  best->lanes = win.lanes;
+  best->unroll = win.unroll;
+  best->block = win.block;
+  if (ms_best) *ms_best = best_ms;
+  // remember the winner for calls that leave the launch fields at zero
+  lj_ctx::Tuned t{};
+  t.precision = opts->precision;
+  t.soa = 0;
+  t.periodic = opts->periodic != 0;
+  t.n = n;
+  t.entries_half = ctx->half.entries;
+  t.entries_full = ctx->full.entries;
+  t.method = win.method;
+  t.kernel = win.kernel;
+  t.lanes = win.lanes;
+  t.unroll = win.unroll;
+  t.block = win.block;
+  auto& v = ctx->tuned;
+  v.erase(std::remove_if(v.begin(), v.end(), [&](const lj_ctx::Tuned& x) {
+            return x.precision == t.precision && x.soa == t.soa && x.periodic == t.periodic;
+          }),
+          v.end());
+  v.push_back(t);
   return LJ_OK;
 }
 

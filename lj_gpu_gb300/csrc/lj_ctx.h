@@ -55,6 +55,11 @@ void md_state_delete(MdState* m);
 struct MdStateDeleter {
   void operator()(MdState* m) const { md_state_delete(m); }
 };
+struct BatchState;  // lj_batch.cu
+void batch_state_delete(BatchState* b);
+struct BatchStateDeleter {
+  void operator()(BatchState* b) const { batch_state_delete(b); }
+};
 
 }  // namespace ljg
 
@@ -89,8 +94,18 @@ struct lj_ctx {
   size_t tev_used = 0;
   double t_ms[3] = {0, 0, 0};
   int64_t t_calls = 0;
+  // autotuner (lj_autotune_aos): scratch p and the chosen shapes
+  ljg::DevBuf<double> tune_p;
+  struct Tuned {
+    int precision, soa, periodic, n;
+    int64_t entries_half, entries_full;
+    int method, kernel, lanes, unroll, block;
+  };
+  std::vector<Tuned> tuned;
   // molecular dynamics state (lj_md_run)
   std::unique_ptr<ljg::MdState, ljg::MdStateDeleter> md;
+  // replica batch state (lj_batch_run)
+  std::unique_ptr<ljg::BatchState, ljg::BatchStateDeleter> batch;
 };
 
 // Error reporting shared by the C-ABI translation units.

@@ -426,6 +426,100 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
     kick_p<SOA>(P, i, widen_f32(hx + lx), widen_f32(hy + ly), widen_f32(hz + lz), K.fscale);
 }
 
+// Batched mixed gather: as k_gather_mixed_u, with every constant that depends
+// on the box (unit, cutoff in fixed units, FP64 image shift) read per row
+// from the row's replica.  Groups walk the row list of one size class.
+template <int G, int U>
+__global__ void __launch_bounds__(256) k_gather_mixed_batch(
+    const Particles P, const Csr C, const int4* __restrict__ qfix, const int32_t* __restrict__ rid,
+    const ReplicaInfo* __restrict__ reps, const int32_t* __restrict__ rows, int nrows, double dt,
+    long long cl2_bits) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int g = t / G;
+  const int lane = t & (G - 1);
+  const bool valid = g < nrows;
+  int cnt = 0, i = 0;
+  int64_t k0 = 0;
+  int4 xi = make_int4(0, 0, 0, 0);
+  MixedConsts K{};
+  if (valid) {
+    i = __ldg(rows + g);
+    cnt = __ldg(C.np + i);
+    k0 = row_start(C, i);
+    xi = __ldg(qfix + i);
+    const ReplicaInfo& R = reps[__ldg(rid + i)];
+    K.k_hi = R.k_hi;
+    K.k_lo = R.k_lo;
+    K.cl2_lo = R.cl2u_lo;
+    K.cl2_hi = R.cl2u_hi;
+    K.f64.cl2_bits = cl2_bits;
+    for (int d = 0; d < 3; d++) {
+      K.f64.len[d] = R.len[d];
+      K.f64.half_bits[d] = R.half_bits[d];
+    }
+    K.fscale[0] = K.fscale[1] = K.fscale[2] = R.unit * dt;
+  }
+  int cmax = cnt;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
+  KahanF ax, ay, az;
+  ax.init();
+  ay.init();
+  az.init();
+  for (int base = 0; base < cmax; base += G * U) {
+    int jj[U];
+    bool ok[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = base + lane + u * G;
+      ok[u] = k < cnt;
+      jj[u] = ok[u] ? __ldg(C.list + k0 + k) : 0;
+    }
+    int4 xj[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    unsigned border = 0u;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const float3 d = sep_mixed<false>(xi, xj[u], K);
+      const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+      const bool in = ok[u] && r2 <= K.cl2_lo;
+      if (ok[u] && r2 > K.cl2_lo && r2 <= K.cl2_hi) border |= 1u << u;
+      float df = df_mixed<false>(r2, K);
+      df = in ? df : 0.0f;
+      sx = fmaf(df, d.x, sx);
+      sy = fmaf(df, d.y, sy);
+      sz = fmaf(df, d.z, sz);
+    }
+    if (__any_sync(kFullMask, border != 0u)) {
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (!(border & (1u << u))) continue;
+        const double3 d64 = sep_fp64<true>(load_q<false>(P, i), load_q<false>(P, jj[u]), K.f64);
+        if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
+        const float3 d = sep_mixed<false>(xi, xj[u], K);
+        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+        const float df = df_mixed<false>(r2, K);
+        sx = fmaf(df, d.x, sx);
+        sy = fmaf(df, d.y, sy);
+        sz = fmaf(df, d.z, sz);
+      }
+    }
+    ax.add(sx);
+    ay.add(sy);
+    az.add(sz);
+  }
+  float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
+  if (G > 1) {
+    group_reduce_comp<G>(hx, lx);
+    group_reduce_comp<G>(hy, ly);
+    group_reduce_comp<G>(hz, lz);
+  }
+  if (valid && lane == 0)
+    kick_p<false>(P, i, widen_f32(hx + lx), widen_f32(hy + ly), widen_f32(hz + lz), K.fscale);
+}
+
 // Compacted FP64 gather (kernel 2).  One warp per row.  Candidates are
 // screened in FP32 from the fixed-point image (cheap), the survivors (inside
 // the cutoff or within 4e-6 of it) are queued in shared memory, and the FP64
@@ -844,6 +938,31 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
   if (soa) k_kick_from_scratch<true><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
   else k_kick_from_scratch<false><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
   return cudaGetLastError();
+}
+
+cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* qfix,
+                               const int32_t* rid, const ReplicaInfo* reps,
+                               const int32_t* rows, int nrows, double dt, double cl2, int lanes,
+                               int unroll, cudaStream_t s) {
+  if (nrows <= 0) return cudaSuccess;
+  long long cl2_bits;
+  std::memcpy(&cl2_bits, &cl2, sizeof cl2_bits);
+  const int block = 128;
+  const int blocks = (int)(((long long)nrows * lanes + block - 1) / block);
+  auto go = [&](auto u) -> cudaError_t {
+    constexpr int U = decltype(u)::value;
+    return dispatch_lanes(lanes, [&](auto g) {
+      constexpr int G = decltype(g)::value;
+      k_gather_mixed_batch<G, U>
+          <<<blocks, block, 0, s>>>(part, c, qfix, rid, reps, rows, nrows, dt, cl2_bits);
+      return cudaGetLastError();
+    });
+  };
+  switch (unroll) {
+    case 2: return go(std::integral_constant<int, 2>{});
+    case 4: return go(std::integral_constant<int, 4>{});
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_force_pairs(const Particles& part, int n, const int32_t* ip,

@@ -44,6 +44,24 @@ struct Periodic {
   double half[3];
 };
 
+// One replica of a batch (cubic periodic box).  Positions of every replica are
+// normalised to the 2^32 fixed-point period of its own box, so pair kernels
+// need only the per-row unit constants below.
+struct ReplicaInfo {
+  FixedAxis ax[3];
+  double len[3];
+  long long half_bits[3];
+  float unit_f[3];          // length per fixed unit
+  float k_hi, k_lo;         // 1 / unit^2, split in two floats
+  float cl2u_lo, cl2u_hi;   // cutoff^2 in fixed units^2, -/+ a relative 4e-6
+  float sl2u_lo, sl2u_hi;   // list radius^2 in fixed units^2, -/+ 4e-6
+  double unit;              // length per fixed unit (FP64)
+  double inv_w[3];          // cells per unit length
+  int nc[3];
+  int cell_base;            // first global cell of this replica
+  int offset, count;        // particle range
+};
+
 // Everything one force launch needs.
 struct ForceLaunch {
   Particles part;
@@ -68,6 +86,13 @@ struct ForceLaunch {
 // Fills axis[] / unit[] / aniso for a periodic box, or for an open box from
 // the largest coordinate magnitude (max_abs).
 void make_fixed_frame(ForceLaunch& L, double max_abs);
+
+// Batched mixed gather over the rows `rows[0..nrows)` (one size class) of a
+// replica batch; padded rows (C.ptr == nullptr).
+cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* qfix,
+                               const int32_t* rid, const ReplicaInfo* reps,
+                               const int32_t* rows, int nrows, double dt, double cl2, int lanes,
+                               int unroll, cudaStream_t s);
 
 // Launchers (return cudaError_t of the launch)
 cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s);

@@ -214,6 +214,89 @@ __global__ void __launch_bounds__(128) k_build_rows(const double* __restrict__ q
   }
 }
 
+// Batched binning: every replica has its own grid starting at cell_base.
+__global__ void k_bin_batch(const double* __restrict__ q, int n, const int32_t* __restrict__ rid,
+                            const ReplicaInfo* __restrict__ reps, int32_t* __restrict__ cell,
+                            int32_t* __restrict__ count, const int32_t* guard) {
+  if (off_guard(guard)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const ReplicaInfo& R = reps[rid[i]];
+  const double* b = q + 4 * (size_t)i;
+  int c[3];
+  for (int d = 0; d < 3; d++) c[d] = wrap_cell((int)floor(b[d] * R.inv_w[d]), R.nc[d]);
+  const int id = R.cell_base + (c[2] * R.nc[1] + c[1]) * R.nc[0] + c[0];
+  cell[i] = id;
+  atomicAdd(count + id, 1);
+}
+
+// Batched warp-cooperative row build (full rows): as k_build_rows, with the
+// cell's replica supplying the local grid and the membership constants.
+__global__ void __launch_bounds__(128) k_build_rows_batch(
+    const double* __restrict__ q, const ReplicaInfo* __restrict__ reps,
+    const int32_t* __restrict__ cell_rid, int ncells, double sl2,
+    const int64_t* __restrict__ start, const int32_t* __restrict__ order,
+    const int4* __restrict__ cq, int maxrow, int32_t* __restrict__ rows,
+    int32_t* __restrict__ cnt, int32_t* __restrict__ overflow, const int32_t* guard) {
+  if (off_guard(guard)) return;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncells; c += nwarps) {
+    const ReplicaInfo& R = reps[cell_rid[c]];
+    CellGrid g{};
+    for (int d = 0; d < 3; d++) g.nc[d] = R.nc[d];
+    g.ncells = R.nc[0] * R.nc[1] * R.nc[2];
+    g.periodic = 1;
+    BuildConsts k{};
+    k.sl2_lo = R.sl2u_lo;
+    k.sl2_hi = R.sl2u_hi;
+    k.aniso = 0;
+    k.periodic = 1;
+    for (int d = 0; d < 3; d++) {
+      k.len[d] = R.len[d];
+      k.half_bits[d] = R.half_bits[d];
+    }
+    k.sl2 = sl2;
+    const int s0 = (int)start[c], s1 = (int)start[c + 1];
+    for (int a = s0; a < s1; a += 32) {
+      const bool act = a + lane < s1;
+      const int i = act ? order[a + lane] : -1;
+      const int4 xi = act ? cq[a + lane] : make_int4(0, 0, 0, 0);
+      const size_t base = act ? (size_t)i * (size_t)maxrow : 0;
+      int count = 0;
+      for_neighbour_cells(c - R.cell_base, g, [&](int c2l) {
+        const int c2 = R.cell_base + c2l;
+        const int t0 = (int)start[c2], t1 = (int)start[c2 + 1];
+        for (int b = t0; b < t1; b += 32) {
+          int jl = -1;
+          int4 xl = make_int4(0, 0, 0, 0);
+          if (b + lane < t1) {
+            jl = order[b + lane];
+            xl = cq[b + lane];
+          }
+          const int m = min(32, t1 - b);
+          for (int kk = 0; kk < m; kk++) {
+            const int j = __shfl_sync(kFullMask, jl, kk);
+            int4 xj;
+            xj.x = __shfl_sync(kFullMask, xl.x, kk);
+            xj.y = __shfl_sync(kFullMask, xl.y, kk);
+            xj.z = __shfl_sync(kFullMask, xl.z, kk);
+            xj.w = 0;
+            if (act && j != i && within(xi, xj, q, i, j, k)) {
+              if (count < maxrow) rows[base + count] = j;
+              count++;
+            }
+          }
+        }
+      });
+      if (act) {
+        cnt[i] = min(count, maxrow);
+        if (count > maxrow) atomicMax(overflow, 1);
+      }
+    }
+  }
+}
+
 // Compact copy of padded rows: out[off[i] + m] = rows[i * maxrow + m].
 __global__ void k_compact_padded(const int32_t* __restrict__ cnt, const int32_t* __restrict__ rows,
                                  int maxrow, const int64_t* __restrict__ off, int n,
@@ -351,5 +434,25 @@ cudaError_t launch_compact_padded(const int32_t* cnt, const int32_t* rows, int m
   return cudaGetLastError();
 }
 
+
+cudaError_t launch_bin_batch(const double* q, int n, const int32_t* rid, const ReplicaInfo* reps,
+                             int ncells, int32_t* cell, int32_t* count, cudaStream_t s,
+                             const int32_t* guard) {
+  cudaError_t e = launch_zero_i32(count, ncells, guard, s);
+  if (e != cudaSuccess || n == 0) return e;
+  k_bin_batch<<<grid_of(n, 256, 0), 256, 0, s>>>(q, n, rid, reps, cell, count, guard);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_rows_batch(const double* q, const ReplicaInfo* reps,
+                                    const int32_t* cell_rid, int ncells, double sl2,
+                                    const int64_t* start, const int32_t* order, const int4* cq,
+                                    int maxrow, int32_t* rows, int32_t* cnt, int32_t* overflow,
+                                    cudaStream_t s, const int32_t* guard) {
+  const int blocks = grid_of((int64_t)ncells * 32, 128, 152 * 64);
+  k_build_rows_batch<<<blocks, 128, 0, s>>>(q, reps, cell_rid, ncells, sl2, start, order, cq,
+                                            maxrow, rows, cnt, overflow, guard);
+  return cudaGetLastError();
+}
 
 }  // namespace ljg

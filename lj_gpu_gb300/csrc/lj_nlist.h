@@ -54,4 +54,14 @@ cudaError_t launch_compact_padded(const int32_t* cnt, const int32_t* rows, int m
                                   const int64_t* off, int n, int32_t* out, cudaStream_t s,
                                   const int32_t* guard = nullptr);
 
+// Batch (one grid per replica, cells numbered from each replica's cell_base).
+cudaError_t launch_bin_batch(const double* q, int n, const int32_t* rid, const ReplicaInfo* reps,
+                             int ncells, int32_t* cell, int32_t* count, cudaStream_t s,
+                             const int32_t* guard = nullptr);
+cudaError_t launch_build_rows_batch(const double* q, const ReplicaInfo* reps,
+                                    const int32_t* cell_rid, int ncells, double sl2,
+                                    const int64_t* start, const int32_t* order, const int4* cq,
+                                    int maxrow, int32_t* rows, int32_t* cnt, int32_t* overflow,
+                                    cudaStream_t s, const int32_t* guard = nullptr);
+
 }  // namespace ljg

@@ -370,3 +370,23 @@ def test_non_compact_list_layout(engine):
         ctx.set_list_csr(dev(npp), dev(new_ptr), dev(big))
         for a, b in zip(ctx.get_list_csr("half"), half):
             assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_autotune_picks_a_valid_shape_and_keeps_results(engine, prec):
+    q, box, half = system("pbc_rho1")
+    ref = oracle_p(q, half, box, 1, 0.005)
+    with engine.Context(0) as ctx:
+        npp, ptr, lst = half
+        ctx.set_list_csr(dev(npp), dev(ptr), dev(lst))
+        qd = dev(q)
+        opts = engine.make_opts(dt=0.005, cl2=9.0, box=box, precision=prec)
+        best, ms = ctx.autotune(qd, opts, reps=2)
+        assert ms > 0 and best.method in (1, 2) and best.kernel in (1, 2)
+        # the tuned shape is used by default-option calls and keeps parity
+        for o in (opts, best):
+            pd = dev(np.zeros_like(q))
+            ctx.force_aos(qd, pd, o)
+            e = ol.rel_errors(host(pd), ref)
+            assert (e["max_rel"] <= FP64_TOL) if prec == "fp64" else \
+                (e["max_rel_rms"] <= MIXED_TOL["max_rel_rms"]), e
