@@ -128,6 +128,39 @@ int lj_list_set_pairs(lj_ctx* ctx, int32_t n, const int32_t* i_particles,
  * returned. */
 int lj_list_get_csr(lj_ctx* ctx, int32_t kind, int32_t* number_of_partners, int32_t* pointer,
                     int32_t* sorted_list, int64_t capacity, int64_t* n_entries, int32_t where);
+/* Installs a list given in the reference's transposed ("ELL") layout: entry
+ * k of row i at transposed_list[i + k * width], width >= n, ell_len ints in
+ * the array (make_transposed_pairlist, cuda/force_cuda.cu:229-240, the input
+ * of its memopt2/memopt3/unrolling kernels).  Converted to the compact CSR on
+ * the device; validation as lj_list_set_csr plus the array bounds. */
+int lj_list_set_ell(lj_ctx* ctx, int32_t n, const int32_t* number_of_partners,
+                    const int32_t* transposed_list, int64_t width, int64_t ell_len,
+                    int32_t kind, int32_t where);
+/* Exports the installed list in that layout (zero-filled first, as the
+ * reference does); ell_len must be >= max_row * width. */
+int lj_list_get_ell(lj_ctx* ctx, int32_t kind, int32_t* number_of_partners,
+                    int32_t* transposed_list, int64_t width, int64_t ell_len, int32_t where);
+/* Host helpers for the reference's list files and row order (no GPU):
+ *   lj_list_shuffle_rows: random_shfl (cuda/force_cuda.cu:255-263), one
+ *     std::mt19937(seed) shuffling every row in i order, in place;
+ *   lj_cache_write_text / lj_cache_read_text: the CUDA driver's text cache
+ *     (.cache_pair_{half,all}.dat, cuda/force_cuda.cu:165-227); the reader
+ *     checks the particle count and the arrays as loadpair and
+ *     check_loadedpair do;
+ *   lj_pairdat_write / lj_pairdat_read: cpu_ref's binary pair.dat
+ *     (cpu_ref/force_aos.cpp:603-620), fixed-size arrays of 400,000 partner
+ *     counts and 12,000,000 (i, j) pairs. */
+int lj_list_shuffle_rows(int32_t n, const int32_t* number_of_partners, const int32_t* pointer,
+                         int32_t* sorted_list, uint32_t seed);
+int lj_cache_write_text(const char* path, int32_t n, const int32_t* number_of_partners,
+                        const int32_t* pointer, const int32_t* sorted_list, int64_t n_entries);
+int lj_cache_read_text(const char* path, int32_t n, int32_t* number_of_partners, int32_t* pointer,
+                       int32_t* sorted_list, int64_t capacity, int64_t* n_entries);
+int lj_pairdat_write(const char* path, int32_t n, const int32_t* i_particles,
+                     const int32_t* j_particles, int64_t n_pairs);
+int lj_pairdat_read(const char* path, int32_t n, int32_t* number_of_partners,
+                    int32_t* i_particles, int32_t* j_particles, int64_t capacity,
+                    int64_t* n_pairs);
 /* Number of particles and entries of the installed list (0 if none). */
 int lj_list_info(const lj_ctx* ctx, int32_t kind, int32_t* n, int64_t* n_entries,
                  int32_t* max_row);
@@ -140,6 +173,11 @@ int lj_force_aos(lj_ctx* ctx, const double* q, double* p, int32_t n, const lj_fo
 /* SoA variant (cpu_ref/force_soa.cpp:163-195); six device arrays of n doubles */
 int lj_force_soa(lj_ctx* ctx, const double* qx, const double* qy, const double* qz, double* px,
                  double* py, double* pz, int32_t n, const lj_force_opts* opts);
+
+/* Interleaved layout z[n][8] = {q.x, q.y, q.z, q.w, p.x, p.y, p.z, p.w}, one
+ * 64-byte record per particle (cpu_ref force_sorted_z,
+ * cpu_ref/force_aos.cpp:226-258); q is read, p updated in place. */
+int lj_force_z(lj_ctx* ctx, double* z, int32_t n, const lj_force_opts* opts);
 
 /* Stateless FP64 drop-in for a reference kernel launch: the argument list of
  * force_kernel_* (cuda/kernel.cuh:5-13) on AoS double4 buffers, with the list

@@ -139,6 +139,17 @@ _SIGNATURES = {
     "lj_batch_run": (C.c_int, [_P, _P, _P, C.c_int32, C.c_int32, _P, _P, C.POINTER(MdParams),
                                C.c_int32, _P, C.c_int32, C.POINTER(C.c_int32),
                                C.POINTER(MdStats), _P]),
+    "lj_force_z": (C.c_int, [_P, _P, C.c_int32, C.POINTER(ForceOpts)]),
+    "lj_list_set_ell": (C.c_int, [_P, C.c_int32, _P, _P, C.c_int64, C.c_int64, C.c_int32,
+                                  C.c_int32]),
+    "lj_list_get_ell": (C.c_int, [_P, C.c_int32, _P, _P, C.c_int64, C.c_int64, C.c_int32]),
+    "lj_list_shuffle_rows": (C.c_int, [C.c_int32, _P, _P, _P, C.c_uint32]),
+    "lj_cache_write_text": (C.c_int, [C.c_char_p, C.c_int32, _P, _P, _P, C.c_int64]),
+    "lj_cache_read_text": (C.c_int, [C.c_char_p, C.c_int32, _P, _P, _P, C.c_int64,
+                                     C.POINTER(C.c_int64)]),
+    "lj_pairdat_write": (C.c_int, [C.c_char_p, C.c_int32, _P, _P, C.c_int64]),
+    "lj_pairdat_read": (C.c_int, [C.c_char_p, C.c_int32, _P, _P, _P, C.c_int64,
+                                  C.POINTER(C.c_int64)]),
     "lj_autotune_aos": (C.c_int, [_P, _P, C.c_int32, C.POINTER(ForceOpts), C.c_int32,
                                   C.POINTER(ForceOpts), C.POINTER(C.c_double)]),
     "lj_md_run": (C.c_int, [_P, _P, _P, C.c_int32, C.POINTER(MdParams), C.c_int32,
@@ -296,6 +307,28 @@ class Context:
         n = q.shape[0] if n is None else n
         self._check(lib().lj_force_aos(self._h, ptr(q), ptr(p), n, C.byref(opts)), "force_aos")
 
+    def force_z(self, z, opts: ForceOpts, n=None):
+        """Interleaved z[n][8] = {q.xyzw, p.xyzw} layout."""
+        _check_contig(z)
+        n = z.shape[0] if n is None else n
+        self._check(lib().lj_force_z(self._h, ptr(z), n, C.byref(opts)), "force_z")
+
+    def set_list_ell(self, number_of_partners, transposed_list, width, kind="full"):
+        _check_contig(number_of_partners, transposed_list)
+        st = lib().lj_list_set_ell(self._h, len(number_of_partners), ptr(number_of_partners),
+                                   ptr(transposed_list), int(width), len(transposed_list),
+                                   _KIND[kind], _where(transposed_list))
+        self._check(st, "set_list_ell")
+
+    def get_list_ell(self, width, kind="full"):
+        import numpy as np
+        n, _, mr = self.list_info(kind)
+        npp = np.zeros(n, np.int32)
+        ell = np.zeros(max(1, mr * int(width)), np.int32)
+        self._check(lib().lj_list_get_ell(self._h, _KIND[kind], ptr(npp), ptr(ell), int(width),
+                                          len(ell), WHERE_HOST), "get_list_ell")
+        return npp, ell
+
     def force_soa(self, qx, qy, qz, px, py, pz, opts: ForceOpts, n=None):
         _check_contig(qx, qy, qz, px, py, pz)
         n = qx.shape[0] if n is None else n
@@ -394,6 +427,47 @@ def init_momenta(n, temperature=1.0, seed=1):
     if st != LJ_OK:
         raise LJError(st, "lj_init_momenta")
     return p
+
+
+def _status(st, what):
+    if st != LJ_OK:
+        raise LJError(st, f"{what}: {lib().lj_status_string(st).decode()}")
+
+
+def shuffle_rows(npp, ptr_, lst, seed=10):
+    """random_shfl: shuffles the rows of host CSR arrays in place."""
+    _status(lib().lj_list_shuffle_rows(len(npp), ptr(npp), ptr(ptr_), ptr(lst), seed),
+            "shuffle_rows")
+
+
+def cache_write_text(path, npp, ptr_, lst):
+    _status(lib().lj_cache_write_text(str(path).encode(), len(npp), ptr(npp), ptr(ptr_),
+                                      ptr(lst), len(lst)), "cache_write_text")
+
+
+def cache_read_text(path, n, capacity):
+    import numpy as np
+    npp, ptr_ = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    lst = np.zeros(max(1, capacity), np.int32)
+    ne = C.c_int64()
+    _status(lib().lj_cache_read_text(str(path).encode(), n, ptr(npp), ptr(ptr_), ptr(lst),
+                                     capacity, C.byref(ne)), "cache_read_text")
+    return npp, ptr_, lst[:ne.value]
+
+
+def pairdat_write(path, n, ii, jj):
+    _status(lib().lj_pairdat_write(str(path).encode(), n, ptr(ii), ptr(jj), len(ii)),
+            "pairdat_write")
+
+
+def pairdat_read(path, n, capacity):
+    import numpy as np
+    npp = np.zeros(n, np.int32)
+    ii, jj = np.zeros(max(1, capacity), np.int32), np.zeros(max(1, capacity), np.int32)
+    k = C.c_int64()
+    _status(lib().lj_pairdat_read(str(path).encode(), n, ptr(npp), ptr(ii), ptr(jj), capacity,
+                                  C.byref(k)), "pairdat_read")
+    return npp, ii[:k.value], jj[:k.value]
 
 
 def force_csr_fp64_aos(q, p, dt, cl2, sorted_list, number_of_partners, pointer, kind="full",

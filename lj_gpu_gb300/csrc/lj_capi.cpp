@@ -644,6 +644,108 @@ int lj_force_soa(lj_ctx* ctx, const double* qx, const double* qy, const double* 
   return run_force(ctx, part, n, o);
 }
 
+int lj_force_z(lj_ctx* ctx, double* z, int32_t n, const lj_force_opts* o) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (n < 0) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "n < 0");
+  if (n > 0 && !z) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "null z");
+  if (!aligned16(z)) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "z must be 16-byte aligned");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  Particles part{};
+  part.soa = 0;
+  part.stride = 8;
+  part.q = z;
+  part.p = z + 4;
+  return run_force(ctx, part, n, o);
+}
+
+int lj_list_set_ell(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ell,
+                    int64_t width, int64_t ell_len, int32_t kind, int32_t where) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (n < 0 || width < n || ell_len < 0 || (n > 0 && (!np || (!ell && ell_len > 0))))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "bad ELL arguments (width must be >= n)");
+  if (kind != LJ_LIST_HALF && kind != LJ_LIST_FULL)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown list kind %d", kind);
+  if (where != LJ_WHERE_HOST && where != LJ_WHERE_DEVICE)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown location %d", where);
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  cudaStream_t s = ctx->stream;
+  DevBuf<int32_t> d_np, d_ell, d_ptr, d_list;
+  DevBuf<int64_t> d_off;
+  LJ_CUDA(ctx, d_np.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, d_ell.ensure((size_t)ell_len), "alloc");
+  int rc;
+  if ((rc = copy_in(ctx, d_np.ptr, np, (size_t)n, where))) return rc;
+  if ((rc = copy_in(ctx, d_ell.ptr, ell, (size_t)ell_len, where))) return rc;
+  LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
+  const int32_t init[2] = {0, 0x7fffffff};
+  LJ_CUDA(ctx, cudaMemcpyAsync(ctx->err2.ptr, init, sizeof init, cudaMemcpyHostToDevice, s),
+          "err init");
+  LJ_CUDA(ctx, launch_ell_check(d_np.ptr, n, width, ell_len, ctx->err2.ptr, s), "check");
+  int32_t out[2];
+  LJ_CUDA(ctx, cudaMemcpyAsync(out, ctx->err2.ptr, sizeof out, cudaMemcpyDeviceToHost, s),
+          "read");
+  LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+  if (out[0] == 1)
+    return fail(ctx, LJ_ERR_BAD_LIST, "number_of_partners[%d] out of range", out[1]);
+  if (out[0] == 3)
+    return fail(ctx, LJ_ERR_BAD_LIST, "row %d runs past the end of the transposed list", out[1]);
+  LJ_CUDA(ctx, d_off.ensure((size_t)n + 1), "alloc");
+  LJ_CUDA(ctx, ctx->tmp_scan.ensure(scan_tmp_bytes(n)), "alloc");
+  LJ_CUDA(ctx, launch_scan_counts(d_np.ptr, n, d_off.ptr, ctx->tmp_scan.ptr, ctx->tmp_scan.cap,
+                                  s), "scan");
+  int64_t total = 0;
+  LJ_CUDA(ctx, cudaMemcpyAsync(&total, d_off.ptr + n, sizeof total, cudaMemcpyDeviceToHost, s),
+          "total");
+  LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+  if (total > 0x7fffffffll) return fail(ctx, LJ_ERR_UNSUPPORTED, "list exceeds 2^31 entries");
+  LJ_CUDA(ctx, d_list.ensure((size_t)std::max<int64_t>(total, 1)), "alloc");
+  LJ_CUDA(ctx, d_ptr.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, launch_ell_to_csr(d_np.ptr, d_ell.ptr, n, width, d_off.ptr, d_list.ptr, s),
+          "transpose");
+  LJ_CUDA(ctx, launch_offsets_to_ptr(d_off.ptr, n, d_ptr.ptr, d_np.ptr, ctx->err2.ptr, s), "ptr");
+  LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+  return lj_list_set_csr(ctx, n, d_np.ptr, d_ptr.ptr, d_list.ptr, total, kind, LJ_WHERE_DEVICE);
+}
+
+int lj_list_get_ell(lj_ctx* ctx, int32_t kind, int32_t* np, int32_t* ell, int64_t width,
+                    int64_t ell_len, int32_t where) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (kind != LJ_LIST_HALF && kind != LJ_LIST_FULL)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown list kind %d", kind);
+  if (where != LJ_WHERE_HOST && where != LJ_WHERE_DEVICE)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown location %d", where);
+  const DevList& l = kind == LJ_LIST_HALF ? ctx->half : ctx->full;
+  if (!l.valid) return fail(ctx, LJ_ERR_NO_LIST, "no list of that kind installed");
+  if (width < l.n) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "width must be >= n");
+  if ((int64_t)l.max_row * width > ell_len)
+    return fail(ctx, LJ_ERR_LIST_OVERFLOW, "transposed list needs %lld entries",
+                (long long)((int64_t)l.max_row * width));
+  if (l.n > 0 && (!np || !ell)) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "null output");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  cudaStream_t s = ctx->stream;
+  DevBuf<int32_t> d_ell;
+  int32_t* dst = ell;
+  if (where == LJ_WHERE_HOST) {
+    LJ_CUDA(ctx, d_ell.ensure((size_t)std::max<int64_t>(ell_len, 1)), "alloc");
+    dst = d_ell.ptr;
+  }
+  // zero-filled first, as make_transposed_pairlist does (set_val(0))
+  LJ_CUDA(ctx, cudaMemsetAsync(dst, 0, sizeof(int32_t) * (size_t)ell_len, s), "memset");
+  LJ_CUDA(ctx, launch_csr_to_ell(l.np.ptr, l.ptr.ptr, l.list.ptr, l.n, width, dst, s),
+          "transpose");
+  const cudaMemcpyKind k = where == LJ_WHERE_HOST ? cudaMemcpyDeviceToHost
+                                                  : cudaMemcpyDeviceToDevice;
+  if (where == LJ_WHERE_HOST)
+    LJ_CUDA(ctx, cudaMemcpyAsync(ell, dst, sizeof(int32_t) * (size_t)ell_len, k, s), "copy");
+  if (l.n > 0)
+    LJ_CUDA(ctx, cudaMemcpyAsync(np, l.np.ptr, sizeof(int32_t) * (size_t)l.n, k, s), "copy");
+  LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+  return LJ_OK;
+}
+
 int lj_force_csr_fp64_aos(const double* q, double* p, int32_t n, double dt, double cl2,
                           const int32_t* list, const int32_t* np, const int32_t* ptr,
                           int32_t kind, const double* box, void* stream) {

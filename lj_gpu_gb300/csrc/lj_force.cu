@@ -29,10 +29,14 @@ namespace {
 // ---------------------------------------------------------------------------
 // particle access
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ size_t rec(const Particles& P, int i) {
+  return (size_t)i * (size_t)(P.stride ? P.stride : 4);
+}
+
 template <bool SOA>
 __device__ __forceinline__ double3 load_q(const Particles& P, int i) {
   if (SOA) return make_double3(__ldg(P.qx + i), __ldg(P.qy + i), __ldg(P.qz + i));
-  const double* b = P.q + 4 * (size_t)i;
+  const double* b = P.q + rec(P, i);
   const double2 xy = __ldg(reinterpret_cast<const double2*>(b));
   return make_double3(xy.x, xy.y, __ldg(b + 2));
 }
@@ -45,7 +49,7 @@ __device__ __forceinline__ void add_p(const Particles& P, int i, double fx, doub
     P.py[i] += fy;
     P.pz[i] += fz;
   } else {
-    double* b = P.p + 4 * (size_t)i;
+    double* b = P.p + rec(P, i);
     double2 xy = *reinterpret_cast<double2*>(b);
     xy.x += fx;
     xy.y += fy;
@@ -64,7 +68,7 @@ __device__ __forceinline__ void kick_p(const Particles& P, int i, double fx, dou
     P.py[i] = fma(fy, s[1], P.py[i]);
     P.pz[i] = fma(fz, s[2], P.pz[i]);
   } else {
-    double* b = P.p + 4 * (size_t)i;
+    double* b = P.p + rec(P, i);
     double2 xy = *reinterpret_cast<double2*>(b);
     xy.x = fma(fx, s[0], xy.x);
     xy.y = fma(fy, s[1], xy.y);
@@ -81,7 +85,7 @@ __device__ __forceinline__ void red_p(const Particles& P, int i, double fx, doub
     atomicAdd(P.py + i, fy);
     atomicAdd(P.pz + i, fz);
   } else {
-    double* b = P.p + 4 * (size_t)i;
+    double* b = P.p + rec(P, i);
     atomicAdd(b + 0, fx);
     atomicAdd(b + 1, fy);
     atomicAdd(b + 2, fz);

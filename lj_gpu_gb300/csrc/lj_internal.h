@@ -11,7 +11,9 @@ namespace ljg {
 
 // Where q / p live and how they are laid out.
 struct Particles {
-  int soa;              // 0: AoS double[n][4], 1: three arrays
+  int soa;              // 0: AoS, 1: three arrays
+  int stride;           // AoS record length in doubles (0 means 4; 8 for the
+                        // interleaved z[N][8] = {q.xyzw, p.xyzw} layout)
   const double* q;      // AoS
   double* p;            // AoS
   const double* qx;     // SoA
@@ -108,6 +110,13 @@ cudaError_t launch_max_abs(const Particles& part, int n, double* out, cudaStream
 // index (the smallest is kept).
 cudaError_t launch_validate_csr(const Csr& c, int32_t* err, cudaStream_t s);
 // Exclusive scan of n int32 counts into out[0..n] (out[n] = total, int64).
+// Transposed ("ELL") lists: entry k of row i at ell[i + k * width].
+cudaError_t launch_ell_check(const int32_t* np, int n, int64_t width, int64_t len, int32_t* err,
+                             cudaStream_t s);
+cudaError_t launch_ell_to_csr(const int32_t* np, const int32_t* ell, int n, int64_t width,
+                              const int64_t* off, int32_t* out, cudaStream_t s);
+cudaError_t launch_csr_to_ell(const int32_t* np, const int32_t* ptr, const int32_t* list, int n,
+                              int64_t width, int32_t* ell, cudaStream_t s);
 // Kernels that take `guard` do nothing while *guard == 0 (nullptr: always run).
 cudaError_t launch_zero_i32(int32_t* p, int64_t count, const int32_t* guard, cudaStream_t s);
 cudaError_t launch_scan_counts(const int32_t* counts, int n, int64_t* out, void* tmp,

@@ -209,6 +209,33 @@ __global__ void k_compact_rows(const int32_t* __restrict__ np, const int32_t* __
   }
 }
 
+// The reference's transposed ("ELL") list: entry k of row i at
+// list[i + k * width] (cuda/force_cuda.cu:229-240).  Bounds of every row are
+// checked against the array length first.
+__global__ void k_ell_check(const int32_t* np, int n, int64_t width, int64_t len, int32_t* err) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int c = np[i];
+    if (c < 0 || c >= n) report(err, 1, i);
+    else if (c > 0 && (int64_t)i + (int64_t)(c - 1) * width >= len) report(err, 3, i);
+  }
+}
+
+__global__ void k_ell_to_csr(const int32_t* np, const int32_t* ell, int n, int64_t width,
+                             const int64_t* off, int32_t* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int c = np[i];
+    for (int k = 0; k < c; k++) out[off[i] + k] = ell[(int64_t)i + (int64_t)k * width];
+  }
+}
+
+__global__ void k_csr_to_ell(const int32_t* np, const int32_t* ptr, const int32_t* list, int n,
+                             int64_t width, int32_t* ell) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int c = np[i], a = ptr[i];
+    for (int k = 0; k < c; k++) ell[(int64_t)i + (int64_t)k * width] = list[a + k];
+  }
+}
+
 int grid_for(int64_t work, int block) {
   int64_t g = (work + block - 1) / block;
   if (g < 1) g = 1;
@@ -227,6 +254,24 @@ cudaError_t launch_validate_csr(const Csr& c, int32_t* err, cudaStream_t s) {
 size_t scan_tmp_bytes(int n) {
   const int tiles = (n + kScanTile - 1) / kScanTile;
   return sizeof(int64_t) * (size_t)(tiles > 0 ? tiles : 1);
+}
+
+cudaError_t launch_ell_check(const int32_t* np, int n, int64_t width, int64_t len, int32_t* err,
+                             cudaStream_t s) {
+  if (n > 0) k_ell_check<<<grid_for(n, 256), 256, 0, s>>>(np, n, width, len, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ell_to_csr(const int32_t* np, const int32_t* ell, int n, int64_t width,
+                              const int64_t* off, int32_t* out, cudaStream_t s) {
+  if (n > 0) k_ell_to_csr<<<grid_for(n, 128), 128, 0, s>>>(np, ell, n, width, off, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_csr_to_ell(const int32_t* np, const int32_t* ptr, const int32_t* list, int n,
+                              int64_t width, int32_t* ell, cudaStream_t s) {
+  if (n > 0) k_csr_to_ell<<<grid_for(n, 128), 128, 0, s>>>(np, ptr, list, n, width, ell);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_zero_i32(int32_t* p, int64_t count, const int32_t* guard, cudaStream_t s) {

@@ -51,6 +51,8 @@ void force_pair(void);
 void force_sorted(void);
 void force_next(void);
 void force_intrin(void);
+void savepair(void);
+void loadpair(void);
 
 static const int kMaxN = 400000;
 static const long kMaxPairs = 30L * 400000L;
@@ -143,6 +145,19 @@ void ref_get_csr(int* np, int* ptr, int* list) {
   std::memcpy(np, number_of_partners, sizeof(int) * (size_t)particle_number);
   std::memcpy(ptr, pointer, sizeof(int) * (size_t)particle_number);
   std::memcpy(list, sorted_list, sizeof(int) * (size_t)number_of_pairs);
+}
+
+// The reference's binary pair cache, written / read in the current directory
+// ("pair.dat", cpu_ref/force_aos.cpp:603-620).  savepair() runs makepair().
+int ref_savepair_cwd(void) {
+  number_of_pairs = 0;
+  savepair();
+  return number_of_pairs;
+}
+
+int ref_loadpair_cwd(void) {
+  loadpair();
+  return number_of_pairs;
 }
 
 // Runs `calls` invocations of the named reference routine (as measure() does).

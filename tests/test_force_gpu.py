@@ -390,3 +390,46 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(engine, prec):
             e = ol.rel_errors(host(pd), ref)
             assert (e["max_rel"] <= FP64_TOL) if prec == "fp64" else \
                 (e["max_rel_rms"] <= MIXED_TOL["max_rel_rms"]), e
+
+
+def test_interleaved_z_layout(engine):
+    """force_sorted_z's interleaved z[N][8] = {q.xyzw, p.xyzw} records."""
+    q, box, half = system("pbc_rho1")
+    ref = oracle_p(q, half, box, 3, 0.005)
+    z = np.zeros((q.shape[0], 8))
+    z[:, :4] = q
+    with engine.Context(0) as ctx:
+        ctx.set_list_csr(dev(half[0]), dev(half[1]), dev(half[2]))
+        for prec in ("fp64", "mixed"):
+            zd = dev(z)
+            for _ in range(3):
+                ctx.force_z(zd, engine.make_opts(dt=0.005, cl2=9.0, box=box, precision=prec))
+            out = host(zd)
+            assert np.array_equal(out[:, :4], q)  # positions untouched
+            e = ol.rel_errors(out[:, 4:8], ref)
+            assert (e["max_rel"] <= FP64_TOL) if prec == "fp64" else (e["max_rel_rms"] <= 1e-5)
+
+
+def test_transposed_list_round_trip(engine):
+    """The reference's transposed layout list[i + k N] in and out."""
+    q, box, half = system("pbc_rho0.5")
+    full = ol.build_list(q, 3.3, box=box, full=True)
+    n = q.shape[0]
+    npp, ptr, lst = full
+    width = n
+    ell = np.zeros(int(npp.max()) * width, np.int32)
+    for i in range(n):
+        ell[i + np.arange(npp[i]) * width] = lst[ptr[i]:ptr[i] + npp[i]]
+    ref = oracle_p(q, half, box, 1, 0.005)
+    with engine.Context(0) as ctx:
+        ctx.set_list_ell(dev(npp), dev(ell), width, kind="full")
+        for a, b in zip(ctx.get_list_csr("full"), full):
+            assert np.array_equal(a, b)
+        np2, ell2 = ctx.get_list_ell(width)
+        assert np.array_equal(np2, npp) and np.array_equal(ell2, ell)
+        pd = dev(np.zeros_like(q))
+        ctx.force_aos(dev(q), pd, engine.make_opts(dt=0.005, cl2=9.0, box=box))
+        assert ol.rel_errors(host(pd), ref)["max_rel"] <= FP64_TOL
+        bad = ell.copy()
+        with pytest.raises(engine.LJError):  # array too short for the rows
+            ctx.set_list_ell(dev(npp), dev(bad[:width]), width, kind="full")
