@@ -106,7 +106,7 @@ Periodic make_periodic(const lj_force_opts* o) {
 //   FP64 gather   : kernel 2 (compacted, one warp per row)
 int default_lanes(int precision, int method, int kernel, int64_t entries, int n) {
   const double avg = n > 0 ? (double)entries / n : 0.0;
-  if (kernel == 2 && precision == LJ_PREC_MIXED) return avg <= 24 ? 2 : 4;
+  if (kernel >= 2 && precision == LJ_PREC_MIXED) return avg <= 24 ? 2 : 4;
   if (precision == LJ_PREC_FP64 && method == LJ_METHOD_SCATTER_HALF) return avg <= 12 ? 2 : 4;
   if (avg <= 12) return 2;
   if (avg <= 24) return 4;
@@ -179,6 +179,7 @@ int install_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ptr,
   DevList& l = kind == LJ_LIST_HALF ? ctx->half : ctx->full;
   ctx->half.valid = false;
   ctx->full.valid = false;
+  ctx->tiled.valid = false;
   LJ_CUDA(ctx, l.np.ensure((size_t)n), "alloc");
   LJ_CUDA(ctx, l.ptr.ensure((size_t)n), "alloc");
   LJ_CUDA(ctx, ctx->tmp_i32a.ensure((size_t)n), "alloc");
@@ -309,13 +310,20 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
   L.cl2 = o->cl2;
   L.precision = o->precision;
   L.method = method;
+  const bool tiled_ok = ctx->tiled.valid && o->precision == LJ_PREC_MIXED &&
+                        method == LJ_METHOD_GATHER_FULL && ctx->full.n == n;
+  // The cell-tiled gather (kernel 3) runs only when asked for or chosen by
+  // lj_autotune_aos; it needs the tiled rows lj_list_build leaves behind.
   L.kernel = o->kernel ? o->kernel : default_kernel(o->precision, method);
+  if (L.kernel == 3 && !tiled_ok) L.kernel = 2;  // no tiled list: unrolled gather
   // the mixed path has no compacted scatter (FP32 atomics lose to the gather)
   if (L.kernel == 2 && method == LJ_METHOD_SCATTER_HALF && o->precision == LJ_PREC_MIXED)
     L.kernel = 1;
   L.unroll = o->unroll ? o->unroll : 4;
   if (L.kernel == 2 && !(L.unroll == 1 || L.unroll == 2 || L.unroll == 4 || L.unroll == 8))
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be 1, 2, 4 or 8");
+  if (L.kernel == 3 && !(L.unroll == 2 || L.unroll == 4))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be 2 or 4 for kernel 3");
   L.lanes = o->lanes ? o->lanes : default_lanes(o->precision, method, L.kernel, l.entries, l.n);
   L.block = o->block ? o->block : 128;
   if (n == 0) return LJ_OK;
@@ -339,6 +347,26 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
     if (o->precision == LJ_PREC_MIXED && method == LJ_METHOD_SCATTER_HALF) {
       LJ_CUDA(ctx, ctx->fscratch.ensure(3 * (size_t)n), "alloc");
       L.fscratch = ctx->fscratch.ptr;
+    }
+    if (L.kernel == 3 && L.aniso) L.kernel = 2;
+    if (L.kernel == 3) {
+      auto& T = ctx->tiled;
+      TiledList tl{};
+      tl.n = n;
+      tl.ncells = T.grid.ncells;
+      for (int d = 0; d < 3; d++) tl.gnc[d] = T.grid.nc[d];
+      tl.periodic = T.grid.periodic;
+      tl.order = T.order.ptr;
+      tl.start = T.start.ptr;
+      tl.rows = T.rows.ptr;
+      tl.cnt = T.cnt.ptr;
+      tl.maxrow = T.maxrow;
+      tl.maxc_shift = T.maxc_shift;
+      LJ_CUDA(ctx, launch_fixed_image_sorted(L, T.order.ptr, T.cq.ptr, ctx->stream), "image");
+      if (tv) LJ_CUDA(ctx, cudaEventRecord(tv[1], ctx->stream), "event");
+      LJ_CUDA(ctx, launch_force_tiled(L, tl, T.cq.ptr, ctx->stream), "tiled force");
+      if (tv) LJ_CUDA(ctx, cudaEventRecord(tv[2], ctx->stream), "event");
+      return LJ_OK;
     }
     LJ_CUDA(ctx, launch_fixed_image(L, ctx->stream), "fixed image");
   }
@@ -907,6 +935,8 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
   int maxrow = std::max(32, ((int)std::ceil(per * 1.5) + 32 + 31) / 32 * 32);
   ctx->half.valid = false;
   ctx->full.valid = false;
+  ctx->tiled.valid = false;
+  int full_maxrow = 0;
   LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
   LJ_CUDA(ctx, ctx->b_cnt_half.ensure((size_t)n), "alloc");
   LJ_CUDA(ctx, ctx->b_off_half.ensure((size_t)n + 1), "alloc");
@@ -926,6 +956,7 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
       if (!ovf) break;
       maxrow *= 2;
     }
+    if (kind == 1) full_maxrow = maxrow;
     int64_t total = 0;
     LJ_CUDA(ctx, launch_scan_counts(ctx->b_cnt_half.ptr, n, ctx->b_off_half.ptr, ctx->tmp_scan.ptr,
                                     ctx->tmp_scan.cap, s), "row scan");
@@ -955,6 +986,43 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
     l.max_row = mr;
     l.valid = true;
   }
+  if (want_full && !F.aniso && n > 0) {
+    // cell-tiled form of the full list: 16-bit indices into the 27-cell tile
+    std::vector<int32_t> counts((size_t)g.ncells);
+    LJ_CUDA(ctx, cudaMemcpyAsync(counts.data(), ctx->b_count.ptr, sizeof(int32_t) * g.ncells,
+                                 cudaMemcpyDeviceToHost, s), "counts");
+    LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+    int maxocc = 1;
+    for (int v : counts) maxocc = std::max(maxocc, v);
+    int shift = 5;
+    while ((1 << shift) < maxocc) shift++;
+    if (27 * (1 << shift) <= 65536 && 27 * (16 << shift) <= 200 * 1024) {
+      {
+        auto& T = ctx->tiled;
+        T.grid = g;
+        T.maxrow = full_maxrow;
+        T.maxc_shift = shift;
+        LJ_CUDA(ctx, T.rows.ensure((size_t)n * full_maxrow), "alloc");
+        LJ_CUDA(ctx, T.cnt.ensure((size_t)n), "alloc");
+        LJ_CUDA(ctx, T.order.ensure((size_t)n), "alloc");
+        LJ_CUDA(ctx, T.start.ensure((size_t)g.ncells + 1), "alloc");
+        LJ_CUDA(ctx, T.cq.ensure((size_t)n), "alloc");
+        LJ_CUDA(ctx, cudaMemcpyAsync(T.order.ptr, ctx->b_order2.ptr, sizeof(int32_t) * n,
+                                     cudaMemcpyDeviceToDevice, s), "copy");
+        LJ_CUDA(ctx, cudaMemcpyAsync(T.start.ptr, ctx->b_start.ptr,
+                                     sizeof(int64_t) * ((size_t)g.ncells + 1),
+                                     cudaMemcpyDeviceToDevice, s), "copy");
+        LJ_CUDA(ctx, cudaMemsetAsync(ctx->err2.ptr, 0, sizeof(int32_t), s), "memset");
+        LJ_CUDA(ctx, launch_build_rows_local(a, full_maxrow, shift, T.rows.ptr, T.cnt.ptr,
+                                             ctx->err2.ptr, s), "tiled rows");
+        int32_t ovf = 0;
+        LJ_CUDA(ctx, cudaMemcpyAsync(&ovf, ctx->err2.ptr, sizeof ovf, cudaMemcpyDeviceToHost, s),
+                "read");
+        LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+        T.valid = ovf == 0;
+      }
+    }
+  }
   ctx->list_from_host = false;
   ctx->h_np.clear();
   ctx->h_ptr.clear();
@@ -982,6 +1050,9 @@ int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts
   for (int block : {128, 256}) {
     if (try_gather) {
       if (mixed) {
+        if (ctx->tiled.valid && block == 128)
+          for (int g : {2, 4, 8})
+            for (int u : {2, 4}) cands.push_back({LJ_METHOD_GATHER_FULL, 3, g, u, 128});
         for (int g : {2, 4, 8})
           for (int u : {2, 4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 2, g, u, block});
         for (int g : {4, 8, 16}) cands.push_back({LJ_METHOD_GATHER_FULL, 1, g, 0, block});

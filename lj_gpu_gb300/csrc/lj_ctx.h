@@ -10,6 +10,7 @@
 
 #include "lj_gb300.h"
 #include "lj_internal.h"
+#include "lj_nlist.h"
 
 namespace ljg {
 
@@ -94,6 +95,16 @@ struct lj_ctx {
   size_t tev_used = 0;
   double t_ms[3] = {0, 0, 0};
   int64_t t_calls = 0;
+  // cell-tiled form of the full list built by lj_list_build (kernel 3)
+  struct Tiled {
+    bool valid = false;
+    ljg::CellGrid grid{};
+    int maxrow = 0, maxc_shift = 0;
+    ljg::DevBuf<uint16_t> rows;
+    ljg::DevBuf<int32_t> cnt, order;
+    ljg::DevBuf<int64_t> start;
+    ljg::DevBuf<int4> cq;  // per-call cell-ordered position image
+  } tiled;
   // autotuner (lj_autotune_aos): scratch p and the chosen shapes
   ljg::DevBuf<double> tune_p;
   struct Tuned {

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <type_traits>
 
+#include "lj_cells.cuh"
 #include "lj_gb300.h"
 #include "lj_internal.h"
 
@@ -524,6 +525,131 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
     kick_p<false>(P, i, widen_f32(hx + lx), widen_f32(hy + ly), widen_f32(hz + lz), K.fscale);
 }
 
+// Cell-tiled mixed gather (kernel 3).  One CTA per cell: it copies the
+// fixed-point positions of its (up to 27) neighbour cells -- contiguous runs of
+// the cell-ordered image -- into shared memory, then walks the rows of its
+// own particles, whose entries are 16-bit indices into that tile.  Every
+// position a pair needs is read from shared memory; the list bytes halve.
+// Arithmetic, masking, compensation and the FP64 kick are those of
+// k_gather_mixed_u.
+constexpr int kTiledThreads = 128;
+
+template <int G, int U, bool PBC, bool SOA>
+__global__ void __launch_bounds__(kTiledThreads) k_gather_mixed_tiled(
+    const Particles P, const TiledList T, const int4* __restrict__ cq, const MixedConsts K) {
+  extern __shared__ int4 tile[];
+  __shared__ int nstart[27], ncount[27];
+  __shared__ int nnb, centre;
+  const int c = blockIdx.x;
+  if (threadIdx.x < 27) {
+    CellGrid g{};
+    g.nc[0] = T.gnc[0];
+    g.nc[1] = T.gnc[1];
+    g.nc[2] = T.gnc[2];
+    g.ncells = T.ncells;
+    g.periodic = T.periodic;
+    int count;
+    const int c2 = neighbour_cell_at(c, g, threadIdx.x, &count);
+    if (c2 >= 0) {
+      const int64_t a = __ldg(T.start + c2), b = __ldg(T.start + c2 + 1);
+      nstart[threadIdx.x] = (int)a;
+      ncount[threadIdx.x] = (int)(b - a);
+      if (c2 == c) centre = threadIdx.x;
+    }
+    if (threadIdx.x == 0) nnb = count;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, wl = threadIdx.x & 31;
+  for (int nb = warp; nb < nnb; nb += kTiledThreads / 32)
+    for (int t = wl; t < ncount[nb]; t += 32) tile[(nb << T.maxc_shift) + t] = __ldg(cq + nstart[nb] + t);
+  __syncthreads();
+  const int s0 = nstart[centre], s1 = s0 + ncount[centre];
+  const int lane = threadIdx.x & (G - 1);
+  const unsigned mask = (1u << T.maxc_shift) - 1u;
+  for (int base = s0; base < s1; base += kTiledThreads / G) {
+    const int s = base + threadIdx.x / G;
+    const bool valid = s < s1;
+    int cnt = 0, i = 0;
+    int4 xi = make_int4(0, 0, 0, 0);
+    const uint16_t* row = T.rows;
+    if (valid) {
+      cnt = __ldg(T.cnt + s);
+      i = __ldg(T.order + s);
+      xi = tile[(centre << T.maxc_shift) + (s - s0)];
+      row = T.rows + (size_t)s * (size_t)T.maxrow;
+    }
+    int cmax = cnt;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+      cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
+    KahanF ax, ay, az;
+    ax.init();
+    ay.init();
+    az.init();
+    for (int kb = 0; kb < cmax; kb += G * U) {
+      unsigned loc[U];
+      bool ok[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int k = kb + lane + u * G;
+        ok[u] = k < cnt;
+        loc[u] = ok[u] ? (unsigned)__ldg(row + k) : 0u;
+      }
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      unsigned border = 0u;
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const float3 d = sep_mixed<false>(xi, tile[loc[u]], K);
+        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+        const bool in = ok[u] && r2 <= K.cl2_lo;
+        if (ok[u] && r2 > K.cl2_lo && r2 <= K.cl2_hi) border |= 1u << u;
+        float df = df_mixed<false>(r2, K);
+        df = in ? df : 0.0f;
+        sx = fmaf(df, d.x, sx);
+        sy = fmaf(df, d.y, sy);
+        sz = fmaf(df, d.z, sz);
+      }
+      if (__any_sync(kFullMask, border != 0u)) {
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          if (!(border & (1u << u))) continue;
+          const int j = __ldg(T.order + nstart[loc[u] >> T.maxc_shift] + (int)(loc[u] & mask));
+          const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, j), K.f64);
+          if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
+          const float3 d = sep_mixed<false>(xi, tile[loc[u]], K);
+          const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+          const float df = df_mixed<false>(r2, K);
+          sx = fmaf(df, d.x, sx);
+          sy = fmaf(df, d.y, sy);
+          sz = fmaf(df, d.z, sz);
+        }
+      }
+      ax.add(sx);
+      ay.add(sy);
+      az.add(sz);
+    }
+    float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
+    if (G > 1) {
+      group_reduce_comp<G>(hx, lx);
+      group_reduce_comp<G>(hy, ly);
+      group_reduce_comp<G>(hz, lz);
+    }
+    if (valid && lane == 0)
+      kick_p<SOA>(P, i, widen_f32(hx + lx), widen_f32(hy + ly), widen_f32(hz + lz), K.fscale);
+  }
+}
+
+template <bool SOA>
+__global__ void __launch_bounds__(256) k_fixed_image_sorted(const Particles P, int n,
+                                                            const int32_t* __restrict__ order,
+                                                            FixedAxis ax, FixedAxis ay,
+                                                            FixedAxis az, int4* __restrict__ cq) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double3 q = load_q<SOA>(P, __ldg(order + s));
+  cq[s] = make_int4(to_fixed(q.x, ax), to_fixed(q.y, ay), to_fixed(q.z, az), 0);
+}
+
 // Compacted FP64 gather (kernel 2).  One warp per row.  Candidates are
 // screened in FP32 from the fixed-point image (cheap), the survivors (inside
 // the cutoff or within 4e-6 of it) are queued in shared memory, and the FP64
@@ -942,6 +1068,50 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
   if (soa) k_kick_from_scratch<true><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
   else k_kick_from_scratch<false><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
   return cudaGetLastError();
+}
+
+cudaError_t launch_fixed_image_sorted(const ForceLaunch& L, const int32_t* order, int4* cq,
+                                      cudaStream_t s) {
+  const int n = L.csr.n;
+  if (n == 0) return cudaSuccess;
+  const int blocks = (n + 255) / 256;
+  if (L.part.soa)
+    k_fixed_image_sorted<true><<<blocks, 256, 0, s>>>(L.part, n, order, L.axis[0], L.axis[1],
+                                                      L.axis[2], cq);
+  else
+    k_fixed_image_sorted<false><<<blocks, 256, 0, s>>>(L.part, n, order, L.axis[0], L.axis[1],
+                                                       L.axis[2], cq);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_force_tiled(const ForceLaunch& L, const TiledList& T, const int4* cq,
+                               cudaStream_t s) {
+  if (T.ncells == 0 || T.n == 0) return cudaSuccess;
+  const MixedConsts K = make_mixed_consts(L);
+  if (L.aniso) return cudaErrorNotSupported;
+  const size_t smem = sizeof(int4) * 27 * ((size_t)1 << T.maxc_shift);
+  const bool pbc = L.box.on != 0, soa = L.part.soa != 0;
+  auto go = [&](auto u) -> cudaError_t {
+    constexpr int U = decltype(u)::value;
+    return dispatch_lanes(L.lanes, [&](auto g) {
+      return dispatch_bools(pbc, soa, [&](auto P, auto S) {
+        constexpr int G = decltype(g)::value;
+        auto kfn = k_gather_mixed_tiled<G, U, P.value, S.value>;
+        if (smem > 48 * 1024) {
+          cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem);
+          if (e != cudaSuccess) return e;
+        }
+        kfn<<<T.ncells, kTiledThreads, smem, s>>>(L.part, T, cq, K);
+        return cudaGetLastError();
+      });
+    });
+  };
+  switch (L.unroll) {
+    case 2: return go(std::integral_constant<int, 2>{});
+    case 4: return go(std::integral_constant<int, 4>{});
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* qfix,

@@ -89,6 +89,30 @@ struct ForceLaunch {
 // the largest coordinate magnitude (max_abs).
 void make_fixed_frame(ForceLaunch& L, double max_abs);
 
+// Cell-tiled full list (built with the list, see lj_nlist.cu): particles in
+// cell order (order[s], cells [start[c], start[c+1])), and for every slot s a
+// padded row of 16-bit local indices nb * maxc + t -- the t-th particle of
+// the nb-th neighbour cell in the walk order of for_neighbour_cells.
+struct TiledList {
+  int n;
+  int ncells;
+  int gnc[3];
+  int periodic;
+  const int32_t* order;
+  const int64_t* start;
+  const uint16_t* rows;
+  const int32_t* cnt;
+  int maxrow;
+  int maxc_shift;  // maxc = 1 << maxc_shift (>= largest cell)
+};
+
+// Position image in cell order: cq[s] = fixed(q[order[s]]).
+cudaError_t launch_fixed_image_sorted(const ForceLaunch& L, const int32_t* order, int4* cq,
+                                      cudaStream_t s);
+// Mixed gather, one CTA per cell staging its neighbour cells in shared memory.
+cudaError_t launch_force_tiled(const ForceLaunch& L, const TiledList& T, const int4* cq,
+                               cudaStream_t s);
+
 // Batched mixed gather over the rows `rows[0..nrows)` (one size class) of a
 // replica batch; padded rows (C.ptr == nullptr).
 cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* qfix,

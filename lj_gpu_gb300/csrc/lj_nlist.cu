@@ -16,16 +16,13 @@
 // candidates within a relative 4e-6 of the search sphere are re-decided in
 // FP64 with the reference's expression (dx = q_i - q_j), so the list is the
 // reference's list without spending FP64 on every candidate.
+#include "lj_cells.cuh"
 #include "lj_internal.h"
 #include "lj_nlist.h"
 
 namespace ljg {
 namespace {
 
-__device__ __forceinline__ int wrap_cell(int c, int nc) {
-  c %= nc;
-  return c < 0 ? c + nc : c;
-}
 
 __device__ __forceinline__ bool off_guard(const int32_t* guard) {
   return guard && *(volatile const int32_t*)guard == 0;
@@ -99,36 +96,6 @@ __device__ __forceinline__ bool within(const int4& a, const int4& b, const doubl
   if (r2 < k.sl2_lo) return true;
   if (!(r2 < k.sl2_hi)) return false;
   return within_fp64(q, i, j, k);
-}
-
-// Visits the candidate cells of particle i's cell.  Along an axis with fewer
-// than 3 cells every cell is visited once; otherwise c-1, c, c+1 (wrapped when
-// periodic, clipped when open).
-template <typename F>
-__device__ __forceinline__ void for_neighbour_cells(int cid, const CellGrid& g, F&& f) {
-  const int cx = cid % g.nc[0], cy = (cid / g.nc[0]) % g.nc[1], cz = cid / (g.nc[0] * g.nc[1]);
-  int lo[3], hi[3];
-  const int c[3] = {cx, cy, cz};
-  for (int d = 0; d < 3; d++) {
-    if (g.nc[d] < 3) {
-      lo[d] = 0;
-      hi[d] = g.nc[d] - 1;
-    } else if (g.periodic) {
-      lo[d] = c[d] - 1;
-      hi[d] = c[d] + 1;
-    } else {
-      lo[d] = max(c[d] - 1, 0);
-      hi[d] = min(c[d] + 1, g.nc[d] - 1);
-    }
-  }
-  for (int z = lo[2]; z <= hi[2]; z++)
-    for (int y = lo[1]; y <= hi[1]; y++)
-      for (int x = lo[0]; x <= hi[0]; x++) {
-        const int wx = g.nc[0] < 3 ? x : wrap_cell(x, g.nc[0]);
-        const int wy = g.nc[1] < 3 ? y : wrap_cell(y, g.nc[1]);
-        const int wz = g.nc[2] < 3 ? z : wrap_cell(z, g.nc[2]);
-        f((wz * g.nc[1] + wy) * g.nc[0] + wx);
-      }
 }
 
 // Deterministic order inside every cell: the slots of cell c sorted by
@@ -297,6 +264,58 @@ __global__ void __launch_bounds__(128) k_build_rows_batch(
   }
 }
 
+// The same walk as k_build_rows (full rows), writing for every slot s a
+// padded row of 16-bit local indices: nb * maxc + (slot in that cell), nb the
+// walk position of the neighbour cell.  The cell-tiled gather stages the
+// neighbour cells in that order and reads positions from shared memory.
+__global__ void __launch_bounds__(128) k_build_rows_local(
+    const double* __restrict__ q, CellGrid g, const int64_t* __restrict__ start,
+    const int32_t* __restrict__ order, const int4* __restrict__ cq, BuildConsts k, int maxrow,
+    int maxc_shift, uint16_t* __restrict__ rows, int32_t* __restrict__ cnt,
+    int32_t* __restrict__ overflow) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < g.ncells; c += nwarps) {
+    const int s0 = (int)start[c], s1 = (int)start[c + 1];
+    for (int a = s0; a < s1; a += 32) {
+      const bool act = a + lane < s1;
+      const int i = act ? order[a + lane] : -1;
+      const int4 xi = act ? cq[a + lane] : make_int4(0, 0, 0, 0);
+      const size_t base = act ? (size_t)(a + lane) * (size_t)maxrow : 0;
+      int count = 0, nb = 0;
+      for_neighbour_cells(c, g, [&](int c2) {
+        const int t0 = (int)start[c2], t1 = (int)start[c2 + 1];
+        for (int b = t0; b < t1; b += 32) {
+          int jl = -1;
+          int4 xl = make_int4(0, 0, 0, 0);
+          if (b + lane < t1) {
+            jl = order[b + lane];
+            xl = cq[b + lane];
+          }
+          const int m = min(32, t1 - b);
+          for (int kk = 0; kk < m; kk++) {
+            const int j = __shfl_sync(kFullMask, jl, kk);
+            int4 xj;
+            xj.x = __shfl_sync(kFullMask, xl.x, kk);
+            xj.y = __shfl_sync(kFullMask, xl.y, kk);
+            xj.z = __shfl_sync(kFullMask, xl.z, kk);
+            xj.w = 0;
+            if (act && j != i && within(xi, xj, q, i, j, k)) {
+              if (count < maxrow) rows[base + count] = (uint16_t)((nb << maxc_shift) + (b + kk - t0));
+              count++;
+            }
+          }
+        }
+        nb++;
+      });
+      if (act) {
+        cnt[a + lane] = min(count, maxrow);
+        if (count > maxrow) atomicMax(overflow, 1);
+      }
+    }
+  }
+}
+
 // Compact copy of padded rows: out[off[i] + m] = rows[i * maxrow + m].
 __global__ void k_compact_padded(const int32_t* __restrict__ cnt, const int32_t* __restrict__ rows,
                                  int maxrow, const int64_t* __restrict__ off, int n,
@@ -422,6 +441,17 @@ cudaError_t launch_build_rows(const BuildArgs& a, bool half, int maxrow, int32_t
   else
     k_build_rows<false><<<blocks, 128, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, maxrow,
                                                rows, cnt, overflow, guard);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_rows_local(const BuildArgs& a, int maxrow, int maxc_shift,
+                                    uint16_t* rows, int32_t* cnt, int32_t* overflow,
+                                    cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  const BuildConsts k = make_build_consts(a);
+  const int blocks = grid_of((int64_t)a.grid.ncells * 32, 128, 152 * 64);
+  k_build_rows_local<<<blocks, 128, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, maxrow,
+                                            maxc_shift, rows, cnt, overflow);
   return cudaGetLastError();
 }
 

@@ -50,6 +50,10 @@ cudaError_t launch_sort_cells(const int64_t* start, int ncells, const int32_t* o
 cudaError_t launch_build_rows(const BuildArgs& a, bool half, int maxrow, int32_t* rows,
                               int32_t* cnt, int32_t* overflow, cudaStream_t s,
                               const int32_t* guard = nullptr);
+// Local-index rows for the cell-tiled gather (full rows, slot-indexed).
+cudaError_t launch_build_rows_local(const BuildArgs& a, int maxrow, int maxc_shift,
+                                    uint16_t* rows, int32_t* cnt, int32_t* overflow,
+                                    cudaStream_t s);
 cudaError_t launch_compact_padded(const int32_t* cnt, const int32_t* rows, int maxrow,
                                   const int64_t* off, int n, int32_t* out, cudaStream_t s,
                                   const int32_t* guard = nullptr);

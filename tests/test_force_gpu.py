@@ -433,3 +433,38 @@ def test_transposed_list_round_trip(engine):
         bad = ell.copy()
         with pytest.raises(engine.LJError):  # array too short for the rows
             ctx.set_list_ell(dev(npp), dev(bad[:width]), width, kind="full")
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+@pytest.mark.parametrize("layout", ["aos", "soa"])
+def test_cell_tiled_gather_on_device_built_lists(engine, name, layout):
+    """Kernel 3 (cell-tiled, 16-bit local rows; opt-in or autotuned) runs once
+    the list was built on the device; it must meet the mixed bounds, and
+    kernels 2 and 3 must see exactly the same pairs."""
+    q, box, half = system(name)
+    ref = oracle_p(q, half, box, 1, 0.005)
+    with engine.Context(0) as ctx:
+        qd = dev(q)
+        ctx.build_list(qd, 3.3, box=box)
+        outs = {}
+        for kernel, lanes, unroll in ((3, 0, 0), (3, 2, 2), (3, 8, 4), (2, 4, 4)):
+            opts = engine.make_opts(dt=0.005, cl2=9.0, box=box, precision="mixed",
+                                    method="gather", kernel=kernel, lanes=lanes, unroll=unroll)
+            if layout == "aos":
+                pd = dev(np.zeros_like(q))
+                ctx.force_aos(qd, pd, opts)
+                got = host(pd)
+            else:
+                qs = [dev(q[:, d].copy()) for d in range(3)]
+                ps = [dev(np.zeros(q.shape[0])) for _ in range(3)]
+                ctx.force_soa(*qs, *ps, opts)
+                got = np.zeros_like(q)
+                for d in range(3):
+                    got[:, d] = host(ps[d])
+            e = ol.rel_errors(got, ref)
+            for k, tol in MIXED_TOL.items():
+                assert e[k] <= tol, (kernel, lanes, unroll, k, e)
+            outs[(kernel, lanes, unroll)] = got
+        # same pairs: tiled vs unrolled differ only by summation order
+        a, b = outs[(3, 0, 0)], outs[(2, 4, 4)]
+        assert ol.rel_errors(a, b)["max_rel_rms"] <= 1e-6
