@@ -246,6 +246,8 @@ template <bool SOA>
 __global__ void __launch_bounds__(256) k_fixed_image(const Particles P, int n,
                                                      FixedAxis ax, FixedAxis ay, FixedAxis az,
                                                      int4* __restrict__ out) {
+  // the pair kernel that follows may launch now (it waits for this grid)
+  asm volatile("griddepcontrol.launch_dependents;");
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double3 q = load_q<SOA>(P, i);
@@ -350,7 +352,9 @@ __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const C
 // the warp, so every lane takes part in every iteration (no divergence, warp
 // votes are safe); each lane issues U independent index loads and U position
 // gathers before any arithmetic, which keeps U x 32 gathers in flight per
-// warp.  Pairs outside the cutoff are masked with a select, not a branch.  The
+// warp; the next step's indices load while this step's positions are in
+// flight, so the index -> position chain is exposed once per row, not once
+// per step.  Pairs outside the cutoff are masked with a select, not a branch.  The
 // U terms of one step are summed in FP32 and the step sum enters the Kahan
 // accumulator, so compensation costs 12/U operations per pair.
 // Accepts padded rows (C.ptr == nullptr, row i at i * C.stride).
@@ -361,6 +365,9 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / G;
   const int lane = t & (G - 1);
+  // Launched as a programmatic dependent of the image pass: nothing the
+  // stream wrote before may be read until the preceding grid has finished.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const bool valid = i < C.n;
   int cnt = 0;
   int64_t k0 = 0;
@@ -377,18 +384,28 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
   ax.init();
   ay.init();
   az.init();
+  int jn[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int k = lane + u * G;
+    jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
+  }
   for (int base = 0; base < cmax; base += G * U) {
     int jj[U];
     bool ok[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      const int k = base + lane + u * G;
-      ok[u] = k < cnt;
-      jj[u] = ok[u] ? __ldg(C.list + k0 + k) : 0;
+      ok[u] = base + lane + u * G < cnt;
+      jj[u] = jn[u];
     }
     int4 xj[U];
 #pragma unroll
     for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = base + G * U + lane + u * G;
+      jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
+    }
     float sx = 0.f, sy = 0.f, sz = 0.f;
     unsigned border = 0u;
 #pragma unroll
@@ -471,18 +488,28 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
   ax.init();
   ay.init();
   az.init();
+  int jn[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int k = lane + u * G;
+    jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
+  }
   for (int base = 0; base < cmax; base += G * U) {
     int jj[U];
     bool ok[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      const int k = base + lane + u * G;
-      ok[u] = k < cnt;
-      jj[u] = ok[u] ? __ldg(C.list + k0 + k) : 0;
+      ok[u] = base + lane + u * G < cnt;
+      jj[u] = jn[u];
     }
     int4 xj[U];
 #pragma unroll
     for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = base + G * U + lane + u * G;
+      jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
+    }
     float sx = 0.f, sy = 0.f, sz = 0.f;
     unsigned border = 0u;
 #pragma unroll
@@ -888,6 +915,25 @@ MixedConsts make_mixed_consts(const ForceLaunch& L) {
   return k;
 }
 
+// Launches `kfn` as a programmatic dependent of the previous kernel on `s`:
+// its blocks may be scheduled while that kernel drains, and the kernel itself
+// executes griddepcontrol.wait before reading anything the stream produced.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_dependent(void (*kfn)(KArgs...), int blocks, int block, cudaStream_t s,
+                             Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kfn, args...);
+}
+
 template <typename F>
 cudaError_t dispatch_lanes(int lanes, F&& f) {
   switch (lanes) {
@@ -1020,13 +1066,12 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
       return dispatch_lanes(L.lanes, [&](auto g) {
         return dispatch_bools(pbc, soa, [&](auto P, auto S) {
           constexpr int G = decltype(g)::value;
+          const int4* qf = L.qfix;
           if (L.aniso)
-            k_gather_mixed_u<G, U, P.value, S.value, true>
-                <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, K);
-          else
-            k_gather_mixed_u<G, U, P.value, S.value, false>
-                <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, K);
-          return cudaGetLastError();
+            return launch_dependent(k_gather_mixed_u<G, U, P.value, S.value, true>, blocks,
+                                    block, s, L.part, L.csr, qf, K);
+          return launch_dependent(k_gather_mixed_u<G, U, P.value, S.value, false>, blocks, block,
+                                  s, L.part, L.csr, qf, K);
         });
       });
     };
