@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--shape", action="append", default=[],
+                    help="extra mixed AoS gather variant KERNEL,LANES,UNROLL (e.g. 3,4,2 for "
+                         "the cell-tiled kernel), timed beside the default variants")
     ap.add_argument("--workload", default="rho0.5_108k",
                     choices=["rho0.5_108k", "rho1_108k", "precision_1m", "large_8m",
                              "batch_512"],
@@ -230,8 +233,10 @@ def run_ours(args, dist, density=DENSITY):
     _, P_full, max_full = ctx.list_info("full")
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    def time_variant(prec, method, layout, steps, warmup):
-        opts = lj.make_opts(dt=DT, cl2=RC * RC, box=L, precision=prec, method=method)
+    def time_variant(prec, method, layout, shape, steps, warmup):
+        k, g, u = shape if shape else (0, 0, 0)
+        opts = lj.make_opts(dt=DT, cl2=RC * RC, box=L, precision=prec, method=method,
+                            kernel=k, lanes=g, unroll=u)
         pd = torch.zeros_like(qd)
         ps = [torch.zeros(N, dtype=torch.float64, device=dev) for _ in range(3)]
 
@@ -267,29 +272,34 @@ def run_ours(args, dist, density=DENSITY):
         tuned[prec] = {"method": {1: "gather", 2: "scatter"}[best.method], "kernel": best.kernel,
                        "lanes": best.lanes, "unroll": best.unroll, "block": best.block,
                        "ms_warm": ms_t}
-    variants = [("mixed", "auto", "aos"), ("mixed", "gather", "soa"),
-                ("mixed", "scatter", "aos"), ("fp64", "auto", "aos"),
-                ("fp64", "scatter", "soa"), ("fp64", "gather", "aos")]
+    variants = [("mixed", "auto", "aos", None), ("mixed", "gather", "soa", None),
+                ("mixed", "scatter", "aos", None), ("fp64", "auto", "aos", None),
+                ("fp64", "scatter", "soa", None), ("fp64", "gather", "aos", None)]
+    for s in args.shape:
+        variants.append(("mixed", "gather", "aos", tuple(int(x) for x in s.split(","))))
+    key = lambda v: "/".join(v[:3]) + ("/k%dg%du%d" % v[3] if v[3] else "")
+    by_key = {key(v): v for v in variants}
     results = {}
     clocks = None
     for v in variants:
         steps = args.steps if v[0] == "mixed" else max(3, min(args.steps, 20))
-        if v == ("mixed", "auto", "aos"):
+        if v == ("mixed", "auto", "aos", None):
             with ClockSampler(dist.local) as cs:
                 ms = time_variant(*v, steps, args.warmup)
             clocks = cs.summary()
         else:
             ms = time_variant(*v, steps, max(3, min(args.warmup, 5)))
         t_max = dist.max(ms / steps / 1e3, dev)  # seconds per call, slowest rank
-        results["/".join(v)] = {"s_per_call": t_max, "steps": steps,
+        results[key(v)] = {"s_per_call": t_max, "steps": steps,
                                 "gpairs": dist.world * P / t_max / 1e9}
 
-    best_mixed = max((k for k in results if k.startswith("mixed")),
+    # explicit --shape variants are reported, not taken as the headline
+    best_mixed = max((k for k in results if k.startswith("mixed") and by_key[k][3] is None),
                      key=lambda k: results[k]["gpairs"])
     best_fp64 = max((k for k in results if k.startswith("fp64")),
                     key=lambda k: results[k]["gpairs"])
     head = results[best_mixed]
-    prec, method, layout = best_mixed.split("/")
+    prec, method, layout, _ = by_key[best_mixed]
     if method == "auto":
         method = tuned[prec]["method"]
 
@@ -297,7 +307,7 @@ def run_ours(args, dist, density=DENSITY):
     # between the position-image pass and the pair kernel)
     def stage_times(variant, steps):
         ctx.set_timing(True)
-        time_variant(*variant.split("/"), steps, 0)
+        time_variant(*by_key[variant], steps, 0)
         t = ctx.get_timing()
         ctx.set_timing(False)
         return t[0] / t[3], t[1] / t[3]

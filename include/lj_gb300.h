@@ -111,8 +111,10 @@ int lj_ctx_get_timing(lj_ctx* ctx, double* ms, int64_t* calls);
  *   pointer[i] + number_of_partners[i] <= n_entries, 0 <= sorted_list[k] < n.
  * kind: LJ_LIST_HALF (each unordered pair once, as makepair with
  * EN_ACTION_REACTION builds it) or LJ_LIST_FULL (each pair in both rows).
- * A half list is expanded on the device into the full list the gather
- * kernels use; both are kept. */
+ * Rows are copied into a compact layout (row i directly after row i - 1),
+ * so pointer may describe any non-overlapping placement; lj_list_get_csr
+ * returns the compact form.  A half list is expanded on the device into the
+ * full list the gather kernels use; both are kept. */
 int lj_list_set_csr(lj_ctx* ctx, int32_t n, const int32_t* number_of_partners,
                     const int32_t* pointer, const int32_t* sorted_list, int64_t n_entries,
                     int32_t kind, int32_t where);

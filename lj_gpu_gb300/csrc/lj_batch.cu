@@ -77,8 +77,8 @@ __global__ void k_batch_image(const double* __restrict__ q, int n,
 __global__ void k_batch_copy_ref(const int4* __restrict__ qfix, int4* __restrict__ qref, int n,
                                  const int32_t* __restrict__ flags) {
   if (!flags[B_REBUILD]) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) qref[i] = qfix[i];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    qref[i] = qfix[i];
 }
 
 __global__ void k_batch_finish(int32_t* flags) {
@@ -200,7 +200,7 @@ cudaError_t batch_rebuild(BatchState& b, const double* q, double sl2, cudaStream
                                    b.order2.ptr, b.cq2.ptr, b.maxrow, b.rows.ptr, b.cnt.ptr,
                                    b.flags.ptr + B_OVERFLOW, s, g)))
     return e;
-  k_batch_copy_ref<<<gridn(b.n, 256), 256, 0, s>>>(b.qfix.ptr, b.qref.ptr, b.n, b.flags.ptr);
+  k_batch_copy_ref<<<std::min(gridn(b.n, 256), 152 * 8), 256, 0, s>>>(b.qfix.ptr, b.qref.ptr, b.n, b.flags.ptr);
   k_batch_finish<<<1, 32, 0, s>>>(b.flags.ptr);
   return cudaGetLastError();
 }

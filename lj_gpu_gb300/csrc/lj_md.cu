@@ -85,8 +85,8 @@ __global__ void __launch_bounds__(256) k_md_drift(double* __restrict__ q,
 __global__ void k_md_copy_ref(const int4* __restrict__ qfix, int4* __restrict__ qref, int n,
                               const int32_t* __restrict__ flags) {
   if (!flags[F_REBUILD]) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) qref[i] = qfix[i];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    qref[i] = qfix[i];
 }
 
 __global__ void k_md_finish(int32_t* flags) {
@@ -241,7 +241,7 @@ cudaError_t md_rebuild(MdState& m, bool compact, cudaStream_t s) {
                                    s, g)))
       return e;
   }
-  k_md_copy_ref<<<grid1(m.n, 256), 256, 0, s>>>(m.qfix.ptr, m.qref.ptr, m.n, m.flags.ptr);
+  k_md_copy_ref<<<std::min(grid1(m.n, 256), 152 * 8), 256, 0, s>>>(m.qfix.ptr, m.qref.ptr, m.n, m.flags.ptr);
   k_md_finish<<<1, 32, 0, s>>>(m.flags.ptr);
   return cudaGetLastError();
 }

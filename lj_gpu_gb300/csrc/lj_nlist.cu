@@ -28,23 +28,29 @@ __device__ __forceinline__ bool off_guard(const int32_t* guard) {
   return guard && *(volatile const int32_t*)guard == 0;
 }
 
+// Grids are capped near one resident wave (152 SMs) and the kernels stride
+// over their work: a guarded launch whose flag is off then costs one short
+// wave of exiting blocks instead of one block per 256 particles.
+constexpr int kResidentBlocks = 152 * 12;     // 128-thread blocks (40 registers: 12 resident)
+constexpr int kResidentBlocks256 = 152 * 8;   // 256-thread blocks
+
 __global__ void k_bin(const double* __restrict__ q, int n, CellGrid g, int32_t* __restrict__ cell,
                       int32_t* __restrict__ count, const int32_t* guard) {
   if (off_guard(guard)) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double* b = q + 4 * (size_t)i;
-  int c[3];
-  for (int d = 0; d < 3; d++) {
-    const double t = (b[d] - g.lo[d]) * g.inv_w[d];
-    int ci = (int)floor(t);
-    if (g.periodic) ci = wrap_cell(ci, g.nc[d]);
-    else ci = min(max(ci, 0), g.nc[d] - 1);
-    c[d] = ci;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double* b = q + 4 * (size_t)i;
+    int c[3];
+    for (int d = 0; d < 3; d++) {
+      const double t = (b[d] - g.lo[d]) * g.inv_w[d];
+      int ci = (int)floor(t);
+      if (g.periodic) ci = wrap_cell(ci, g.nc[d]);
+      else ci = min(max(ci, 0), g.nc[d] - 1);
+      c[d] = ci;
+    }
+    const int id = (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
+    cell[i] = id;
+    atomicAdd(count + id, 1);
   }
-  const int id = (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
-  cell[i] = id;
-  atomicAdd(count + id, 1);
 }
 
 __global__ void k_place(const int32_t* __restrict__ cell, int n, const int64_t* __restrict__ start,
@@ -52,12 +58,12 @@ __global__ void k_place(const int32_t* __restrict__ cell, int n, const int64_t* 
                         int32_t* __restrict__ order, int4* __restrict__ cq,
                         const int32_t* guard) {
   if (off_guard(guard)) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int c = cell[i];
-  const int slot = (int)start[c] + atomicAdd(cursor + c, 1);
-  order[slot] = i;
-  cq[slot] = qfix[i];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int c = cell[i];
+    const int slot = (int)start[c] + atomicAdd(cursor + c, 1);
+    order[slot] = i;
+    cq[slot] = qfix[i];
+  }
 }
 
 struct BuildConsts {
@@ -122,63 +128,132 @@ __global__ void k_sort_cells(const int64_t* __restrict__ start, int ncells,
   }
 }
 
-// Warp-cooperative neighbour build into a padded row layout (row i at
-// i * maxrow, length cnt[i]).  One warp per cell: the lanes hold up to 32 of
-// the cell's particles; every neighbour cell is read 32 particles at a time
-// with coalesced loads and broadcast to all lanes by shuffles, so a candidate
-// costs shuffles and FP32/integer arithmetic instead of a scattered load.
-// Rows come out in cell-walk order (deterministic after k_sort_cells).  A row
-// longer than maxrow is truncated and raises *overflow.
-template <bool HALF>
-__global__ void __launch_bounds__(128) k_build_rows(const double* __restrict__ q, CellGrid g,
-                                                    const int64_t* __restrict__ start,
-                                                    const int32_t* __restrict__ order,
-                                                    const int4* __restrict__ cq, BuildConsts k,
-                                                    int maxrow, int32_t* __restrict__ rows,
-                                                    int32_t* __restrict__ cnt,
-                                                    int32_t* __restrict__ overflow,
-                                                    const int32_t* guard) {
-  if (off_guard(guard)) return;
-  const int lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < g.ncells; c += nwarps) {
-    const int s0 = (int)start[c], s1 = (int)start[c + 1];
-    for (int a = s0; a < s1; a += 32) {
-      const bool act = a + lane < s1;
-      const int i = act ? order[a + lane] : -1;
-      const int4 xi = act ? cq[a + lane] : make_int4(0, 0, 0, 0);
-      const size_t base = act ? (size_t)i * (size_t)maxrow : 0;
-      int count = 0;
-      for_neighbour_cells(c, g, [&](int c2) {
-        const int t0 = (int)start[c2], t1 = (int)start[c2 + 1];
-        for (int b = t0; b < t1; b += 32) {
-          int jl = -1;
-          int4 xl = make_int4(0, 0, 0, 0);
-          if (b + lane < t1) {
-            jl = order[b + lane];
-            xl = cq[b + lane];
+// Warp-cooperative neighbour build into padded rows.  One warp per cell:
+// the candidates of the 27-cell walk are flattened into one sequence (walk
+// order, then slot order inside each cell) and the lanes hold 32 consecutive
+// candidates with coalesced loads; the cell's own particles are staged in
+// shared memory and the warp loops over them, testing all 32 candidates
+// against one particle per step.  A ballot and a prefix popcount place the
+// hits of a step at the end of that particle's row, so rows come out in walk
+// order (deterministic after k_sort_cells) and every store writes a run of
+// one row.  Rows longer than maxrow are truncated and raise *overflow.
+constexpr int kBuildBlock = 128;
+constexpr int kBuildWarps = kBuildBlock / 32;
+constexpr int kBuildI = 64;  // particles of the centre cell staged per pass
+
+enum RowMode { ROWS_FULL = 0, ROWS_HALF = 1, ROWS_LOCAL = 2 };
+
+struct BuildStage {
+  int4 xi[kBuildI];  // fixed-point position, particle index in w
+  int nb_start[32];  // first slot of each walk cell
+  int nb_pref[32];   // candidates before it in the flattened walk
+};
+
+// Row of the particle in slot a + t: particle-indexed (i * maxrow) for
+// ROWS_FULL / ROWS_HALF, slot-indexed 16-bit local indices (walk position
+// << maxc_shift | slot in that cell) for ROWS_LOCAL.
+template <int MODE>
+__device__ __forceinline__ void build_cell_rows(int c, int cell_base, const CellGrid& g,
+                                                const int64_t* __restrict__ start,
+                                                const int32_t* __restrict__ order,
+                                                const int4* __restrict__ cq, const double* q,
+                                                const BuildConsts& k, int maxrow, int maxc_shift,
+                                                int32_t* __restrict__ rows,
+                                                uint16_t* __restrict__ lrows,
+                                                int32_t* __restrict__ cnt, int32_t* overflow,
+                                                BuildStage& ws, int lane) {
+  int nnb;
+  const int c2 = neighbour_cell_at(c, g, lane, &nnb);
+  int st = 0, n2 = 0;
+  if (c2 >= 0) {
+    const int64_t a = start[cell_base + c2];
+    st = (int)a;
+    n2 = (int)(start[cell_base + c2 + 1] - a);
+  }
+  int incl = n2;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int v = __shfl_up_sync(kFullMask, incl, off);
+    if (lane >= off) incl += v;
+  }
+  const int total = __shfl_sync(kFullMask, incl, 31);
+  if (lane < nnb) {
+    ws.nb_start[lane] = st;
+    ws.nb_pref[lane] = incl - n2;
+  }
+  __syncwarp();
+  const int s0 = (int)start[cell_base + c], s1 = (int)start[cell_base + c + 1];
+  for (int a = s0; a < s1; a += kBuildI) {
+    const int ni = min(kBuildI, s1 - a);
+    for (int t = lane; t < ni; t += 32) {
+      int4 x = cq[a + t];
+      x.w = order[a + t];
+      ws.xi[t] = x;
+    }
+    __syncwarp();
+    int len0 = 0, len1 = 0;  // row lengths of staged particles lane, lane + 32
+    for (int base = 0; base < total; base += 32) {
+      const int gi = base + lane;
+      const bool act = gi < total;
+      int nb = 0;  // walk cell holding candidate gi: last nb with nb_pref[nb] <= gi
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1)
+        if (nb + step < nnb && ws.nb_pref[nb + step] <= gi) nb += step;
+      const int r = gi - ws.nb_pref[nb];
+      int j = -1;
+      int4 xj = make_int4(0, 0, 0, 0);
+      if (act) {
+        j = order[ws.nb_start[nb] + r];
+        xj = cq[ws.nb_start[nb] + r];
+      }
+      const uint16_t loc = (uint16_t)((nb << maxc_shift) + r);
+#pragma unroll 2
+      for (int t = 0; t < ni; t++) {
+        const int4 x = ws.xi[t];
+        const int i = x.w;
+        const bool ok = act && j != i && (MODE != ROWS_HALF || j > i) && within(x, xj, q, i, j, k);
+        const unsigned bal = __ballot_sync(kFullMask, ok);
+        if (bal) {
+          const int len = __shfl_sync(kFullMask, t < 32 ? len0 : len1, t & 31);
+          const int pos = len + __popc(bal & ((1u << lane) - 1u));
+          if (ok && pos < maxrow) {
+            if (MODE == ROWS_LOCAL) lrows[(size_t)(a + t) * (size_t)maxrow + pos] = loc;
+            else rows[(size_t)i * (size_t)maxrow + pos] = j;
           }
-          const int m = min(32, t1 - b);
-          for (int kk = 0; kk < m; kk++) {
-            const int j = __shfl_sync(kFullMask, jl, kk);
-            int4 xj;
-            xj.x = __shfl_sync(kFullMask, xl.x, kk);
-            xj.y = __shfl_sync(kFullMask, xl.y, kk);
-            xj.z = __shfl_sync(kFullMask, xl.z, kk);
-            xj.w = 0;
-            if (act && j != i && (!HALF || j > i) && within(xi, xj, q, i, j, k)) {
-              if (count < maxrow) rows[base + count] = j;
-              count++;
-            }
+          if (lane == (t & 31)) {
+            if (t < 32) len0 += __popc(bal);
+            else len1 += __popc(bal);
           }
         }
-      });
-      if (act) {
-        cnt[i] = min(count, maxrow);
-        if (count > maxrow) atomicMax(overflow, 1);
       }
     }
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int t = lane + 32 * h;
+      if (t < ni) {
+        const int len = h ? len1 : len0;
+        cnt[MODE == ROWS_LOCAL ? a + t : ws.xi[t].w] = min(len, maxrow);
+        if (len > maxrow) atomicMax(overflow, 1);
+      }
+    }
+    __syncwarp();
   }
+  __syncwarp();
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kBuildBlock) k_build_rows(
+    const double* __restrict__ q, CellGrid g, const int64_t* __restrict__ start,
+    const int32_t* __restrict__ order, const int4* __restrict__ cq, BuildConsts k, int maxrow,
+    int maxc_shift, int32_t* __restrict__ rows, uint16_t* __restrict__ lrows,
+    int32_t* __restrict__ cnt, int32_t* __restrict__ overflow, const int32_t* guard) {
+  if (off_guard(guard)) return;
+  __shared__ BuildStage stage[kBuildWarps];
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < g.ncells; c += nwarps)
+    build_cell_rows<MODE>(c, 0, g, start, order, cq, q, k, maxrow, maxc_shift, rows, lrows, cnt,
+                          overflow, stage[threadIdx.x >> 5], lane);
 }
 
 // Batched binning: every replica has its own grid starting at cell_base.
@@ -186,26 +261,27 @@ __global__ void k_bin_batch(const double* __restrict__ q, int n, const int32_t* 
                             const ReplicaInfo* __restrict__ reps, int32_t* __restrict__ cell,
                             int32_t* __restrict__ count, const int32_t* guard) {
   if (off_guard(guard)) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const ReplicaInfo& R = reps[rid[i]];
-  const double* b = q + 4 * (size_t)i;
-  int c[3];
-  for (int d = 0; d < 3; d++) c[d] = wrap_cell((int)floor(b[d] * R.inv_w[d]), R.nc[d]);
-  const int id = R.cell_base + (c[2] * R.nc[1] + c[1]) * R.nc[0] + c[0];
-  cell[i] = id;
-  atomicAdd(count + id, 1);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const ReplicaInfo& R = reps[rid[i]];
+    const double* b = q + 4 * (size_t)i;
+    int c[3];
+    for (int d = 0; d < 3; d++) c[d] = wrap_cell((int)floor(b[d] * R.inv_w[d]), R.nc[d]);
+    const int id = R.cell_base + (c[2] * R.nc[1] + c[1]) * R.nc[0] + c[0];
+    cell[i] = id;
+    atomicAdd(count + id, 1);
+  }
 }
 
-// Batched warp-cooperative row build (full rows): as k_build_rows, with the
-// cell's replica supplying the local grid and the membership constants.
-__global__ void __launch_bounds__(128) k_build_rows_batch(
+// Batched row build (full rows): as k_build_rows, with the cell's replica
+// supplying the local grid and the membership constants.
+__global__ void __launch_bounds__(kBuildBlock) k_build_rows_batch(
     const double* __restrict__ q, const ReplicaInfo* __restrict__ reps,
     const int32_t* __restrict__ cell_rid, int ncells, double sl2,
     const int64_t* __restrict__ start, const int32_t* __restrict__ order,
     const int4* __restrict__ cq, int maxrow, int32_t* __restrict__ rows,
     int32_t* __restrict__ cnt, int32_t* __restrict__ overflow, const int32_t* guard) {
   if (off_guard(guard)) return;
+  __shared__ BuildStage stage[kBuildWarps];
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncells; c += nwarps) {
@@ -224,95 +300,8 @@ __global__ void __launch_bounds__(128) k_build_rows_batch(
       k.half_bits[d] = R.half_bits[d];
     }
     k.sl2 = sl2;
-    const int s0 = (int)start[c], s1 = (int)start[c + 1];
-    for (int a = s0; a < s1; a += 32) {
-      const bool act = a + lane < s1;
-      const int i = act ? order[a + lane] : -1;
-      const int4 xi = act ? cq[a + lane] : make_int4(0, 0, 0, 0);
-      const size_t base = act ? (size_t)i * (size_t)maxrow : 0;
-      int count = 0;
-      for_neighbour_cells(c - R.cell_base, g, [&](int c2l) {
-        const int c2 = R.cell_base + c2l;
-        const int t0 = (int)start[c2], t1 = (int)start[c2 + 1];
-        for (int b = t0; b < t1; b += 32) {
-          int jl = -1;
-          int4 xl = make_int4(0, 0, 0, 0);
-          if (b + lane < t1) {
-            jl = order[b + lane];
-            xl = cq[b + lane];
-          }
-          const int m = min(32, t1 - b);
-          for (int kk = 0; kk < m; kk++) {
-            const int j = __shfl_sync(kFullMask, jl, kk);
-            int4 xj;
-            xj.x = __shfl_sync(kFullMask, xl.x, kk);
-            xj.y = __shfl_sync(kFullMask, xl.y, kk);
-            xj.z = __shfl_sync(kFullMask, xl.z, kk);
-            xj.w = 0;
-            if (act && j != i && within(xi, xj, q, i, j, k)) {
-              if (count < maxrow) rows[base + count] = j;
-              count++;
-            }
-          }
-        }
-      });
-      if (act) {
-        cnt[i] = min(count, maxrow);
-        if (count > maxrow) atomicMax(overflow, 1);
-      }
-    }
-  }
-}
-
-// The same walk as k_build_rows (full rows), writing for every slot s a
-// padded row of 16-bit local indices: nb * maxc + (slot in that cell), nb the
-// walk position of the neighbour cell.  The cell-tiled gather stages the
-// neighbour cells in that order and reads positions from shared memory.
-__global__ void __launch_bounds__(128) k_build_rows_local(
-    const double* __restrict__ q, CellGrid g, const int64_t* __restrict__ start,
-    const int32_t* __restrict__ order, const int4* __restrict__ cq, BuildConsts k, int maxrow,
-    int maxc_shift, uint16_t* __restrict__ rows, int32_t* __restrict__ cnt,
-    int32_t* __restrict__ overflow) {
-  const int lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < g.ncells; c += nwarps) {
-    const int s0 = (int)start[c], s1 = (int)start[c + 1];
-    for (int a = s0; a < s1; a += 32) {
-      const bool act = a + lane < s1;
-      const int i = act ? order[a + lane] : -1;
-      const int4 xi = act ? cq[a + lane] : make_int4(0, 0, 0, 0);
-      const size_t base = act ? (size_t)(a + lane) * (size_t)maxrow : 0;
-      int count = 0, nb = 0;
-      for_neighbour_cells(c, g, [&](int c2) {
-        const int t0 = (int)start[c2], t1 = (int)start[c2 + 1];
-        for (int b = t0; b < t1; b += 32) {
-          int jl = -1;
-          int4 xl = make_int4(0, 0, 0, 0);
-          if (b + lane < t1) {
-            jl = order[b + lane];
-            xl = cq[b + lane];
-          }
-          const int m = min(32, t1 - b);
-          for (int kk = 0; kk < m; kk++) {
-            const int j = __shfl_sync(kFullMask, jl, kk);
-            int4 xj;
-            xj.x = __shfl_sync(kFullMask, xl.x, kk);
-            xj.y = __shfl_sync(kFullMask, xl.y, kk);
-            xj.z = __shfl_sync(kFullMask, xl.z, kk);
-            xj.w = 0;
-            if (act && j != i && within(xi, xj, q, i, j, k)) {
-              if (count < maxrow) rows[base + count] = (uint16_t)((nb << maxc_shift) + (b + kk - t0));
-              count++;
-            }
-          }
-        }
-        nb++;
-      });
-      if (act) {
-        cnt[a + lane] = min(count, maxrow);
-        if (count > maxrow) atomicMax(overflow, 1);
-      }
-    }
+    build_cell_rows<ROWS_FULL>(c - R.cell_base, R.cell_base, g, start, order, cq, q, k, maxrow,
+                               0, rows, nullptr, cnt, overflow, stage[threadIdx.x >> 5], lane);
   }
 }
 
@@ -385,7 +374,7 @@ cudaError_t launch_bin(const double* q, int n, const CellGrid& g, int32_t* cell,
   cudaError_t e = guard ? launch_zero_i32(count, g.ncells, guard, s)
                         : cudaMemsetAsync(count, 0, sizeof(int32_t) * (size_t)g.ncells, s);
   if (e != cudaSuccess || n == 0) return e;
-  k_bin<<<grid_of(n, 256, 0), 256, 0, s>>>(q, n, g, cell, count, guard);
+  k_bin<<<grid_of(n, 256, kResidentBlocks256), 256, 0, s>>>(q, n, g, cell, count, guard);
   return cudaGetLastError();
 }
 
@@ -395,7 +384,7 @@ cudaError_t launch_place(const int32_t* cell, int n, const int64_t* start, int32
   cudaError_t e = guard ? launch_zero_i32(cursor, ncells, guard, s)
                         : cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncells, s);
   if (e != cudaSuccess || n == 0) return e;
-  k_place<<<grid_of(n, 256, 0), 256, 0, s>>>(cell, n, start, cursor, qfix, order, cq, guard);
+  k_place<<<grid_of(n, 256, kResidentBlocks256), 256, 0, s>>>(cell, n, start, cursor, qfix, order, cq, guard);
   return cudaGetLastError();
 }
 
@@ -424,7 +413,7 @@ BuildConsts make_build_consts(const BuildArgs& a) {
 cudaError_t launch_sort_cells(const int64_t* start, int ncells, const int32_t* order,
                               const int4* cq, int32_t* order2, int4* cq2, cudaStream_t s,
                               const int32_t* guard) {
-  k_sort_cells<<<grid_of((int64_t)ncells * 32, 256, 152 * 64), 256, 0, s>>>(
+  k_sort_cells<<<grid_of((int64_t)ncells * 32, 256, kResidentBlocks256), 256, 0, s>>>(
       start, ncells, order, cq, order2, cq2, guard);
   return cudaGetLastError();
 }
@@ -434,13 +423,13 @@ cudaError_t launch_build_rows(const BuildArgs& a, bool half, int maxrow, int32_t
                               const int32_t* guard) {
   if (a.n == 0) return cudaSuccess;
   const BuildConsts k = make_build_consts(a);
-  const int blocks = grid_of((int64_t)a.grid.ncells * 32, 128, 152 * 64);
+  const int blocks = grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, kResidentBlocks);
   if (half)
-    k_build_rows<true><<<blocks, 128, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, maxrow,
-                                              rows, cnt, overflow, guard);
+    k_build_rows<ROWS_HALF><<<blocks, kBuildBlock, 0, s>>>(
+        a.q, a.grid, a.start, a.order, a.cq, k, maxrow, 0, rows, nullptr, cnt, overflow, guard);
   else
-    k_build_rows<false><<<blocks, 128, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, maxrow,
-                                               rows, cnt, overflow, guard);
+    k_build_rows<ROWS_FULL><<<blocks, kBuildBlock, 0, s>>>(
+        a.q, a.grid, a.start, a.order, a.cq, k, maxrow, 0, rows, nullptr, cnt, overflow, guard);
   return cudaGetLastError();
 }
 
@@ -449,9 +438,10 @@ cudaError_t launch_build_rows_local(const BuildArgs& a, int maxrow, int maxc_shi
                                     cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   const BuildConsts k = make_build_consts(a);
-  const int blocks = grid_of((int64_t)a.grid.ncells * 32, 128, 152 * 64);
-  k_build_rows_local<<<blocks, 128, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, maxrow,
-                                            maxc_shift, rows, cnt, overflow);
+  const int blocks = grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, kResidentBlocks);
+  k_build_rows<ROWS_LOCAL><<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k,
+                                                          maxrow, maxc_shift, nullptr, rows, cnt,
+                                                          overflow, nullptr);
   return cudaGetLastError();
 }
 
@@ -459,7 +449,7 @@ cudaError_t launch_compact_padded(const int32_t* cnt, const int32_t* rows, int m
                                   const int64_t* off, int n, int32_t* out, cudaStream_t s,
                                   const int32_t* guard) {
   if (n > 0)
-    k_compact_padded<<<grid_of((int64_t)n * 32, 256, 152 * 64), 256, 0, s>>>(
+    k_compact_padded<<<grid_of((int64_t)n * 32, 256, kResidentBlocks256), 256, 0, s>>>(
         cnt, rows, maxrow, off, n, out, guard);
   return cudaGetLastError();
 }
@@ -470,7 +460,7 @@ cudaError_t launch_bin_batch(const double* q, int n, const int32_t* rid, const R
                              const int32_t* guard) {
   cudaError_t e = launch_zero_i32(count, ncells, guard, s);
   if (e != cudaSuccess || n == 0) return e;
-  k_bin_batch<<<grid_of(n, 256, 0), 256, 0, s>>>(q, n, rid, reps, cell, count, guard);
+  k_bin_batch<<<grid_of(n, 256, kResidentBlocks256), 256, 0, s>>>(q, n, rid, reps, cell, count, guard);
   return cudaGetLastError();
 }
 
@@ -479,9 +469,9 @@ cudaError_t launch_build_rows_batch(const double* q, const ReplicaInfo* reps,
                                     const int64_t* start, const int32_t* order, const int4* cq,
                                     int maxrow, int32_t* rows, int32_t* cnt, int32_t* overflow,
                                     cudaStream_t s, const int32_t* guard) {
-  const int blocks = grid_of((int64_t)ncells * 32, 128, 152 * 64);
-  k_build_rows_batch<<<blocks, 128, 0, s>>>(q, reps, cell_rid, ncells, sl2, start, order, cq,
-                                            maxrow, rows, cnt, overflow, guard);
+  const int blocks = grid_of((int64_t)ncells * 32, kBuildBlock, kResidentBlocks);
+  k_build_rows_batch<<<blocks, kBuildBlock, 0, s>>>(q, reps, cell_rid, ncells, sl2, start, order,
+                                                    cq, maxrow, rows, cnt, overflow, guard);
   return cudaGetLastError();
 }
 
