@@ -21,15 +21,6 @@ namespace {
 
 enum { B_REBUILD = 0, B_OVERFLOW = 2, B_COUNT = 3, B_STEP = 5, B_WORDS = 8 };
 
-__device__ __forceinline__ double bwrap(double x, double len) {
-  long long sb = 0;
-  if (!(x < len) && x == x) sb = __double_as_longlong(-len);
-  if (x < 0.0) sb = __double_as_longlong(len);
-  double y = x + __longlong_as_double(sb);
-  if (y >= len) y = 0.0;
-  return y;
-}
-
 __global__ void __launch_bounds__(256) k_batch_drift(double* __restrict__ q,
                                                      const double* __restrict__ p, int n,
                                                      double dt, const int32_t* __restrict__ rid,
@@ -48,9 +39,9 @@ __global__ void __launch_bounds__(256) k_batch_drift(double* __restrict__ q,
   const ReplicaInfo& R = reps[rid[i]];
   double* qi = q + 4 * (size_t)i;
   const double* pi = p + 4 * (size_t)i;
-  const double x = bwrap(fma(pi[0], dt, qi[0]), R.len[0]);
-  const double y = bwrap(fma(pi[1], dt, qi[1]), R.len[1]);
-  const double z = bwrap(fma(pi[2], dt, qi[2]), R.len[2]);
+  const double x = wrap_into_box(fma(pi[0], dt, qi[0]), R.len[0]);
+  const double y = wrap_into_box(fma(pi[1], dt, qi[1]), R.len[1]);
+  const double z = wrap_into_box(fma(pi[2], dt, qi[2]), R.len[2]);
   qi[0] = x;
   qi[1] = y;
   qi[2] = z;

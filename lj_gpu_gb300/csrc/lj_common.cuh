@@ -105,6 +105,24 @@ __device__ __forceinline__ int to_fixed(double x, const FixedAxis& ax) {
   return (b >> 63) ? -(int)v : (int)v;
 }
 
+// Periodic wrap of a coordinate into [0, len) with one shift and one FP64
+// add; the comparisons run on the IEEE bit patterns (integer pipe), since
+// FP64 compares issue on the slow FP64 pipe.  x >= len (or +inf) gets -len,
+// x < 0 gets +len, anything else (including -0.0) adds +0.0; a result that
+// rounds up to len becomes 0; NaN passes through.
+__device__ __forceinline__ double wrap_into_box(double x, double len) {
+  const unsigned long long b = (unsigned long long)dbits(x);
+  const unsigned long long lb = (unsigned long long)dbits(len);
+  const unsigned long long mag = b & 0x7fffffffffffffffull;
+  const bool nan = mag > 0x7ff0000000000000ull;
+  long long sb = 0;
+  if ((b >> 63) == 0 && !nan && b >= lb) sb = dbits(-len);
+  if ((b >> 63) != 0 && mag != 0 && !nan) sb = (long long)lb;
+  const double y = x + __longlong_as_double(sb);
+  const unsigned long long by = (unsigned long long)dbits(y);
+  return ((by >> 63) == 0 && by <= 0x7ff0000000000000ull && by >= lb) ? 0.0 : y;
+}
+
 // int32 difference with wrap-around (no signed-overflow UB)
 __device__ __forceinline__ int wrap_sub(int a, int b) {
   return (int)((unsigned)a - (unsigned)b);

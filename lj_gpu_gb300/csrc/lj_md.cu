@@ -36,16 +36,6 @@ enum {
   F_WORDS = 8
 };
 
-__device__ __forceinline__ double wrap_box(double x, double len) {
-  // single shift into [0, len), selected on bit patterns: one FP64 add
-  long long sb = 0;
-  if (!(x < len) && x == x) sb = __double_as_longlong(-len);
-  if (x < 0.0) sb = __double_as_longlong(len);
-  double y = x + __longlong_as_double(sb);
-  if (y >= len) y = 0.0;  // -tiny + len rounds up to len
-  return y;
-}
-
 __global__ void __launch_bounds__(256) k_md_drift(double* __restrict__ q,
                                                   const double* __restrict__ p, int n, double dt,
                                                   double lx, double ly, double lz, FixedAxis ax,
@@ -69,9 +59,9 @@ __global__ void __launch_bounds__(256) k_md_drift(double* __restrict__ q,
   const double pz = pi[2];
   double2 xy = *reinterpret_cast<double2*>(qi);
   double z = qi[2];
-  xy.x = wrap_box(fma(pxy.x, dt, xy.x), lx);
-  xy.y = wrap_box(fma(pxy.y, dt, xy.y), ly);
-  z = wrap_box(fma(pz, dt, z), lz);
+  xy.x = wrap_into_box(fma(pxy.x, dt, xy.x), lx);
+  xy.y = wrap_into_box(fma(pxy.y, dt, xy.y), ly);
+  z = wrap_into_box(fma(pz, dt, z), lz);
   *reinterpret_cast<double2*>(qi) = xy;
   qi[2] = z;
   const int4 x = make_int4(to_fixed(xy.x, ax), to_fixed(xy.y, ay), to_fixed(z, az), 0);
@@ -382,6 +372,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   b.order = m.order2.ptr;  // per-cell sorted order (k_sort_cells output)
   b.cq = m.cq2.ptr;
   b.cell = m.cell.ptr;
+  b.superset = 1;  // the force kernels and energies apply the cutoff
   b.want_half = mixed ? 0 : 1;
   b.want_full = mixed ? 1 : 0;
 

@@ -16,6 +16,8 @@
 // candidates within a relative 4e-6 of the search sphere are re-decided in
 // FP64 with the reference's expression (dx = q_i - q_j), so the list is the
 // reference's list without spending FP64 on every candidate.
+#include <type_traits>
+
 #include "lj_cells.cuh"
 #include "lj_internal.h"
 #include "lj_nlist.h"
@@ -131,28 +133,35 @@ __global__ void k_sort_cells(const int64_t* __restrict__ start, int ncells,
 // Warp-cooperative neighbour build into padded rows.  One warp per cell:
 // the candidates of the 27-cell walk are flattened into one sequence (walk
 // order, then slot order inside each cell) and the lanes hold 32 consecutive
-// candidates with coalesced loads; the cell's own particles are staged in
-// shared memory and the warp loops over them, testing all 32 candidates
-// against one particle per step.  A ballot and a prefix popcount place the
-// hits of a step at the end of that particle's row, so rows come out in walk
-// order (deterministic after k_sort_cells) and every store writes a run of
-// one row.  Rows longer than maxrow are truncated and raise *overflow.
+// candidates, loaded with coalesced reads.  Up to 32 of the cell's own
+// particles are staged in shared memory; the warp tests all 32 candidates
+// against one of them per step and keeps the step's ballot in that
+// particle's lane.  After a chunk of candidates every lane appends its hits,
+// in candidate order, to its particle's row, so rows come out in walk order
+// (deterministic after k_sort_cells).  Membership is decided in FP32 from the
+// exact fixed-point separation; a step with a candidate near the search
+// sphere re-decides those in FP64 with the reference's expression.  Rows
+// longer than maxrow are truncated and raise *overflow.
 constexpr int kBuildBlock = 128;
 constexpr int kBuildWarps = kBuildBlock / 32;
-constexpr int kBuildI = 64;  // particles of the centre cell staged per pass
 
 enum RowMode { ROWS_FULL = 0, ROWS_HALF = 1, ROWS_LOCAL = 2 };
 
 struct BuildStage {
-  int4 xi[kBuildI];  // fixed-point position, particle index in w
+  int4 xi[32];       // fixed-point position, particle index in w
+  unsigned bal[32];  // hits of staged particle t among the chunk's candidates
+  int js[32];        // the chunk's candidates (particle index)
+  int loc[32];       // and their 16-bit local indices (ROWS_LOCAL)
   int nb_start[32];  // first slot of each walk cell
   int nb_pref[32];   // candidates before it in the flattened walk
 };
 
 // Row of the particle in slot a + t: particle-indexed (i * maxrow) for
 // ROWS_FULL / ROWS_HALF, slot-indexed 16-bit local indices (walk position
-// << maxc_shift | slot in that cell) for ROWS_LOCAL.
-template <int MODE>
+// << maxc_shift | slot in that cell) for ROWS_LOCAL.  EXACT: the reference's
+// membership (FP64 re-decision near the sphere); otherwise every candidate
+// with FP32 r2 < sl2_hi, a superset by at most a relative 4e-6.
+template <int MODE, bool ANISO, bool EXACT>
 __device__ __forceinline__ void build_cell_rows(int c, int cell_base, const CellGrid& g,
                                                 const int64_t* __restrict__ start,
                                                 const int32_t* __restrict__ order,
@@ -177,21 +186,26 @@ __device__ __forceinline__ void build_cell_rows(int c, int cell_base, const Cell
     if (lane >= off) incl += v;
   }
   const int total = __shfl_sync(kFullMask, incl, 31);
+  // flattened index of the centre cell's first slot
+  const int self_pref =
+      __shfl_sync(kFullMask, incl - n2, __ffs(__ballot_sync(kFullMask, c2 == c)) - 1);
   if (lane < nnb) {
     ws.nb_start[lane] = st;
     ws.nb_pref[lane] = incl - n2;
   }
-  __syncwarp();
+  const float sl2 = EXACT ? k.sl2_lo : k.sl2_hi;
   const int s0 = (int)start[cell_base + c], s1 = (int)start[cell_base + c + 1];
-  for (int a = s0; a < s1; a += kBuildI) {
-    const int ni = min(kBuildI, s1 - a);
-    for (int t = lane; t < ni; t += 32) {
-      int4 x = cq[a + t];
-      x.w = order[a + t];
-      ws.xi[t] = x;
+  for (int a = s0; a < s1; a += 32) {
+    const int ni = min(32, s1 - a);
+    int my_i = -1;
+    if (lane < ni) {
+      int4 x = cq[a + lane];
+      my_i = order[a + lane];
+      x.w = my_i;
+      ws.xi[lane] = x;
     }
     __syncwarp();
-    int len0 = 0, len1 = 0;  // row lengths of staged particles lane, lane + 32
+    int len = 0;
     for (int base = 0; base < total; base += 32) {
       const int gi = base + lane;
       const bool act = gi < total;
@@ -206,42 +220,58 @@ __device__ __forceinline__ void build_cell_rows(int c, int cell_base, const Cell
         j = order[ws.nb_start[nb] + r];
         xj = cq[ws.nb_start[nb] + r];
       }
-      const uint16_t loc = (uint16_t)((nb << maxc_shift) + r);
-#pragma unroll 2
+      ws.js[lane] = j;
+      if (MODE == ROWS_LOCAL) ws.loc[lane] = (nb << maxc_shift) + r;
+#pragma unroll 4
       for (int t = 0; t < ni; t++) {
         const int4 x = ws.xi[t];
-        const int i = x.w;
-        const bool ok = act && j != i && (MODE != ROWS_HALF || j > i) && within(x, xj, q, i, j, k);
-        const unsigned bal = __ballot_sync(kFullMask, ok);
-        if (bal) {
-          const int len = __shfl_sync(kFullMask, t < 32 ? len0 : len1, t & 31);
-          const int pos = len + __popc(bal & ((1u << lane) - 1u));
-          if (ok && pos < maxrow) {
-            if (MODE == ROWS_LOCAL) lrows[(size_t)(a + t) * (size_t)maxrow + pos] = loc;
-            else rows[(size_t)i * (size_t)maxrow + pos] = j;
-          }
-          if (lane == (t & 31)) {
-            if (t < 32) len0 += __popc(bal);
-            else len1 += __popc(bal);
-          }
+        float dx = (float)wrap_sub(x.x, xj.x), dy = (float)wrap_sub(x.y, xj.y),
+              dz = (float)wrap_sub(x.z, xj.z);
+        if (ANISO) {
+          dx = fmaf(dx, k.u_hi[0], dx * k.u_lo[0]);
+          dy = fmaf(dy, k.u_hi[1], dy * k.u_lo[1]);
+          dz = fmaf(dz, k.u_hi[2], dz * k.u_lo[2]);
         }
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const bool keep = MODE != ROWS_HALF || j > x.w;
+        unsigned bal = __ballot_sync(kFullMask, keep && r2 < sl2);
+        if (EXACT) {
+          const bool maybe = keep && r2 < k.sl2_hi;
+          if (__ballot_sync(kFullMask, maybe) != bal)
+            bal |= __ballot_sync(kFullMask,
+                                 act && maybe && !(r2 < sl2) && within_fp64(q, x.w, j, k));
+        }
+        if (lane == 0) ws.bal[t] = bal;
       }
+      __syncwarp();
+      unsigned mine = lane < ni ? ws.bal[lane] : 0u;
+      mine &= __ballot_sync(kFullMask, act);
+      if (MODE != ROWS_HALF) {  // a particle is its own candidate once
+        const int d = self_pref + (a - s0) + lane - base;
+        if (d >= 0 && d < 32) mine &= ~(1u << d);
+      }
+      const size_t rb = (size_t)(MODE == ROWS_LOCAL ? a + lane : max(my_i, 0)) * (size_t)maxrow;
+      while (mine) {
+        const int b = __ffs(mine) - 1;
+        mine &= mine - 1u;
+        if (len < maxrow) {
+          if (MODE == ROWS_LOCAL) lrows[rb + len] = (uint16_t)ws.loc[b];
+          else rows[rb + len] = ws.js[b];
+        }
+        len++;
+      }
+      __syncwarp();
     }
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int t = lane + 32 * h;
-      if (t < ni) {
-        const int len = h ? len1 : len0;
-        cnt[MODE == ROWS_LOCAL ? a + t : ws.xi[t].w] = min(len, maxrow);
-        if (len > maxrow) atomicMax(overflow, 1);
-      }
+    if (lane < ni) {
+      cnt[MODE == ROWS_LOCAL ? a + lane : my_i] = min(len, maxrow);
+      if (len > maxrow) atomicMax(overflow, 1);
     }
     __syncwarp();
   }
   __syncwarp();
 }
 
-template <int MODE>
+template <int MODE, bool ANISO, bool EXACT>
 __global__ void __launch_bounds__(kBuildBlock) k_build_rows(
     const double* __restrict__ q, CellGrid g, const int64_t* __restrict__ start,
     const int32_t* __restrict__ order, const int4* __restrict__ cq, BuildConsts k, int maxrow,
@@ -252,8 +282,9 @@ __global__ void __launch_bounds__(kBuildBlock) k_build_rows(
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < g.ncells; c += nwarps)
-    build_cell_rows<MODE>(c, 0, g, start, order, cq, q, k, maxrow, maxc_shift, rows, lrows, cnt,
-                          overflow, stage[threadIdx.x >> 5], lane);
+    build_cell_rows<MODE, ANISO, EXACT>(c, 0, g, start, order, cq, q, k, maxrow, maxc_shift,
+                                        rows, lrows, cnt, overflow, stage[threadIdx.x >> 5],
+                                        lane);
 }
 
 // Batched binning: every replica has its own grid starting at cell_base.
@@ -300,8 +331,9 @@ __global__ void __launch_bounds__(kBuildBlock) k_build_rows_batch(
       k.half_bits[d] = R.half_bits[d];
     }
     k.sl2 = sl2;
-    build_cell_rows<ROWS_FULL>(c - R.cell_base, R.cell_base, g, start, order, cq, q, k, maxrow,
-                               0, rows, nullptr, cnt, overflow, stage[threadIdx.x >> 5], lane);
+    build_cell_rows<ROWS_FULL, false, false>(c - R.cell_base, R.cell_base, g, start, order, cq,
+                                             q, k, maxrow, 0, rows, nullptr, cnt, overflow,
+                                             stage[threadIdx.x >> 5], lane);
   }
 }
 
@@ -424,13 +456,22 @@ cudaError_t launch_build_rows(const BuildArgs& a, bool half, int maxrow, int32_t
   if (a.n == 0) return cudaSuccess;
   const BuildConsts k = make_build_consts(a);
   const int blocks = grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, kResidentBlocks);
-  if (half)
-    k_build_rows<ROWS_HALF><<<blocks, kBuildBlock, 0, s>>>(
-        a.q, a.grid, a.start, a.order, a.cq, k, maxrow, 0, rows, nullptr, cnt, overflow, guard);
-  else
-    k_build_rows<ROWS_FULL><<<blocks, kBuildBlock, 0, s>>>(
-        a.q, a.grid, a.start, a.order, a.cq, k, maxrow, 0, rows, nullptr, cnt, overflow, guard);
-  return cudaGetLastError();
+  auto go = [&](auto mode, auto aniso, auto exact) {
+    k_build_rows<decltype(mode)::value, decltype(aniso)::value, decltype(exact)::value>
+        <<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, maxrow, 0, rows,
+                                        nullptr, cnt, overflow, guard);
+    return cudaGetLastError();
+  };
+  using H = std::integral_constant<int, ROWS_HALF>;
+  using F = std::integral_constant<int, ROWS_FULL>;
+  using T = std::true_type;
+  using N = std::false_type;
+  if (a.superset) {
+    if (a.aniso) return half ? go(H{}, T{}, N{}) : go(F{}, T{}, N{});
+    return half ? go(H{}, N{}, N{}) : go(F{}, N{}, N{});
+  }
+  if (a.aniso) return half ? go(H{}, T{}, T{}) : go(F{}, T{}, T{});
+  return half ? go(H{}, N{}, T{}) : go(F{}, N{}, T{});
 }
 
 cudaError_t launch_build_rows_local(const BuildArgs& a, int maxrow, int maxc_shift,
@@ -439,9 +480,10 @@ cudaError_t launch_build_rows_local(const BuildArgs& a, int maxrow, int maxc_shi
   if (a.n == 0) return cudaSuccess;
   const BuildConsts k = make_build_consts(a);
   const int blocks = grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, kResidentBlocks);
-  k_build_rows<ROWS_LOCAL><<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k,
-                                                          maxrow, maxc_shift, nullptr, rows, cnt,
-                                                          overflow, nullptr);
+  // the cell-tiled kernel applies the cutoff itself; isotropic frames only
+  k_build_rows<ROWS_LOCAL, false, false><<<blocks, kBuildBlock, 0, s>>>(
+      a.q, a.grid, a.start, a.order, a.cq, k, maxrow, maxc_shift, nullptr, rows, cnt, overflow,
+      nullptr);
   return cudaGetLastError();
 }
 

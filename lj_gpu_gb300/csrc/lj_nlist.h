@@ -30,6 +30,10 @@ struct BuildArgs {
   const int4* cq;
   const int32_t* cell;
   int want_half, want_full;
+  // 0: membership exactly r2 < search^2 in FP64 (the reference's list);
+  // 1: a superset that may add pairs within a relative 4e-6 outside the
+  //    sphere (Verlet lists whose users apply the cutoff themselves)
+  int superset;
 };
 
 double key_to_double(unsigned long long k);
