@@ -15,7 +15,9 @@
 // Membership is decided in FP32 from the exact int32 fixed-point separation;
 // candidates within a relative 4e-6 of the search sphere are re-decided in
 // FP64 with the reference's expression (dx = q_i - q_j), so the list is the
-// reference's list without spending FP64 on every candidate.
+// reference's list without spending FP64 on every candidate.  Verlet lists
+// of the MD and batch loops (whose users apply the cutoff) skip that
+// re-decision and keep every candidate below the upper edge of the band.
 #include <type_traits>
 
 #include "lj_cells.cuh"
@@ -91,20 +93,6 @@ __device__ __forceinline__ bool within_fp64(const double* q, int i, int j, const
   return r2 < k.sl2;
 }
 
-__device__ __forceinline__ bool within(const int4& a, const int4& b, const double* q, int i,
-                                       int j, const BuildConsts& k) {
-  float dx = (float)wrap_sub(a.x, b.x), dy = (float)wrap_sub(a.y, b.y),
-        dz = (float)wrap_sub(a.z, b.z);
-  if (k.aniso) {
-    dx = fmaf(dx, k.u_hi[0], dx * k.u_lo[0]);
-    dy = fmaf(dy, k.u_hi[1], dy * k.u_lo[1]);
-    dz = fmaf(dz, k.u_hi[2], dz * k.u_lo[2]);
-  }
-  const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-  if (r2 < k.sl2_lo) return true;
-  if (!(r2 < k.sl2_hi)) return false;
-  return within_fp64(q, i, j, k);
-}
 
 // Deterministic order inside every cell: the slots of cell c sorted by
 // particle index (one warp per cell, stable rank sort, out of place).  The
