@@ -55,6 +55,11 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="time the 'auto' variants with the engine's default launch shapes "
+                         "(what the tuner picks on this workload) instead of tuning first; "
+                         "for runs under a profiler, whose per-launch overhead swamps the "
+                         "tuner's timings")
     ap.add_argument("--shape", action="append", default=[],
                     help="extra mixed AoS gather variant KERNEL,LANES,UNROLL (e.g. 3,4,2 for "
                          "the cell-tiled kernel), timed beside the default variants")
@@ -267,6 +272,10 @@ def run_ours(args, dist, density=DENSITY):
     # leave the launch fields at their defaults ("auto" below)
     tuned = {}
     for prec in ("mixed", "fp64"):
+        if args.no_autotune:
+            tuned[prec] = {"method": "gather" if prec == "mixed" else "scatter",
+                           "kernel": "default", "note": "autotuner skipped (--no-autotune)"}
+            continue
         best, ms_t = ctx.autotune(qd, lj.make_opts(dt=DT, cl2=RC * RC, box=L, precision=prec),
                                   reps=5)
         tuned[prec] = {"method": {1: "gather", 2: "scatter"}[best.method], "kernel": best.kernel,
