@@ -72,7 +72,11 @@ typedef struct lj_force_opts {
   int32_t lanes;      /* lanes per i-particle, 0 = default, else 1,2,4,..,32  */
   int32_t block;      /* threads per block, 0 = default, else 64..256         */
   int32_t kernel;     /* kernel generation: 0 = default, 1 = simple strided,
-                         2 = unrolled / compacted (see lj_force.cu)           */
+                         2 = unrolled / compacted, 3 = cell-tiled (mixed
+                         gather on a list from lj_list_build), 4 = unrolled
+                         with 16-byte index loads (mixed gather, unroll 4);
+                         3 and 4 fall back to 2 when their list form is
+                         missing (see lj_force.cu)                          */
   int32_t unroll;     /* entries per lane in flight (kernel 2), 0 = default   */
   int32_t reserved;
 } lj_force_opts;

@@ -76,6 +76,9 @@ int check_opts(lj_ctx* ctx, const lj_force_opts* o) {
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "lanes must be 0 or a power of two <= 32");
   if (o->block != 0 && (o->block < 64 || o->block > 256 || (o->block % 32) != 0))
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "block must be 0 or a multiple of 32 in [64, 256]");
+  if (o->kernel < 0 || o->kernel > 4)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kernel must be 0 (default) or 1..4");
+  if (o->unroll < 0) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be >= 0");
   if (!(o->cl2 >= 0.0) || !std::isfinite(o->dt))
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "cl2 must be >= 0 and dt finite");
   if (o->periodic) {
@@ -170,6 +173,35 @@ int expand_full(lj_ctx* ctx) {
   return LJ_OK;
 }
 
+// Keeps beside ctx->full a copy whose rows start on 16-byte boundaries (each
+// row zero-padded to a multiple of 4 entries), read by the mixed gather's
+// vector index loads.  Lists beyond 2^31 padded entries keep the scalar path.
+int build_aligned(lj_ctx* ctx) {
+  DevList& f = ctx->full;
+  f.avalid = false;
+  const int n = f.n;
+  if (!f.valid || n == 0) return LJ_OK;
+  cudaStream_t s = ctx->stream;
+  LJ_CUDA(ctx, ctx->tmp_i32a.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, f.aoff.ensure((size_t)n + 1), "alloc");
+  LJ_CUDA(ctx, ctx->tmp_scan.ensure(scan_tmp_bytes(n)), "alloc");
+  LJ_CUDA(ctx, launch_round4(f.np.ptr, n, ctx->tmp_i32a.ptr, s), "round");
+  LJ_CUDA(ctx, launch_scan_counts(ctx->tmp_i32a.ptr, n, f.aoff.ptr, ctx->tmp_scan.ptr,
+                                  ctx->tmp_scan.cap, s), "scan");
+  int64_t total = 0;
+  LJ_CUDA(ctx, cudaMemcpyAsync(&total, f.aoff.ptr + n, sizeof total, cudaMemcpyDeviceToHost, s),
+          "total");
+  LJ_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+  if (total > 0x7fffffffll) return LJ_OK;
+  LJ_CUDA(ctx, f.aptr.ensure((size_t)n), "alloc");
+  LJ_CUDA(ctx, f.alist.ensure((size_t)std::max<int64_t>(total, 4)), "alloc");
+  LJ_CUDA(ctx, launch_copy_rows4(f.np.ptr, f.ptr.ptr, f.list.ptr, f.aoff.ptr, n, f.alist.ptr,
+                                 f.aptr.ptr, s), "aligned copy");
+  f.aentries = total;
+  f.avalid = true;
+  return LJ_OK;
+}
+
 // Copies a caller CSR into the context, validates it, and stores it compact:
 // rows in i order, contiguous, pointer[i] = sum of the earlier row lengths
 // (what sortpair produces).  Kernels that sweep several rows as one flat range
@@ -179,6 +211,7 @@ int install_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ptr,
   DevList& l = kind == LJ_LIST_HALF ? ctx->half : ctx->full;
   ctx->half.valid = false;
   ctx->full.valid = false;
+  ctx->full.avalid = false;
   ctx->tiled.valid = false;
   LJ_CUDA(ctx, l.np.ensure((size_t)n), "alloc");
   LJ_CUDA(ctx, l.ptr.ensure((size_t)n), "alloc");
@@ -235,7 +268,7 @@ int install_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ptr,
       return rc;
     }
   }
-  return LJ_OK;
+  return build_aligned(ctx);
 }
 
 int resolve_method(lj_ctx* ctx, const lj_force_opts* o, int* method) {
@@ -316,15 +349,24 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
   // lj_autotune_aos; it needs the tiled rows lj_list_build leaves behind.
   L.kernel = o->kernel ? o->kernel : default_kernel(o->precision, method);
   if (L.kernel == 3 && !tiled_ok) L.kernel = 2;  // no tiled list: unrolled gather
+  if (L.kernel == 4 && !(o->precision == LJ_PREC_MIXED && method == LJ_METHOD_GATHER_FULL &&
+                         ctx->full.avalid && ctx->full.n == n))
+    L.kernel = 2;  // no aligned copy: scalar index loads
   // the mixed path has no compacted scatter (FP32 atomics lose to the gather)
   if (L.kernel == 2 && method == LJ_METHOD_SCATTER_HALF && o->precision == LJ_PREC_MIXED)
     L.kernel = 1;
   L.unroll = o->unroll ? o->unroll : 4;
+  if (L.kernel == 4 && L.unroll != 4)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kernel 4 takes 4 entries per lane (unroll 0 or 4)");
   if (L.kernel == 2 && !(L.unroll == 1 || L.unroll == 2 || L.unroll == 4 || L.unroll == 8))
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be 1, 2, 4 or 8");
   if (L.kernel == 3 && !(L.unroll == 2 || L.unroll == 4))
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be 2 or 4 for kernel 3");
   L.lanes = o->lanes ? o->lanes : default_lanes(o->precision, method, L.kernel, l.entries, l.n);
+  if (L.kernel == 4) {  // kernel 2 over the 16-byte-aligned copy, vector index loads
+    L.csr = ctx->full.acsr();
+    L.kernel = 2;
+  }
   L.block = o->block ? o->block : 128;
   if (n == 0) return LJ_OK;
   const bool fixed = o->precision == LJ_PREC_MIXED || L.kernel == 2;
@@ -935,6 +977,7 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
   int maxrow = std::max(32, ((int)std::ceil(per * 1.5) + 32 + 31) / 32 * 32);
   ctx->half.valid = false;
   ctx->full.valid = false;
+  ctx->full.avalid = false;
   ctx->tiled.valid = false;
   int full_maxrow = 0;
   LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
@@ -1027,7 +1070,7 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
   ctx->h_np.clear();
   ctx->h_ptr.clear();
   ctx->h_list.clear();
-  return LJ_OK;
+  return want_full ? build_aligned(ctx) : LJ_OK;
 }
 
 int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts* opts,
@@ -1041,6 +1084,7 @@ int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts
   if (!ctx->half.valid && !ctx->full.valid) return fail(ctx, LJ_ERR_NO_LIST, "no list installed");
   if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
   LJ_CUDA(ctx, ctx->tune_p.ensure(4 * (size_t)n), "alloc");
+  LJ_CUDA(ctx, ctx->tune_flush.ensure((size_t)256 << 20), "alloc");  // > L2 (126 MB)
   // candidate launch shapes
   struct Cand { int method, kernel, lanes, unroll, block; };
   std::vector<Cand> cands;
@@ -1055,6 +1099,8 @@ int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts
             for (int u : {2, 4}) cands.push_back({LJ_METHOD_GATHER_FULL, 3, g, u, 128});
         for (int g : {2, 4, 8})
           for (int u : {2, 4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 2, g, u, block});
+        if (ctx->full.avalid)
+          for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 4, g, 4, block});
         for (int g : {4, 8, 16}) cands.push_back({LJ_METHOD_GATHER_FULL, 1, g, 0, block});
       } else {
         if (block == 128) cands.push_back({LJ_METHOD_GATHER_FULL, 2, 0, 0, 128});
@@ -1085,16 +1131,24 @@ int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts
       ctx->timing = was_timing;
       return rc;
     }
-    LJ_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream), "event");
-    for (int r = 0; r < reps; r++)
+    // each call starts with a cold L2 (a write larger than it in between), as
+    // a force call on a list that does not fit in L2 -- or a benchmark that
+    // flushes -- sees it; warm-cache timings favour other shapes
+    float ms = 0.f;
+    for (int r = 0; r < reps; r++) {
+      LJ_CUDA(ctx, cudaMemsetAsync(ctx->tune_flush.ptr, r & 0xff, ctx->tune_flush.cap,
+                                   ctx->stream), "flush");
+      LJ_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream), "event");
       if ((rc = run_force(ctx, part, n, &o))) {
         ctx->timing = was_timing;
         return rc;
       }
-    LJ_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream), "event");
-    LJ_CUDA(ctx, cudaEventSynchronize(ctx->ev[1]), "sync");
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+      LJ_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream), "event");
+      LJ_CUDA(ctx, cudaEventSynchronize(ctx->ev[1]), "sync");
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]);
+      ms += t;
+    }
     if (ms / reps < best_ms) {
       best_ms = ms / reps;
       win = c;
@@ -1155,6 +1209,9 @@ int lj_measure_aos(lj_ctx* ctx, const double* q_host, double* p_host, int32_t n,
       return rc;
     if ((rc = copy_in(ctx, l.list.ptr, ctx->h_list.data(), ctx->h_list.size(), LJ_WHERE_HOST)))
       return rc;
+    if (ctx->host_kind == LJ_LIST_FULL && l.avalid)  // the gather reads the aligned copy
+      LJ_CUDA(ctx, launch_copy_rows4(l.np.ptr, l.ptr.ptr, l.list.ptr, l.aoff.ptr, n,
+                                     l.alist.ptr, l.aptr.ptr, s), "aligned copy");
   }
   LJ_CUDA(ctx, cudaEventRecord(ctx->ev[1], s), "event");
   Particles part{};

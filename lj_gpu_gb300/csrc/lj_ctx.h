@@ -48,7 +48,14 @@ struct DevList {
   int64_t entries = 0;
   int max_row = 0;
   bool valid = false;
-  Csr csr() const { return Csr{n, entries, np.ptr, ptr.ptr, list.ptr}; }
+  Csr csr() const { return Csr{n, entries, np.ptr, ptr.ptr, list.ptr, 0, 0}; }
+  // copy with 16-byte row starts (rows zero-padded to multiples of 4) for the
+  // vector index loads of the mixed gather; full lists only
+  DevBuf<int32_t> aptr, alist;
+  DevBuf<int64_t> aoff;  // n + 1 row offsets of the copy
+  int64_t aentries = 0;
+  bool avalid = false;
+  Csr acsr() const { return Csr{n, entries, np.ptr, aptr.ptr, alist.ptr, 0, 1}; }
 };
 
 struct MdState;  // lj_md.cu
@@ -107,6 +114,7 @@ struct lj_ctx {
   } tiled;
   // autotuner (lj_autotune_aos): scratch p and the chosen shapes
   ljg::DevBuf<double> tune_p;
+  ljg::DevBuf<unsigned char> tune_flush;  // written between timed tuner calls (> L2)
   struct Tuned {
     int precision, soa, periodic, n;
     int64_t entries_half, entries_full;

@@ -357,11 +357,16 @@ __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const C
 // per step.  Pairs outside the cutoff are masked with a select, not a branch.  The
 // U terms of one step are summed in FP32 and the step sum enters the Kahan
 // accumulator, so compensation costs 12/U operations per pair.
-// Accepts padded rows (C.ptr == nullptr, row i at i * C.stride).
-template <int G, int U, bool PBC, bool SOA, bool ANISO>
+// Accepts padded rows (C.ptr == nullptr, row i at i * C.stride).  VEC
+// (U == 4, rows on 16-byte boundaries and readable to a multiple of 4): lane
+// l of a row takes the 4 consecutive entries base + 4 l .. + 3 with one
+// 16-byte load, which quarters the index-load instructions and the L1
+// wavefronts they cost (a 32-lane scalar index load touches one line per row).
+template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC = false>
 __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const Csr C,
                                                         const int4* __restrict__ qfix,
                                                         const MixedConsts K) {
+  static_assert(!VEC || U == 4, "vector index loads take 4 entries per lane");
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / G;
   const int lane = t & (G - 1);
@@ -384,28 +389,37 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
   ax.init();
   ay.init();
   az.init();
-  int jn[U];
+  // entry of step `base` taken by (lane, u)
+  auto entry = [&](int base, int u) { return VEC ? base + 4 * lane + u : base + lane + u * G; };
+  auto load_idx = [&](int base, int* jn) {
+    if (VEC) {
+      int4 v = make_int4(0, 0, 0, 0);
+      if (entry(base, 0) < cnt)
+        v = __ldg(reinterpret_cast<const int4*>(C.list + k0 + entry(base, 0)));
+      jn[0] = v.x;
+      jn[1] = v.y;
+      jn[2] = v.z;
+      jn[3] = v.w;
+    } else {
 #pragma unroll
-  for (int u = 0; u < U; u++) {
-    const int k = lane + u * G;
-    jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
-  }
+      for (int u = 0; u < U; u++)
+        jn[u] = entry(base, u) < cnt ? __ldg(C.list + k0 + entry(base, u)) : 0;
+    }
+  };
+  int jn[U];
+  load_idx(0, jn);
   for (int base = 0; base < cmax; base += G * U) {
     int jj[U];
     bool ok[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      ok[u] = base + lane + u * G < cnt;
-      jj[u] = jn[u];
+      ok[u] = entry(base, u) < cnt;
+      jj[u] = ok[u] ? jn[u] : 0;
     }
     int4 xj[U];
 #pragma unroll
     for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const int k = base + G * U + lane + u * G;
-      jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
-    }
+    load_idx(base + G * U, jn);
     float sx = 0.f, sy = 0.f, sz = 0.f;
     unsigned border = 0u;
 #pragma unroll
@@ -1067,6 +1081,13 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
         return dispatch_bools(pbc, soa, [&](auto P, auto S) {
           constexpr int G = decltype(g)::value;
           const int4* qf = L.qfix;
+          if (U == 4 && L.csr.aligned4) {
+            if (L.aniso)
+              return launch_dependent(k_gather_mixed_u<G, 4, P.value, S.value, true, true>,
+                                      blocks, block, s, L.part, L.csr, qf, K);
+            return launch_dependent(k_gather_mixed_u<G, 4, P.value, S.value, false, true>, blocks,
+                                    block, s, L.part, L.csr, qf, K);
+          }
           if (L.aniso)
             return launch_dependent(k_gather_mixed_u<G, U, P.value, S.value, true>, blocks,
                                     block, s, L.part, L.csr, qf, K);

@@ -34,6 +34,7 @@ struct Csr {
   const int32_t* ptr;
   const int32_t* list;
   int64_t stride;
+  int aligned4;  // every row starts on a 16-byte boundary and is readable to a multiple of 4
 };
 
 __device__ __forceinline__ int64_t row_start(const Csr& c, int i) {
@@ -157,6 +158,11 @@ cudaError_t launch_sort_rows_into(const int64_t* off, int n, const int32_t* in, 
 // Compact copy of CSR rows: out[off[i] + m] = in[ptr[i] + m], m < np[i].
 cudaError_t launch_compact_rows(const int32_t* np, const int32_t* ptr, const int32_t* in,
                                 const int64_t* off, int n, int32_t* out, cudaStream_t s);
+// 16-byte-aligned copy of a CSR: rows padded with zeros to multiples of 4.
+cudaError_t launch_round4(const int32_t* np, int n, int32_t* out, cudaStream_t s);
+cudaError_t launch_copy_rows4(const int32_t* np, const int32_t* ptr, const int32_t* list,
+                              const int64_t* off, int n, int32_t* out, int32_t* aptr,
+                              cudaStream_t s);
 cudaError_t launch_offsets_to_ptr(const int64_t* off, int n, int32_t* ptr, int32_t* np,
                                   int32_t* max_row, cudaStream_t s,
                                   const int32_t* guard = nullptr);

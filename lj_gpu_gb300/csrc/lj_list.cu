@@ -182,6 +182,27 @@ __global__ void k_offsets_to_ptr(const int64_t* off, int n, int32_t* ptr, int32_
   if ((threadIdx.x & 31) == 0) atomicMax(max_row, m);
 }
 
+// Row lengths rounded up to a multiple of 4 (16-byte row starts).
+__global__ void k_round4(const int32_t* __restrict__ np, int n, int32_t* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = (np[i] + 3) & ~3;
+}
+
+// Copies row i of (np, ptr, list) to out[off[i] ...], zero-filling up to the
+// next multiple of 4; aptr[i] = off[i].
+__global__ void k_copy_rows4(const int32_t* __restrict__ np, const int32_t* __restrict__ ptr,
+                             const int32_t* __restrict__ list, const int64_t* __restrict__ off,
+                             int n, int32_t* __restrict__ out, int32_t* __restrict__ aptr) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nwarps) {
+    const int c = np[i], cp = (c + 3) & ~3;
+    const int64_t a = ptr[i], b = off[i];
+    for (int m = lane; m < cp; m += 32) out[b + m] = m < c ? list[a + m] : 0;
+    if (lane == 0) aptr[i] = (int32_t)b;
+  }
+}
+
 __global__ void k_pairs_count(const int32_t* ip, int64_t npairs, int n, int32_t* cnt,
                               int32_t* err) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npairs;
@@ -321,6 +342,19 @@ cudaError_t launch_sort_rows_into(const int64_t* off, int n, const int32_t* in, 
 cudaError_t launch_compact_rows(const int32_t* np, const int32_t* ptr, const int32_t* in,
                                 const int64_t* off, int n, int32_t* out, cudaStream_t s) {
   if (n > 0) k_compact_rows<<<grid_for((int64_t)n * 32, 256), 256, 0, s>>>(np, ptr, in, off, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_round4(const int32_t* np, int n, int32_t* out, cudaStream_t s) {
+  if (n > 0) k_round4<<<grid_for(n, 256), 256, 0, s>>>(np, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_rows4(const int32_t* np, const int32_t* ptr, const int32_t* list,
+                              const int64_t* off, int n, int32_t* out, int32_t* aptr,
+                              cudaStream_t s) {
+  if (n > 0)
+    k_copy_rows4<<<grid_for((int64_t)n * 32, 256), 256, 0, s>>>(np, ptr, list, off, n, out, aptr);
   return cudaGetLastError();
 }
 

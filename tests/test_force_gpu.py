@@ -382,7 +382,7 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(engine, prec):
         qd = dev(q)
         opts = engine.make_opts(dt=0.005, cl2=9.0, box=box, precision=prec)
         best, ms = ctx.autotune(qd, opts, reps=2)
-        assert ms > 0 and best.method in (1, 2) and best.kernel in (1, 2)
+        assert ms > 0 and best.method in (1, 2) and best.kernel in (1, 2, 3, 4)
         # the tuned shape is used by default-option calls and keeps parity
         for o in (opts, best):
             pd = dev(np.zeros_like(q))
@@ -465,6 +465,61 @@ def test_cell_tiled_gather_on_device_built_lists(engine, name, layout):
             for k, tol in MIXED_TOL.items():
                 assert e[k] <= tol, (kernel, lanes, unroll, k, e)
             outs[(kernel, lanes, unroll)] = got
-        # same pairs: tiled vs unrolled differ only by summation order
+        # same pairs: tiled vs unrolled differ only by FP32 summation order
+        # (a few 1e-6 of the rms force); one pair more or less, even at the
+        # cutoff (df ~ 4e-3), would differ by orders of magnitude more
         a, b = outs[(3, 0, 0)], outs[(2, 4, 4)]
-        assert ol.rel_errors(a, b)["max_rel_rms"] <= 1e-6
+        assert ol.rel_errors(a, b)["max_rel_rms"] <= 5e-6
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+@pytest.mark.parametrize("layout", ["aos", "soa"])
+def test_vector_index_loads_kernel4(engine, name, layout):
+    """Kernel 4 (kernel 2 over the 16-byte-aligned copy of the full list, one
+    16-byte index load per lane and step) meets the mixed bounds and sees the
+    same pairs as kernel 2 (rows of any length, including rows shorter than
+    4 and empty rows of open systems)."""
+    q, box, half = system(name)
+    ref = oracle_p(q, half, box, 1, 0.005)
+    with engine.Context(0) as ctx:
+        outs = {}
+        for kernel, lanes in ((4, 0), (4, 2), (4, 8), (2, 4)):
+            got = run_engine(engine, q, half, box, "mixed", "gather", layout, 1, 0.005,
+                             lanes=lanes, ctx=ctx, kernel=kernel, unroll=4)
+            e = ol.rel_errors(got, ref)
+            for k, tol in MIXED_TOL.items():
+                assert e[k] <= tol, (kernel, lanes, k, e)
+            outs[(kernel, lanes)] = got
+        assert ol.rel_errors(outs[(4, 0)], outs[(2, 4)])["max_rel_rms"] <= 5e-6
+
+
+def test_kernel4_measure_uses_the_uploaded_list(engine, fixture_rho05):
+    """lj_measure_aos re-uploads a host list and refreshes the aligned copy
+    from it inside the timed region; results match the FP64 oracle's bounds."""
+    f = fixture_rho05
+    half = (f["np"], f["ptr"], f["list"])
+    with engine.Context(0) as ctx:
+        ctx.set_list_csr(*half)
+        fnp, fptr, flist = ctx.get_list_csr("full")
+        ctx.set_list_csr(fnp, fptr, flist, kind="full")  # host full list
+        opts = engine.make_opts(dt=0.001, cl2=9.0, precision="mixed", method="gather",
+                                kernel=4, unroll=4)
+        p = np.zeros_like(f["q"])
+        ctx.measure_aos(np.ascontiguousarray(f["q"]), p, opts, calls=1)
+        e = ol.rel_errors(p, ol.force_sorted_aos(f["q"], np.zeros_like(f["q"]), *half,
+                                                 dt=0.001, box=None, calls=1))
+        for k, tol in MIXED_TOL.items():
+            assert e[k] <= tol, (k, e)
+
+
+def test_launch_option_checks(engine, fixture_rho05):
+    f = fixture_rho05
+    with engine.Context(0) as ctx:
+        ctx.set_list_csr(dev(f["np"]), dev(f["ptr"]), dev(f["list"]))
+        qd, pd = dev(f["q"]), dev(np.zeros_like(f["q"]))
+        for kw in (dict(kernel=5), dict(kernel=-1), dict(unroll=-1),
+                   dict(precision="mixed", method="gather", kernel=4, unroll=2)):
+            opts = engine.make_opts(**kw)
+            with pytest.raises(engine.LJError) as e:
+                ctx.force_aos(qd, pd, opts)
+            assert e.value.status == engine.LJ_ERR_INVALID_ARGUMENT, kw
