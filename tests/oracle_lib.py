@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes as C
 import platform
+import re
 import subprocess
 from pathlib import Path
 
@@ -211,3 +212,47 @@ def load_ref(layout="aos") -> C.CDLL:
     L.ref_get_csr.argtypes = [_ip, _ip, _ip]
     L.ref_run.argtypes = [C.c_char_p, C.c_int]
     return L
+
+
+# ---------------------------------------------------------------------------
+# the reference's CUDA kernels (oracle/_ref/refcuda.cubin, built from the
+# reference checkout by `make -C oracle refcuda`) and their loader
+# ---------------------------------------------------------------------------
+REFCUDA_CUBIN = ORACLE_DIR / "_ref" / "refcuda.cubin"
+REFCUDA_LOADER = ORACLE_DIR / "_build" / "librefcuda.so"
+_refcuda = None
+
+
+def refcuda_available() -> bool:
+    return REFCUDA_CUBIN.exists()
+
+
+def load_refcuda():
+    """Loads the cubin into the current CUDA context (call after the CUDA
+    runtime is initialised).  Returns (lib, {(kernel_name, vec): index})."""
+    global _refcuda
+    if _refcuda is not None:
+        return _refcuda
+    build_oracle()
+    L = C.CDLL(str(REFCUDA_LOADER))
+    L.rc_load.argtypes = [C.c_char_p]
+    L.rc_name.restype = C.c_char_p
+    L.rc_name.argtypes = [C.c_int]
+    L.rc_launch.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int32,
+                            C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
+                            C.c_void_p]
+    count = L.rc_load(str(REFCUDA_CUBIN).encode())
+    if count <= 0:
+        raise RuntimeError(f"loading {REFCUDA_CUBIN} failed ({count})")
+    table = {}
+    for k in range(count):
+        name = L.rc_name(k).decode()
+        m = re.match(r"_Z(\d+)", name)  # Itanium mangling: length-prefixed name
+        if not m:
+            continue
+        base = name[m.end():m.end() + int(m.group(1))]
+        rest = name[m.end() + int(m.group(1)):]
+        vec = "double4" if rest.startswith("I7double4") else "double3"
+        table[(base, vec)] = k
+    _refcuda = (L, table)
+    return _refcuda
