@@ -375,17 +375,15 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
   if (fixed) {
     LJ_CUDA(ctx, ctx->qfix.ensure((size_t)n), "alloc");
     L.qfix = ctx->qfix.ptr;
-    double max_abs = 0.0;
     if (!L.box.on) {
+      // the fixed-point frame of an open box follows the largest |coordinate|;
+      // the kernels read it on the device (no host round trip per call)
       LJ_CUDA(ctx, ctx->maxabs.ensure(1), "alloc");
       LJ_CUDA(ctx, launch_max_abs(part, n, ctx->maxabs.ptr, ctx->stream), "max_abs");
-      LJ_CUDA(ctx, cudaMemcpyAsync(&max_abs, ctx->maxabs.ptr, sizeof max_abs,
-                                   cudaMemcpyDeviceToHost, ctx->stream), "max_abs read");
-      LJ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-      if (!std::isfinite(max_abs))
-        return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "non-finite position");
+      make_device_frame(L, reinterpret_cast<const unsigned long long*>(ctx->maxabs.ptr));
+    } else {
+      make_fixed_frame(L, 0.0);
     }
-    make_fixed_frame(L, max_abs);
     if (o->precision == LJ_PREC_MIXED && method == LJ_METHOD_SCATTER_HALF) {
       LJ_CUDA(ctx, ctx->fscratch.ensure(3 * (size_t)n), "alloc");
       L.fscratch = ctx->fscratch.ptr;

@@ -88,6 +88,27 @@ struct FixedAxis {
   int pad;
 };
 
+// Open boxes: exponent k of the fixed-point scale 2^k chosen from the largest
+// |coordinate| (key: its IEEE bits, as k_max_abs leaves them): |x| < 2^e and
+// k = 30 - e keep |X| <= 2^30, so every difference fits in int32.  k is held
+// in [-60, 50] so the FP32 pair constants (which scale by 2^2k) stay finite
+// and normal.  Must equal the host's choice in make_fixed_frame.
+__host__ __device__ __forceinline__ int open_frame_exp(unsigned long long key) {
+  const int be = (int)((key >> 52) & 0x7ffull);
+  const int e = key == 0ull ? 1 : (be == 0 ? -1021 : be - 1022);  // frexp exponent
+  const int k = 30 - e;
+  return k < -60 ? -60 : (k > 50 ? 50 : k);
+}
+
+// The axis of scale 2^k (mult 2^63, sigma 63 - k).
+__host__ __device__ __forceinline__ FixedAxis pow2_axis(int k) {
+  FixedAxis a;
+  a.mult = 1ull << 63;
+  a.sigma = 63 - k;
+  a.pad = 0;
+  return a;
+}
+
 __device__ __forceinline__ int to_fixed(double x, const FixedAxis& ax) {
   const unsigned long long b = (unsigned long long)dbits(x);
   const int e = (int)((b >> 52) & 0x7ffull);

@@ -240,16 +240,35 @@ struct MixedConsts {
   float u_hi[3], u_lo[3];  // per-axis unit split in two floats (anisotropic)
   double fscale[3];      // unit * dt per axis (isotropic) or dt (anisotropic)
   Fp64Consts f64;        // for the rare FP64 cutoff decision
+  const unsigned long long* open_key;  // device-chosen open-box frame, see frame_consts
 };
+
+// Constants of the frame in use.  With an open box whose frame is chosen on
+// the device (scale 2^k from the largest |coordinate|), the host built them
+// for k = 0; every frame-dependent one scales exactly by a power of two.
+__device__ __forceinline__ MixedConsts frame_consts(const MixedConsts& K0) {
+  MixedConsts K = K0;
+  if (K0.open_key) {
+    const int k = open_frame_exp(*K0.open_key);
+    K.cl2_lo = ldexpf(K0.cl2_lo, 2 * k);
+    K.cl2_hi = ldexpf(K0.cl2_hi, 2 * k);
+    K.k_hi = ldexpf(K0.k_hi, 2 * k);
+    K.k_lo = ldexpf(K0.k_lo, 2 * k);
+    for (int d = 0; d < 3; d++) K.fscale[d] = ldexp(K0.fscale[d], -k);
+  }
+  return K;
+}
 
 template <bool SOA>
 __global__ void __launch_bounds__(256) k_fixed_image(const Particles P, int n,
                                                      FixedAxis ax, FixedAxis ay, FixedAxis az,
+                                                     const unsigned long long* open_key,
                                                      int4* __restrict__ out) {
   // the pair kernel that follows may launch now (it waits for this grid)
   asm volatile("griddepcontrol.launch_dependents;");
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (open_key) ax = ay = az = pow2_axis(open_frame_exp(*open_key));
   const double3 q = load_q<SOA>(P, i);
   out[i] = make_int4(to_fixed(q.x, ax), to_fixed(q.y, ay), to_fixed(q.z, az), 0);
 }
@@ -312,7 +331,9 @@ __device__ __forceinline__ float df_mixed(float r2, const MixedConsts& k) {
 template <int G, bool PBC, bool SOA, bool ANISO>
 __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const Csr C,
                                                       const int4* __restrict__ qfix,
-                                                      const MixedConsts K) {
+                                                      const MixedConsts K0) {
+  // a periodic frame is fixed on the host; an open one may come from the device
+  const MixedConsts K = PBC ? K0 : frame_consts(K0);
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / G;
   const int lane = t & (G - 1);
@@ -365,7 +386,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const C
 template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC = false>
 __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const Csr C,
                                                         const int4* __restrict__ qfix,
-                                                        const MixedConsts K) {
+                                                        const MixedConsts K0) {
   static_assert(!VEC || U == 4, "vector index loads take 4 entries per lane");
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / G;
@@ -373,6 +394,8 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
   // Launched as a programmatic dependent of the image pass: nothing the
   // stream wrote before may be read until the preceding grid has finished.
   asm volatile("griddepcontrol.wait;" ::: "memory");
+  // a periodic frame is fixed on the host; an open one may come from the device
+  const MixedConsts K = PBC ? K0 : frame_consts(K0);
   const bool valid = i < C.n;
   int cnt = 0;
   int64_t k0 = 0;
@@ -577,7 +600,9 @@ constexpr int kTiledThreads = 128;
 
 template <int G, int U, bool PBC, bool SOA>
 __global__ void __launch_bounds__(kTiledThreads) k_gather_mixed_tiled(
-    const Particles P, const TiledList T, const int4* __restrict__ cq, const MixedConsts K) {
+    const Particles P, const TiledList T, const int4* __restrict__ cq, const MixedConsts K0) {
+  // a periodic frame is fixed on the host; an open one may come from the device
+  const MixedConsts K = PBC ? K0 : frame_consts(K0);
   extern __shared__ int4 tile[];
   __shared__ int nstart[27], ncount[27];
   __shared__ int nnb, centre;
@@ -684,9 +709,12 @@ template <bool SOA>
 __global__ void __launch_bounds__(256) k_fixed_image_sorted(const Particles P, int n,
                                                             const int32_t* __restrict__ order,
                                                             FixedAxis ax, FixedAxis ay,
-                                                            FixedAxis az, int4* __restrict__ cq) {
+                                                            FixedAxis az,
+                                                            const unsigned long long* open_key,
+                                                            int4* __restrict__ cq) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
+  if (open_key) ax = ay = az = pow2_axis(open_frame_exp(*open_key));
   const double3 q = load_q<SOA>(P, __ldg(order + s));
   cq[s] = make_int4(to_fixed(q.x, ax), to_fixed(q.y, ay), to_fixed(q.z, az), 0);
 }
@@ -715,7 +743,9 @@ __device__ __forceinline__ void fp64_pair_acc(const Particles& P, const double3&
 
 template <bool PBC, bool SOA, bool ANISO>
 __global__ void __launch_bounds__(32 * kCompactWarps) k_gather_fp64_c(
-    const Particles P, const Csr C, const int4* __restrict__ qfix, const MixedConsts K) {
+    const Particles P, const Csr C, const int4* __restrict__ qfix, const MixedConsts K0) {
+  // a periodic frame is fixed on the host; an open one may come from the device
+  const MixedConsts K = PBC ? K0 : frame_consts(K0);
   __shared__ int queue[kCompactWarps][64];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kCompactWarps + w;
@@ -779,7 +809,9 @@ __device__ __forceinline__ void fp64_pair_red(const Particles& P, int i, int j,
 
 template <bool PBC, bool SOA, bool ANISO>
 __global__ void __launch_bounds__(32 * kScatterWarps) k_scatter_fp64_c(
-    const Particles P, const Csr C, const int4* __restrict__ qfix, const MixedConsts K) {
+    const Particles P, const Csr C, const int4* __restrict__ qfix, const MixedConsts K0) {
+  // a periodic frame is fixed on the host; an open one may come from the device
+  const MixedConsts K = PBC ? K0 : frame_consts(K0);
   __shared__ int2 queue[kScatterWarps][64];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r0 = (blockIdx.x * kScatterWarps + w) * 32;
@@ -836,7 +868,9 @@ template <int G, bool PBC, bool SOA, bool ANISO>
 __global__ void __launch_bounds__(256) k_scatter_mixed(const Particles P, const Csr C,
                                                        const int4* __restrict__ qfix,
                                                        float* __restrict__ facc,
-                                                       const MixedConsts K) {
+                                                       const MixedConsts K0) {
+  // a periodic frame is fixed on the host; an open one may come from the device
+  const MixedConsts K = PBC ? K0 : frame_consts(K0);
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / G;
   const int lane = t & (G - 1);
@@ -882,7 +916,8 @@ __global__ void __launch_bounds__(256) k_scatter_mixed(const Particles P, const 
 template <bool SOA>
 __global__ void __launch_bounds__(256) k_kick_from_scratch(const Particles P, int n,
                                                            const float* __restrict__ facc,
-                                                           const MixedConsts K) {
+                                                           const MixedConsts K0) {
+  const MixedConsts K = frame_consts(K0);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   kick_p<SOA>(P, i, widen_f32(facc[3 * (size_t)i]), widen_f32(facc[3 * (size_t)i + 1]),
@@ -926,6 +961,7 @@ MixedConsts make_mixed_consts(const ForceLaunch& L) {
     split_float(L.unit[d], k.u_hi[d], k.u_lo[d]);
     k.fscale[d] = L.aniso ? L.dt : L.unit[d] * L.dt;
   }
+  k.open_key = L.open_key;
   return k;
 }
 
@@ -990,10 +1026,10 @@ void make_fixed_frame(ForceLaunch& L, double max_abs) {
     }
     L.aniso = !(L.box.len[0] == L.box.len[1] && L.box.len[1] == L.box.len[2]);
   } else {
-    // |X| <= 2^30 for every particle keeps |Xj - Xi| < 2^31
-    int e;
-    std::frexp(max_abs > 0 ? max_abs : 1.0, &e);  // max_abs < 2^e
-    const int k = 30 - e;
+    // |X| <= 2^30 for every particle keeps |Xj - Xi| < 2^31 (open_frame_exp)
+    unsigned long long key;
+    std::memcpy(&key, &max_abs, sizeof key);
+    const int k = open_frame_exp(key & 0x7fffffffffffffffull);
     for (int d = 0; d < 3; d++) {
       axis_for(std::ldexp(1.0, k), L.axis[d]);
       L.unit[d] = std::ldexp(1.0, -k);
@@ -1002,16 +1038,21 @@ void make_fixed_frame(ForceLaunch& L, double max_abs) {
   }
 }
 
+void make_device_frame(ForceLaunch& L, const unsigned long long* key) {
+  make_fixed_frame(L, std::ldexp(1.0, 29));  // the k = 0 frame
+  L.open_key = key;
+}
+
 cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s) {
   const int n = L.csr.n;
   if (n == 0) return cudaSuccess;
   const int blocks = (n + 255) / 256;
   if (L.part.soa)
     k_fixed_image<true><<<blocks, 256, 0, s>>>(L.part, n, L.axis[0], L.axis[1], L.axis[2],
-                                              L.qfix);
+                                              L.open_key, L.qfix);
   else
     k_fixed_image<false><<<blocks, 256, 0, s>>>(L.part, n, L.axis[0], L.axis[1], L.axis[2],
-                                               L.qfix);
+                                               L.open_key, L.qfix);
   return cudaGetLastError();
 }
 
@@ -1143,10 +1184,10 @@ cudaError_t launch_fixed_image_sorted(const ForceLaunch& L, const int32_t* order
   const int blocks = (n + 255) / 256;
   if (L.part.soa)
     k_fixed_image_sorted<true><<<blocks, 256, 0, s>>>(L.part, n, order, L.axis[0], L.axis[1],
-                                                      L.axis[2], cq);
+                                                      L.axis[2], L.open_key, cq);
   else
     k_fixed_image_sorted<false><<<blocks, 256, 0, s>>>(L.part, n, order, L.axis[0], L.axis[1],
-                                                       L.axis[2], cq);
+                                                       L.axis[2], L.open_key, cq);
   return cudaGetLastError();
 }
 

@@ -84,11 +84,19 @@ struct ForceLaunch {
   FixedAxis axis[3];
   double unit[3];  // length per fixed unit on each axis
   int aniso;       // axes with different units
+  // Open boxes: device word holding the largest |coordinate| (IEEE bits,
+  // written by launch_max_abs on the same stream).  When set, the kernels
+  // derive the fixed-point frame from it (see open_frame_exp) and the host
+  // frame above is the k = 0 frame they rescale; no host round trip.
+  const unsigned long long* open_key;
 };
 
 // Fills axis[] / unit[] / aniso for a periodic box, or for an open box from
 // the largest coordinate magnitude (max_abs).
 void make_fixed_frame(ForceLaunch& L, double max_abs);
+// Open box with the frame chosen on the device from *key (launch_max_abs):
+// sets L.open_key and the k = 0 host frame the kernels rescale.
+void make_device_frame(ForceLaunch& L, const unsigned long long* key);
 
 // Cell-tiled full list (built with the list, see lj_nlist.cu): particles in
 // cell order (order[s], cells [start[c], start[c+1])), and for every slot s a

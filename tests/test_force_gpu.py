@@ -523,3 +523,25 @@ def test_launch_option_checks(engine, fixture_rho05):
             with pytest.raises(engine.LJError) as e:
                 ctx.force_aos(qd, pd, opts)
             assert e.value.status == engine.LJ_ERR_INVALID_ARGUMENT, kw
+
+
+@pytest.mark.parametrize("kernel", [1, 2, 4])
+def test_open_box_frame_follows_the_coordinates(engine, kernel):
+    """Open boxes take their fixed-point frame from the largest |coordinate|,
+    chosen on the device each call: translating the system (a coarser frame)
+    and back within one context keeps every call within the mixed bounds."""
+    q, box, half = system("open_rho0.5")
+    with engine.Context(0) as ctx:
+        npp, ptr, lst = half
+        ctx.set_list_csr(dev(npp), dev(ptr), dev(lst), kind="half")
+        opts = engine.make_opts(dt=0.001, cl2=9.0, precision="mixed", method="gather",
+                                kernel=kernel, unroll=4 if kernel > 1 else 0)
+        for shift in (0.0, 100.0, 0.0, -37.5):
+            qs = q.copy()
+            qs[:, :3] += shift
+            ref = oracle_p(qs, half, None, 1, 0.001)
+            pd = dev(np.zeros_like(q))
+            ctx.force_aos(dev(qs), pd, opts)
+            e = ol.rel_errors(host(pd), ref)
+            for k, tol in MIXED_TOL.items():
+                assert e[k] <= tol, (shift, k, e)
