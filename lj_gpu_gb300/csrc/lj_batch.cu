@@ -161,6 +161,7 @@ namespace {
 struct SizeClass {
   int first, count;  // range in the class-ordered row list
   int lanes, unroll;
+  bool vec;          // 16-byte index loads (unroll 4; rows are 16-byte aligned)
   double ms;
 };
 
@@ -202,7 +203,7 @@ cudaError_t batch_kick(BatchState& b, const Particles& part, const std::vector<S
   for (const SizeClass& k : cls) {
     cudaError_t e = launch_force_batch(part, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                        b.classrows.ptr + k.first, k.count, dt, cl2, k.lanes,
-                                       k.unroll, s);
+                                       k.unroll, k.vec, s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -299,7 +300,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
   std::vector<SizeClass> cls;
   for (int k = 0; k < 3; k++) {
     if (class_rows[(size_t)k].empty()) continue;
-    cls.push_back({(int)rows_flat.size(), (int)class_rows[(size_t)k].size(), 4, 4, 0.0});
+    cls.push_back({(int)rows_flat.size(), (int)class_rows[(size_t)k].size(), 4, 4, false, 0.0});
     rows_flat.insert(rows_flat.end(), class_rows[(size_t)k].begin(), class_rows[(size_t)k].end());
   }
   b.n = n_total;
@@ -365,18 +366,20 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     cudaEvent_t e0, e1;
     B_CUDA(ctx, cudaEventCreate(&e0), "event");
     B_CUDA(ctx, cudaEventCreate(&e1), "event");
-    const int shapes[][2] = {{2, 4}, {4, 2}, {4, 4}, {8, 2}, {8, 4}};
+    // lanes, entries in flight, 16-byte index loads
+    const int shapes[][3] = {{2, 4, 0}, {4, 2, 0}, {4, 4, 0}, {8, 2, 0}, {8, 4, 0},
+                             {2, 4, 1}, {4, 4, 1}, {8, 4, 1}};
     for (SizeClass& k : cls) {
       k.ms = 1e300;
       for (const auto& sh : shapes) {
         cudaError_t e = launch_force_batch(tp, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                            b.classrows.ptr + k.first, k.count, prm->dt, cl2,
-                                           sh[0], sh[1], s);
+                                           sh[0], sh[1], sh[2] != 0, s);
         cudaEventRecord(e0, s);
         for (int rep = 0; rep < 3 && e == cudaSuccess; rep++)
           e = launch_force_batch(tp, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                  b.classrows.ptr + k.first, k.count, prm->dt, cl2, sh[0], sh[1],
-                                 s);
+                                 sh[2] != 0, s);
         cudaEventRecord(e1, s);
         if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
           cudaEventDestroy(e0);
@@ -389,6 +392,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
           k.ms = ms / 3;
           k.lanes = sh[0];
           k.unroll = sh[1];
+          k.vec = sh[2] != 0;
         }
       }
     }

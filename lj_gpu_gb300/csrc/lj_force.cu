@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
 // Batched mixed gather: as k_gather_mixed_u, with every constant that depends
 // on the box (unit, cutoff in fixed units, FP64 image shift) read per row
 // from the row's replica.  Groups walk the row list of one size class.
-template <int G, int U>
+template <int G, int U, bool VEC>
 __global__ void __launch_bounds__(256) k_gather_mixed_batch(
     const Particles P, const Csr C, const int4* __restrict__ qfix, const int32_t* __restrict__ rid,
     const ReplicaInfo* __restrict__ reps, const int32_t* __restrict__ rows, int nrows, double dt,
@@ -525,28 +525,38 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
   ax.init();
   ay.init();
   az.init();
-  int jn[U];
+  static_assert(!VEC || U == 4, "vector index loads take 4 entries per lane");
+  // entry of step `base` taken by (lane, u); VEC as in k_gather_mixed_u
+  auto entry = [&](int base, int u) { return VEC ? base + 4 * lane + u : base + lane + u * G; };
+  auto load_idx = [&](int base, int* jn) {
+    if (VEC) {
+      int4 v = make_int4(0, 0, 0, 0);
+      if (entry(base, 0) < cnt)
+        v = __ldg(reinterpret_cast<const int4*>(C.list + k0 + entry(base, 0)));
+      jn[0] = v.x;
+      jn[1] = v.y;
+      jn[2] = v.z;
+      jn[3] = v.w;
+    } else {
 #pragma unroll
-  for (int u = 0; u < U; u++) {
-    const int k = lane + u * G;
-    jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
-  }
+      for (int u = 0; u < U; u++)
+        jn[u] = entry(base, u) < cnt ? __ldg(C.list + k0 + entry(base, u)) : 0;
+    }
+  };
+  int jn[U];
+  load_idx(0, jn);
   for (int base = 0; base < cmax; base += G * U) {
     int jj[U];
     bool ok[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      ok[u] = base + lane + u * G < cnt;
-      jj[u] = jn[u];
+      ok[u] = entry(base, u) < cnt;
+      jj[u] = ok[u] ? jn[u] : 0;
     }
     int4 xj[U];
 #pragma unroll
     for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const int k = base + G * U + lane + u * G;
-      jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
-    }
+    load_idx(base + G * U, jn);
     float sx = 0.f, sy = 0.f, sz = 0.f;
     unsigned border = 0u;
 #pragma unroll
@@ -1224,7 +1234,8 @@ cudaError_t launch_force_tiled(const ForceLaunch& L, const TiledList& T, const i
 cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* qfix,
                                const int32_t* rid, const ReplicaInfo* reps,
                                const int32_t* rows, int nrows, double dt, double cl2, int lanes,
-                               int unroll, cudaStream_t s) {
+                               int unroll, bool vec, cudaStream_t s) {
+  if (vec && (unroll != 4 || c.ptr || c.stride % 4 != 0)) return cudaErrorInvalidValue;
   if (nrows <= 0) return cudaSuccess;
   long long cl2_bits;
   std::memcpy(&cl2_bits, &cl2, sizeof cl2_bits);
@@ -1234,8 +1245,12 @@ cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* 
     constexpr int U = decltype(u)::value;
     return dispatch_lanes(lanes, [&](auto g) {
       constexpr int G = decltype(g)::value;
-      k_gather_mixed_batch<G, U>
-          <<<blocks, block, 0, s>>>(part, c, qfix, rid, reps, rows, nrows, dt, cl2_bits);
+      if (U == 4 && vec)
+        k_gather_mixed_batch<G, 4, true>
+            <<<blocks, block, 0, s>>>(part, c, qfix, rid, reps, rows, nrows, dt, cl2_bits);
+      else
+        k_gather_mixed_batch<G, U, false>
+            <<<blocks, block, 0, s>>>(part, c, qfix, rid, reps, rows, nrows, dt, cl2_bits);
       return cudaGetLastError();
     });
   };

@@ -127,7 +127,7 @@ cudaError_t launch_force_tiled(const ForceLaunch& L, const TiledList& T, const i
 cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* qfix,
                                const int32_t* rid, const ReplicaInfo* reps,
                                const int32_t* rows, int nrows, double dt, double cl2, int lanes,
-                               int unroll, cudaStream_t s);
+                               int unroll, bool vec, cudaStream_t s);
 
 // Launchers (return cudaError_t of the launch)
 cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s);
