@@ -1,7 +1,8 @@
 // lj_md.cu -- velocity-Verlet molecular dynamics around the force path.
 //
 // The reference never integrates (its 100 "steps" re-kick p from a fixed q,
-// cpu_ref/force_aos.cpp:592-601); this loop is the benchmark spec's extension.
+// cpu_ref/force_aos.cpp:592-601); this loop extends the path with the
+// integrator and on-device list rebuilds an MD code needs around it.
 //
 // One step (m = 1, force routine = kick p += F dt):
 //   drift   q += p dt, wrap into [0, L), fixed-point image of q, and the
