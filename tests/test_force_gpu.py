@@ -545,3 +545,41 @@ def test_open_box_frame_follows_the_coordinates(engine, kernel):
             e = ol.rel_errors(host(pd), ref)
             for k, tol in MIXED_TOL.items():
                 assert e[k] <= tol, (shift, k, e)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_systems_every_path(engine, seed):
+    """Random systems: a jittered FCC lattice of random size and density with
+    a random subset of sites removed (particle counts that are not multiples
+    of 4, a warp or a block) in a random particle order, open or periodic,
+    rows sorted or shuffled (random_shfl): every FP64 path within 1e-12 of
+    the oracle, every mixed path within its bounds, and the device-built list
+    equal to the oracle's."""
+    rng = np.random.default_rng(1000 + seed)
+    ncell = int(rng.integers(3, 8))
+    rho = float(rng.uniform(0.4, 1.0))
+    q0, L = ol.init_fcc_periodic(ncell, rho, 0.2, seed=77 + seed)
+    keep = rng.permutation(q0.shape[0])[: int(q0.shape[0] * rng.uniform(0.6, 0.97))]
+    q = np.ascontiguousarray(q0[keep])
+    periodic = bool(seed % 2) and L > 2 * 3.3
+    box = L if periodic else None
+    half = ol.build_list(q, 3.3, box=box)
+    if seed % 3 == 0:  # shuffled rows, as the reference's random_shfl leaves them
+        engine.shuffle_rows(*half, seed=10)
+    ref = oracle_p(q, half, box, 1, 0.005)
+    with engine.Context(0) as ctx:
+        for method, kernel in (("scatter", 1), ("scatter", 2), ("gather", 1), ("gather", 2)):
+            got = run_engine(engine, q, half, box, "fp64", method, "aos", 1, 0.005, ctx=ctx,
+                             kernel=kernel)
+            assert ol.rel_errors(got, ref)["max_rel"] <= FP64_TOL, (seed, method, kernel)
+        for method, kernel, unroll in (("gather", 1, 0), ("gather", 2, 4), ("gather", 4, 4),
+                                       ("scatter", 1, 0)):
+            got = run_engine(engine, q, half, box, "mixed", method, "soa" if seed % 2 else "aos",
+                             1, 0.005, ctx=ctx, kernel=kernel, unroll=unroll)
+            e = ol.rel_errors(got, ref)
+            for k, tol in MIXED_TOL.items():
+                assert e[k] <= tol, (seed, method, kernel, k, e)
+        ctx.build_list(dev(q), 3.3, box=box)
+        np_d, ptr_d, lst_d = ctx.get_list_csr("half")
+        np_r, ptr_r, lst_r = ol.build_list(q, 3.3, box=box)
+        assert np.array_equal(np_d, np_r) and np.array_equal(lst_d, lst_r), seed
