@@ -351,9 +351,15 @@ def run_ours(args, dist, density=DENSITY):
     hbm, peak_kind = peaks()
     alg = pair_kernel_bytes(method, layout, P, N)
     achieved = alg / (t_pair_ms * 1e-3) / 1e9
-    traffic = profiled_traffic("force_mixed_gather_aos_108k_rho0.5.txt")
+    # DRAM traffic per launch from the committed ncu capture of this kernel on
+    # this workload (the AoS headline at rho 0.5); other workloads have none
+    prof = "force_mixed_gather_aos_108k_rho0.5.txt"
+    matches = density == DENSITY and layout == "aos"
+    traffic = profiled_traffic(prof) if matches else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                "frac": achieved / hbm, "traffic": traffic,
+                "traffic_source": f"profiles/{prof}" if traffic else None,
+                "peak_kind": peak_kind,
                 "kernel": f"pair kernel of {best_mixed}, shape {tuned['mixed']}",
                 "algorithmic_bytes_per_launch": alg,
                 "kernel_ms": t_pair_ms, "position_image_ms": t_image_ms,
@@ -427,6 +433,15 @@ def force_errors(torch, lj, L, qd, rs=RS):
                                                                      torch.linalg.norm(r))}
 
 
+def md_step_bytes(P, N, rebuilds_per_step, mixed=True):
+    """Algorithmic HBM bytes of one MD step: the force call (gather over the
+    full list 8 P + 104 N, or scatter over the half list 4 P + 104 N), the
+    drift (q read + write, p read, image write, reference image read: 112 N)
+    and the list rows written by rebuilds, amortised (4 B per entry)."""
+    entries = 2 * P if mixed else P
+    return 4 * entries + 104 * N + 112 * N + 4 * entries * rebuilds_per_step
+
+
 def run_precision(args, dist):
     """1,000,188 particles (FCC 63^3 x 4), rho = 1, rc 3.0, skin 0.3, MB momenta
     at T* = 1, 1,000 mixed velocity-Verlet steps at dt = 0.005."""
@@ -452,10 +467,17 @@ def run_precision(args, dist):
         errors.append(dict(step=100 * (seg + 1), **force_errors(torch, lj, L, qd)))
     e0 = records[0][1] + records[0][2]
     drift = max(abs(r[1] + r[2] - e0) for r in records) / abs(e0)
+    ctx.build_list(qd, RS, box=L, kinds=("half",))
+    P = ctx.list_info("half")[1]
     ctx.close()
+    hbm, _ = peaks()
+    sb = md_step_bytes(P, N, rebuilds / 1000)
     return {"metric": "mixed-precision MD force error vs FP64 and energy drift",
             "workload": "precision_1m", "N": N, "box": L, "steps": 1000, "dt": DT,
-            "ms_per_step": ms / 1000, "rebuilds": rebuilds,
+            "ms_per_step": ms / 1000, "rebuilds": rebuilds, "pairs_half": P,
+            "gpairs": P / (ms / 1000 * 1e-3) / 1e9,
+            "hbm_gbs": sb / (ms / 1000 * 1e-3) / 1e9,
+            "hbm_frac": sb / (ms / 1000 * 1e-3) / 1e9 / hbm,
             "max_rel_rms_force_error": max(e["max_rel_rms"] for e in errors),
             "global_rel_force_error": max(e["global_rel"] for e in errors),
             "force_errors": errors, "energy_drift_rel": drift,
@@ -492,11 +514,7 @@ def run_large(args, dist):
         _, P, _ = ctx.list_info("half")
         ctx.close()
         ms = st["ms_total"] / steps
-        # per step: force call (gather 8P + 104N, scatter 4P + 104N), drift
-        # (q r/w, p read, image write, reference image read: 112N), rebuild
-        # list write amortised over 20 steps
-        fbytes = (8 * P if prec == "mixed" else 4 * P) + 104 * N
-        step_bytes = fbytes + 112 * N + (8 * P if prec == "mixed" else 4 * P) / 20
+        step_bytes = md_step_bytes(P, N, 1 / 20, mixed=prec == "mixed")
         out[prec] = {"ms_per_step": ms, "ns_per_step_per_particle": ms * 1e6 / N,
                      "gpairs": P / (ms * 1e-3) / 1e9, "hbm_gbs": step_bytes / (ms * 1e-3) / 1e9,
                      "hbm_frac": step_bytes / (ms * 1e-3) / 1e9 / hbm,
@@ -549,10 +567,13 @@ def run_batch(args, dist):
     e0 = en[0, :, 0] + en[0, :, 1]
     e1 = en[-1, :, 0] + en[-1, :, 1]
     ms = st["ms_total"] / steps
+    hbm, _ = peaks()
+    sb = md_step_bytes(pairs, q.shape[0], st["rebuilds"] / max(steps, 1))
     return {"metric": "batched MD G pair-interactions/s (mixed)", "workload": "batch_512",
             "replicas": 512, "N_total": int(q.shape[0]), "N_min": int(min(np.diff(offs))),
             "N_max": int(max(np.diff(offs))), "steps": steps, "ms_per_step": ms,
             "gpairs": pairs / (ms * 1e-3) / 1e9, "pairs_half_within_list_radius": int(pairs),
+            "hbm_gbs": sb / (ms * 1e-3) / 1e9, "hbm_frac": sb / (ms * 1e-3) / 1e9 / hbm,
             "rebuilds": st["rebuilds"],
             "size_classes": [{"rows": int(s[0]), "lanes": int(s[1]), "entries_in_flight": int(s[2])}
                              for s in shapes if s[0] > 0],
