@@ -118,8 +118,8 @@ int default_lanes(int precision, int method, int kernel, int64_t entries, int n)
 }
 
 int default_kernel(int precision, int method) {
-  if (precision == LJ_PREC_MIXED) return method == LJ_METHOD_GATHER_FULL ? 2 : 1;
-  return 2;
+  (void)method;
+  return 2;  // unrolled gather / vector-atomic scatter (mixed), compacted (FP64)
 }
 
 int copy_in(lj_ctx* ctx, int32_t* dst, const int32_t* src, size_t count, int where) {
@@ -352,9 +352,8 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
   if (L.kernel == 4 && !(o->precision == LJ_PREC_MIXED && method == LJ_METHOD_GATHER_FULL &&
                          ctx->full.avalid && ctx->full.n == n))
     L.kernel = 2;  // no aligned copy: scalar index loads
-  // the mixed path has no compacted scatter (FP32 atomics lose to the gather)
-  if (L.kernel == 2 && method == LJ_METHOD_SCATTER_HALF && o->precision == LJ_PREC_MIXED)
-    L.kernel = 1;
+  // the mixed scatter has kernels 1 (simple) and 2 (unrolled, vector atomics)
+  if (L.kernel > 2 && method == LJ_METHOD_SCATTER_HALF) L.kernel = 2;
   L.unroll = o->unroll ? o->unroll : 4;
   if (L.kernel == 4 && L.unroll != 4)
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kernel 4 takes 4 entries per lane (unroll 0 or 4)");
@@ -385,7 +384,7 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
       make_fixed_frame(L, 0.0);
     }
     if (o->precision == LJ_PREC_MIXED && method == LJ_METHOD_SCATTER_HALF) {
-      LJ_CUDA(ctx, ctx->fscratch.ensure(3 * (size_t)n), "alloc");
+      LJ_CUDA(ctx, ctx->fscratch.ensure(4 * (size_t)n), "alloc");
       L.fscratch = ctx->fscratch.ptr;
     }
     if (L.kernel == 3 && L.aniso) L.kernel = 2;
@@ -1107,6 +1106,9 @@ int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts
     }
     if (try_scatter) {
       if (!mixed && block == 128) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, 0, 0, 128});
+      if (mixed)
+        for (int g : {2, 4, 8})
+          for (int u : {2, 4}) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, g, u, block});
       for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_SCATTER_HALF, 1, g, 0, block});
     }
   }

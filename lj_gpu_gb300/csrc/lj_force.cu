@@ -906,9 +906,9 @@ __global__ void __launch_bounds__(256) k_scatter_mixed(const Particles P, const 
     ax.add(fx);
     ay.add(fy);
     az.add(fz);
-    atomicAdd(facc + 3 * (size_t)j + 0, -fx);
-    atomicAdd(facc + 3 * (size_t)j + 1, -fy);
-    atomicAdd(facc + 3 * (size_t)j + 2, -fz);
+    atomicAdd(facc + 4 * (size_t)j + 0, -fx);
+    atomicAdd(facc + 4 * (size_t)j + 1, -fy);
+    atomicAdd(facc + 4 * (size_t)j + 2, -fz);
   }
   float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
   if (G > 1) {
@@ -917,10 +917,95 @@ __global__ void __launch_bounds__(256) k_scatter_mixed(const Particles P, const 
     group_reduce_comp<G>(hz, lz);
   }
   if (valid && lane == 0) {
-    atomicAdd(facc + 3 * (size_t)i + 0, hx + lx);
-    atomicAdd(facc + 3 * (size_t)i + 1, hy + ly);
-    atomicAdd(facc + 3 * (size_t)i + 2, hz + lz);
+    atomicAdd(facc + 4 * (size_t)i + 0, hx + lx);
+    atomicAdd(facc + 4 * (size_t)i + 1, hy + ly);
+    atomicAdd(facc + 4 * (size_t)i + 2, hz + lz);
   }
+}
+
+// Unrolled mixed scatter over the half list (mixed kernel 2): the traversal
+// of k_gather_mixed_u (G lanes per row, U entries in flight, next indices
+// prefetched, FP32 step sums into a Kahan accumulator for i), each pair's
+// reaction on j added with one 16-byte vector atomic (float4 RED), so a pair
+// costs one position gather and one atomic -- half the gathers of the full
+// gather.  j-side sums are plain FP32 and their order varies run to run.
+template <int G, int U, bool PBC, bool SOA, bool ANISO>
+__global__ void __launch_bounds__(256) k_scatter_mixed_u(const Particles P, const Csr C,
+                                                         const int4* __restrict__ qfix,
+                                                         float4* __restrict__ facc,
+                                                         const MixedConsts K0) {
+  const MixedConsts K = PBC ? K0 : frame_consts(K0);
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / G;
+  const int lane = t & (G - 1);
+  const bool valid = i < C.n;
+  int cnt = 0;
+  int64_t k0 = 0;
+  int4 xi = make_int4(0, 0, 0, 0);
+  if (valid) {
+    cnt = __ldg(C.np + i);
+    k0 = row_start(C, i);
+    xi = __ldg(qfix + i);
+  }
+  int cmax = cnt;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
+  KahanF ax, ay, az;
+  ax.init();
+  ay.init();
+  az.init();
+  int jn[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int k = lane + u * G;
+    jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
+  }
+  for (int base = 0; base < cmax; base += G * U) {
+    int jj[U];
+    bool ok[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      ok[u] = base + lane + u * G < cnt;
+      jj[u] = ok[u] ? jn[u] : 0;
+    }
+    int4 xj[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = base + G * U + lane + u * G;
+      jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
+    }
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
+      const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+      bool in = ok[u] && r2 <= K.cl2_lo;
+      if (ok[u] && r2 > K.cl2_lo && r2 <= K.cl2_hi) {  // rare: decided in FP64
+        const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, jj[u]), K.f64);
+        in = !beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits);
+      }
+      if (in) {
+        const float df = df_mixed<ANISO>(r2, K);
+        const float fx = df * d.x, fy = df * d.y, fz = df * d.z;
+        sx += fx;
+        sy += fy;
+        sz += fz;
+        atomicAdd(facc + jj[u], make_float4(-fx, -fy, -fz, 0.f));
+      }
+    }
+    ax.add(sx);
+    ay.add(sy);
+    az.add(sz);
+  }
+  float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
+  if (G > 1) {
+    group_reduce_comp<G>(hx, lx);
+    group_reduce_comp<G>(hy, ly);
+    group_reduce_comp<G>(hz, lz);
+  }
+  if (valid && lane == 0) atomicAdd(facc + i, make_float4(hx + lx, hy + ly, hz + lz, 0.f));
 }
 
 template <bool SOA>
@@ -930,8 +1015,8 @@ __global__ void __launch_bounds__(256) k_kick_from_scratch(const Particles P, in
   const MixedConsts K = frame_consts(K0);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  kick_p<SOA>(P, i, widen_f32(facc[3 * (size_t)i]), widen_f32(facc[3 * (size_t)i + 1]),
-              widen_f32(facc[3 * (size_t)i + 2]), K.fscale);
+  kick_p<SOA>(P, i, widen_f32(facc[4 * (size_t)i]), widen_f32(facc[4 * (size_t)i + 1]),
+              widen_f32(facc[4 * (size_t)i + 2]), K.fscale);
 }
 
 // ---------------------------------------------------------------------------
@@ -1156,8 +1241,39 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
     }
   }
   if (!gather) {
-    cudaError_t e = cudaMemsetAsync(L.fscratch, 0, sizeof(float) * 3 * (size_t)n, s);
+    cudaError_t e = cudaMemsetAsync(L.fscratch, 0, sizeof(float) * 4 * (size_t)n, s);
     if (e != cudaSuccess) return e;
+  }
+  if (!gather && L.kernel == 2) {
+    auto launch_su = [&](auto u) -> cudaError_t {
+      constexpr int U = decltype(u)::value;
+      return dispatch_lanes(L.lanes, [&](auto g) {
+        return dispatch_bools(pbc, soa, [&](auto P, auto S) {
+          constexpr int G = decltype(g)::value;
+          float4* fa = reinterpret_cast<float4*>(L.fscratch);
+          if (L.aniso)
+            k_scatter_mixed_u<G, U, P.value, S.value, true>
+                <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, fa, K);
+          else
+            k_scatter_mixed_u<G, U, P.value, S.value, false>
+                <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, fa, K);
+          return cudaGetLastError();
+        });
+      });
+    };
+    cudaError_t e;
+    switch (L.unroll) {
+      case 1: e = launch_su(std::integral_constant<int, 1>{}); break;
+      case 2: e = launch_su(std::integral_constant<int, 2>{}); break;
+      case 4: e = launch_su(std::integral_constant<int, 4>{}); break;
+      case 8: e = launch_su(std::integral_constant<int, 8>{}); break;
+      default: return cudaErrorInvalidValue;
+    }
+    if (e != cudaSuccess) return e;
+    const int kb = (n + 255) / 256;
+    if (soa) k_kick_from_scratch<true><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
+    else k_kick_from_scratch<false><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
+    return cudaGetLastError();
   }
   cudaError_t e = dispatch_lanes(L.lanes, [&](auto g) {
     return dispatch_bools(pbc, soa, [&](auto P, auto S) {

@@ -80,7 +80,7 @@ struct ForceLaunch {
   int unroll;      // entries in flight per lane (kernel 2, mixed)
   // mixed precision only
   int4* qfix;      // n entries, written by the fixed-image pass
-  float* fscratch; // 3 n floats (scatter-half mixed only)
+  float* fscratch; // 4 n floats, one float4 per particle (scatter-half mixed only)
   FixedAxis axis[3];
   double unit[3];  // length per fixed unit on each axis
   int aniso;       // axes with different units
