@@ -199,7 +199,7 @@ cudaError_t batch_rebuild(BatchState& b, const double* q, double sl2, cudaStream
 
 cudaError_t batch_kick(BatchState& b, const Particles& part, const std::vector<SizeClass>& cls,
                        double dt, double cl2, cudaStream_t s) {
-  const Csr c{b.n, 0, b.cnt.ptr, nullptr, b.rows.ptr, (int64_t)b.maxrow};
+  const Csr c{b.n, 0, b.cnt.ptr, nullptr, b.rows.ptr, (int64_t)b.maxrow, 1};
   for (const SizeClass& k : cls) {
     cudaError_t e = launch_force_batch(part, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                        b.classrows.ptr + k.first, k.count, dt, cl2, k.lanes,
@@ -362,7 +362,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
   {
     Particles tp = part;
     tp.p = b.ptmp.ptr;
-    const Csr c{b.n, 0, b.cnt.ptr, nullptr, b.rows.ptr, (int64_t)b.maxrow};
+    const Csr c{b.n, 0, b.cnt.ptr, nullptr, b.rows.ptr, (int64_t)b.maxrow, 1};
     cudaEvent_t e0, e1;
     B_CUDA(ctx, cudaEventCreate(&e0), "event");
     B_CUDA(ctx, cudaEventCreate(&e1), "event");
@@ -422,7 +422,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
   auto record = [&](int64_t stepno) -> int {
     if (!energies || nrec >= max_records) return LJ_OK;
     B_CUDA(ctx, cudaMemsetAsync(b.energy.ptr, 0, 2 * sizeof(double) * R, s), "memset");
-    const Csr c{b.n, 0, b.cnt.ptr, nullptr, b.rows.ptr, (int64_t)b.maxrow};
+    const Csr c{b.n, 0, b.cnt.ptr, nullptr, b.rows.ptr, (int64_t)b.maxrow, 1};
     k_batch_energy<<<gridn(n_total, 256), 256, 0, s>>>(q, p, b.qfix.ptr, c, b.rid.ptr, b.reps.ptr,
                                                       cl2, b.energy.ptr);
     B_CUDA(ctx, cudaGetLastError(), "energy");

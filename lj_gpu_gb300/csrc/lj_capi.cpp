@@ -117,10 +117,6 @@ int default_lanes(int precision, int method, int kernel, int64_t entries, int n)
   return 16;
 }
 
-int default_kernel(int precision, int method) {
-  (void)method;
-  return 2;  // unrolled gather / vector-atomic scatter (mixed), compacted (FP64)
-}
 
 int copy_in(lj_ctx* ctx, int32_t* dst, const int32_t* src, size_t count, int where) {
   if (count == 0) return LJ_OK;
@@ -347,7 +343,7 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
                         method == LJ_METHOD_GATHER_FULL && ctx->full.n == n;
   // The cell-tiled gather (kernel 3) runs only when asked for or chosen by
   // lj_autotune_aos; it needs the tiled rows lj_list_build leaves behind.
-  L.kernel = o->kernel ? o->kernel : default_kernel(o->precision, method);
+  L.kernel = o->kernel ? o->kernel : 2;  // unrolled gather / scatter (mixed), compacted (FP64)
   if (L.kernel == 3 && !tiled_ok) L.kernel = 2;  // no tiled list: unrolled gather
   if (L.kernel == 4 && !(o->precision == LJ_PREC_MIXED && method == LJ_METHOD_GATHER_FULL &&
                          ctx->full.avalid && ctx->full.n == n))
@@ -825,7 +821,7 @@ int lj_force_csr_fp64_aos(const double* q, double* p, int32_t n, double dt, doub
   L.part.soa = 0;
   L.part.q = q;
   L.part.p = p;
-  L.csr = Csr{n, 0, np, ptr, list};
+  L.csr = Csr{n, 0, np, ptr, list, 0, 0};
   if (box) {
     L.box.on = 1;
     for (int d = 0; d < 3; d++) {

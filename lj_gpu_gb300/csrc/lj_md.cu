@@ -339,7 +339,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   // mixed: padded rows read in place (64-bit row starts i * maxrow); FP64:
   // compacted rows with int32 offsets
   K.csr = mixed ? Csr{n, m.cap, m.cnt.ptr, nullptr, m.rows.ptr, (int64_t)m.maxrow, 1}
-                : Csr{n, m.cap, m.cnt.ptr, m.ptr.ptr, m.list.ptr, 0};
+                : Csr{n, m.cap, m.cnt.ptr, m.ptr.ptr, m.list.ptr, 0, 0};
   K.box.on = 1;
   for (int d = 0; d < 3; d++) {
     K.box.len[d] = prm->box[d];

@@ -81,7 +81,7 @@ extern "C" int lj_force_mixed_noalloc_aos(const double* q, double* p, int32_t n,
   L.part.soa = 0;
   L.part.q = q;
   L.part.p = p;
-  L.csr = Csr{n, 0, number_of_partners, pointer, sorted_list};
+  L.csr = Csr{n, 0, number_of_partners, pointer, sorted_list, 0, 0};
   if (box) {
     L.box.on = 1;
     for (int d = 0; d < 3; d++) {
