@@ -218,7 +218,7 @@ int install_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ptr,
   if ((rc = copy_in(ctx, ctx->tmp_i32a.ptr, ptr, (size_t)n, where))) return rc;
   if ((rc = copy_in(ctx, ctx->tmp_i32b.ptr, list, (size_t)entries, where))) return rc;
   // validation runs on the caller's layout, as check_loadedpair does
-  const Csr raw{n, entries, l.np.ptr, ctx->tmp_i32a.ptr, ctx->tmp_i32b.ptr};
+  const Csr raw{n, entries, l.np.ptr, ctx->tmp_i32a.ptr, ctx->tmp_i32b.ptr, 0, 0};
   {
     LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
     const int32_t init[2] = {0, 0x7fffffff};
