@@ -325,7 +325,7 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
   if (rc) return rc;
   lj_force_opts tuned_opts;
   const lj_force_opts* o = apply_tuned(ctx, o_in, part.soa, &tuned_opts);
-  int method;
+  int method = LJ_METHOD_GATHER_FULL;
   if ((rc = resolve_method(ctx, o, &method))) return rc;
   const DevList& l = method == LJ_METHOD_SCATTER_HALF ? ctx->half : ctx->full;
   if (n != l.n)
