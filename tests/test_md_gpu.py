@@ -106,3 +106,45 @@ def test_md_list_overflow_is_reported(engine):
         with pytest.raises(engine.LJError) as e:
             ctx.md_run(qd, pd, prm, 5)
         assert e.value.status == engine.LJ_ERR_LIST_OVERFLOW
+
+
+def _oracle_vv_box(q, p, box, rc, dt, steps):
+    q, p = q.copy(), p.copy()
+    O = ol.oracle()
+    b = np.ascontiguousarray(box, np.float64)
+    for _ in range(steps):
+        half = ol.build_list(q, rc + 0.2, box=b)
+        ol.force_sorted_aos(q, p, *half, cl2=rc * rc, dt=0.5 * dt, box=b)
+        O.lj_or_drift(q, p, q.shape[0], dt, b.ctypes.data)
+        half = ol.build_list(q, rc + 0.2, box=b)
+        ol.force_sorted_aos(q, p, *half, cl2=rc * rc, dt=0.5 * dt, box=b)
+    return q, p
+
+
+def test_md_in_a_non_cubic_box(engine):
+    """An orthorhombic box (per-axis fixed-point frame in the drift, the list
+    build and the force kernels): FP64 against the oracle's integrator, mixed
+    against FP64."""
+    q, L = ol.init_fcc_periodic(5, 0.8, 0.05, seed=31)
+    stretch = np.array([1.25, 1.0, 0.9])
+    q[:, :3] *= stretch
+    box = L * stretch
+    p = engine.init_momenta(q.shape[0], 1.0, seed=5)
+    rc, skin, dt, steps = 2.5, 0.3, 0.005, 40
+    out = {}
+    for prec in ("fp64", "mixed"):
+        qd, pd = _dev(q), _dev(p)
+        prm = engine.make_md_params(dt, rc, skin, box, precision=prec, record_every=steps)
+        with engine.Context(0) as ctx:
+            ctx.md_run(qd, pd, prm, steps)
+        import torch
+        torch.cuda.synchronize()
+        out[prec] = (qd.cpu().numpy(), pd.cpu().numpy())
+    qo, po = _oracle_vv_box(q, p, box, rc, dt, steps)
+    d = out["fp64"][0][:, :3] - qo[:, :3]
+    d -= box * np.round(d / box)
+    assert np.abs(d).max() < 1e-11
+    assert ol.rel_errors(out["fp64"][1], po)["max_rel_rms"] < 1e-10
+    d = out["mixed"][0][:, :3] - out["fp64"][0][:, :3]
+    d -= box * np.round(d / box)
+    assert np.abs(d).max() < 1e-5
