@@ -1101,7 +1101,8 @@ int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts
       }
     }
     if (try_scatter) {
-      if (!mixed && block == 128) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, 0, 0, 128});
+      if (!mixed && block == 128)
+        for (int g : {1, 2, 4, 8}) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, g, 0, 128});
       if (mixed)
         for (int g : {2, 4, 8})
           for (int u : {2, 4}) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, g, u, block});

@@ -817,16 +817,20 @@ __device__ __forceinline__ void fp64_pair_red(const Particles& P, int i, int j,
   red_p<SOA>(P, j, flip_sign(fx), flip_sign(fy), flip_sign(fz));
 }
 
-template <bool PBC, bool SOA, bool ANISO>
+// R rows per warp (32, 16, 8 or 4): fewer rows per warp give more warps,
+// which the FP64 pipe needs for latency hiding on lists of ~1e5 rows, but a
+// larger share of partly filled last batches.
+template <bool PBC, bool SOA, bool ANISO, int R = 32>
 __global__ void __launch_bounds__(32 * kScatterWarps) k_scatter_fp64_c(
     const Particles P, const Csr C, const int4* __restrict__ qfix, const MixedConsts K0) {
+  static_assert(R == 4 || R == 8 || R == 16 || R == 32, "rows per warp");
   // a periodic frame is fixed on the host; an open one may come from the device
   const MixedConsts K = PBC ? K0 : frame_consts(K0);
   __shared__ int2 queue[kScatterWarps][64];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r0 = (blockIdx.x * kScatterWarps + w) * 32;
+  const int r0 = (blockIdx.x * kScatterWarps + w) * R;
   if (r0 >= C.n) return;  // warp-uniform
-  const int nrows = min(32, C.n - r0);
+  const int nrows = min(R, C.n - r0);
   int2* q = queue[w];
   // start offset of row r0 + lane (rows past the end start at e1)
   const int my_start = lane < nrows ? __ldg(C.ptr + r0 + lane) : 0x7fffffff;
@@ -841,7 +845,7 @@ __global__ void __launch_bounds__(32 * kScatterWarps) k_scatter_fp64_c(
     // every shuffle is executed by the full warp; r + step stays below 32)
     int r = 0;
 #pragma unroll
-    for (int step = 16; step > 0; step >>= 1) {
+    for (int step = R / 2; step > 0; step >>= 1) {
       const int s = __shfl_sync(kFullMask, my_start, r + step);
       if (s <= k) r += step;
     }
@@ -1173,16 +1177,24 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
   if (L.precision == LJ_PREC_FP64) {
     if (!gather && L.kernel == 2) {
       const MixedConsts K = make_mixed_consts(L);
-      const int cb = (n + 32 * kScatterWarps - 1) / (32 * kScatterWarps);
-      return dispatch_bools(pbc, soa, [&](auto P, auto S) {
-        if (L.aniso)
-          k_scatter_fp64_c<P.value, S.value, true>
-              <<<cb, 32 * kScatterWarps, 0, s>>>(L.part, L.csr, L.qfix, K);
-        else
-          k_scatter_fp64_c<P.value, S.value, false>
-              <<<cb, 32 * kScatterWarps, 0, s>>>(L.part, L.csr, L.qfix, K);
-        return cudaGetLastError();
-      });
+      // lanes per row on average: 1 -> 32 rows per warp, 2 -> 16, 4 -> 8, 8 or more -> 4
+      auto go = [&](auto rows) -> cudaError_t {
+        constexpr int R = decltype(rows)::value;
+        const int cb = (n + R * kScatterWarps - 1) / (R * kScatterWarps);
+        return dispatch_bools(pbc, soa, [&](auto P, auto S) {
+          if (L.aniso)
+            k_scatter_fp64_c<P.value, S.value, true, R>
+                <<<cb, 32 * kScatterWarps, 0, s>>>(L.part, L.csr, L.qfix, K);
+          else
+            k_scatter_fp64_c<P.value, S.value, false, R>
+                <<<cb, 32 * kScatterWarps, 0, s>>>(L.part, L.csr, L.qfix, K);
+          return cudaGetLastError();
+        });
+      };
+      if (L.lanes <= 1) return go(std::integral_constant<int, 32>{});
+      if (L.lanes == 2) return go(std::integral_constant<int, 16>{});
+      if (L.lanes == 4) return go(std::integral_constant<int, 8>{});
+      return go(std::integral_constant<int, 4>{});
     }
     if (gather && L.kernel == 2) {
       const MixedConsts K = make_mixed_consts(L);
