@@ -21,7 +21,7 @@
  * safe: use one per host thread.
  *
  * Layouts: AoS q/p are double[n][4] (x, y, z, w; w unused and untouched,
- * 32-byte aligned: the reference's double4 / cpu_ref q[N][4]).  SoA passes
+ * at least 16-byte aligned: the reference's double4 / cpu_ref q[N][4]).  SoA passes
  * the three coordinate arrays separately (cpu_ref/force_soa.cpp q[X], q[Y],
  * q[Z] rows).  Indices are int32, offsets in pointer[] are int32 (as in the
  * reference), list lengths are int64.
