@@ -1189,6 +1189,11 @@ int lj_measure_aos(lj_ctx* ctx, const double* q_host, double* p_host, int32_t n,
   if (n > 0 && (!q_host || !p_host)) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "null q or p");
   int rc = check_opts(ctx, o);
   if (rc) return rc;
+  if (!ctx->half.valid && !ctx->full.valid) return fail(ctx, LJ_ERR_NO_LIST, "no list installed");
+  const int32_t rows = ctx->full.valid ? ctx->full.n : ctx->half.n;
+  if (n != rows)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "n = %d but the installed list has %d rows", n,
+                rows);
   if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
   const size_t bytes = sizeof(double) * 4 * (size_t)n;
   LJ_CUDA(ctx, ctx->mq.ensure(4 * (size_t)n), "alloc");
@@ -1207,7 +1212,7 @@ int lj_measure_aos(lj_ctx* ctx, const double* q_host, double* p_host, int32_t n,
     if ((rc = copy_in(ctx, l.list.ptr, ctx->h_list.data(), ctx->h_list.size(), LJ_WHERE_HOST)))
       return rc;
     if (ctx->host_kind == LJ_LIST_FULL && l.avalid)  // the gather reads the aligned copy
-      LJ_CUDA(ctx, launch_copy_rows4(l.np.ptr, l.ptr.ptr, l.list.ptr, l.aoff.ptr, n,
+      LJ_CUDA(ctx, launch_copy_rows4(l.np.ptr, l.ptr.ptr, l.list.ptr, l.aoff.ptr, l.n,
                                      l.alist.ptr, l.aptr.ptr, s), "aligned copy");
   }
   LJ_CUDA(ctx, cudaEventRecord(ctx->ev[1], s), "event");

@@ -583,3 +583,17 @@ def test_random_systems_every_path(engine, seed):
         np_d, ptr_d, lst_d = ctx.get_list_csr("half")
         np_r, ptr_r, lst_r = ol.build_list(q, 3.3, box=box)
         assert np.array_equal(np_d, np_r) and np.array_equal(lst_d, lst_r), seed
+
+
+def test_measure_checks_the_particle_count(engine, fixture_rho05):
+    f = fixture_rho05
+    with engine.Context(0) as ctx:
+        q = np.ascontiguousarray(f["q"])
+        with pytest.raises(engine.LJError) as e:  # no list yet
+            ctx.measure_aos(q, np.zeros_like(q), engine.make_opts(), calls=1)
+        assert e.value.status == engine.LJ_ERR_NO_LIST
+        ctx.set_list_csr(f["np"], f["ptr"], f["list"])
+        q2 = np.ascontiguousarray(np.concatenate([q, q[:7]]))  # 7 particles too many
+        with pytest.raises(engine.LJError) as e:
+            ctx.measure_aos(q2, np.zeros_like(q2), engine.make_opts(), calls=1)
+        assert e.value.status == engine.LJ_ERR_INVALID_ARGUMENT
