@@ -196,7 +196,9 @@ int lj_force_csr_fp64_aos(const double* q, double* p, int32_t n, double dt, doub
                           const int32_t* pointer, int32_t kind, const double* box,
                           void* stream);
 /* force_pair on the device (cpu_ref/force_aos.cpp:171-190): FP64 scatter over
- * an unsorted (i, j) pair array, both ends updated with atomics. */
+ * an unsorted (i, j) pair array, both ends updated with atomics.  The pair
+ * indices are not validated (force_pair does not either): each must be in
+ * [0, n). */
 int lj_force_pairs_fp64_aos(const double* q, double* p, int32_t n, double dt, double cl2,
                             const int32_t* i_particles, const int32_t* j_particles,
                             int64_t n_pairs, const double* box, void* stream);
