@@ -116,17 +116,83 @@ class Dist:
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
+class _Nvml:
+    """Read-only NVML queries through ctypes (the library ships with the
+    driver): SM clock, its maximum, power and the active clock-event reasons
+    of one device.  Nothing here sets anything."""
+    SM = 1  # NVML_CLOCK_SM
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, cuda_index):
+        import ctypes
+        self.c = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        bus = self._bus_id(cuda_index)
+        rc = (self.lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(self.h))
+              if bus else self.lib.nvmlDeviceGetHandleByIndex_v2(cuda_index,
+                                                                 ctypes.byref(self.h)))
+        if rc != 0:
+            self.lib.nvmlShutdown()
+            raise OSError("no NVML handle for CUDA device %d" % cuda_index)
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.max_mhz = self._uint(self.lib.nvmlDeviceGetMaxClockInfo, self.SM)
+
+    @staticmethod
+    def _bus_id(cuda_index):
+        # NVML numbers devices in PCI order, CUDA by CUDA_VISIBLE_DEVICES:
+        # match them by bus id where torch reports it
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(cuda_index)
+            return "%08X:%02X:%02X.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+        except (AttributeError, RuntimeError, AssertionError):
+            return None
+
+    def _uint(self, fn, *args):
+        v = self.c.c_uint()
+        return v.value if fn(self.h, *args, self.c.byref(v)) == 0 else None
+
+    def sample(self):
+        r = self.c.c_ulonglong()
+        ok = self.reasons_fn(self.h, self.c.byref(r)) == 0
+        return (self._uint(self.lib.nvmlDeviceGetClockInfo, self.SM),
+                self._uint(self.lib.nvmlDeviceGetPowerUsage),
+                [nm for bit, nm in self.REASONS.items() if ok and r.value & bit])
+
+    def close(self):
+        self.lib.nvmlShutdown()
+
+
 class ClockSampler:
+    """SM clock and clock-event reasons sampled during a timed region: NVML
+    every 2 ms where the library loads, else `nvidia-smi -lms 100`."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_S = 0.002
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
+        self.nvml = None
         self.lines = []
+        self.samples = []  # (sm MHz, power mW, reasons) from NVML
+        self.stop = threading.Event()
 
     def __enter__(self):
+        try:
+            self.nvml = _Nvml(self.gpu)
+            self.samples.append(self.nvml.sample())
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return self
+        except (OSError, AttributeError):
+            self.nvml = None
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
@@ -138,11 +204,20 @@ class ClockSampler:
             self.proc = None
         return self
 
+    def _poll(self):
+        while not self.stop.wait(self.PERIOD_S):
+            self.samples.append(self.nvml.sample())
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        if self.nvml:
+            self.stop.set()
+            self.t.join(timeout=5)
+            self.samples.append(self.nvml.sample())
+            self.nvml.close()
         if self.proc:
             self.proc.terminate()
             try:
@@ -151,6 +226,15 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml:
+            sm = [s[0] for s in self.samples if s[0] is not None]
+            pw = [s[1] / 1e3 for s in self.samples if s[1] is not None]
+            reasons = sorted({nm for s in self.samples for nm in s[2]})
+            if sm:
+                return {"sm_mhz": statistics.median(sm), "sm_min_mhz": min(sm),
+                        "sm_max_mhz": self.nvml.max_mhz, "reasons": reasons,
+                        "power_w_median": statistics.median(pw) if pw else None,
+                        "samples": len(sm), "source": "nvml, every 2 ms"}
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
@@ -168,7 +252,25 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi -lms 100"}
+
+
+def merge_clocks(parts):
+    """One clock record from several sampled segments: the median of the
+    segments' medians, the lowest clock seen and every reason seen."""
+    got = [c for c in parts if c.get("samples")]
+    if not got:
+        return parts[0] if parts else None
+    out = dict(got[0])
+    out["sm_mhz"] = statistics.median(c["sm_mhz"] for c in got)
+    if all("sm_min_mhz" in c for c in got):
+        out["sm_min_mhz"] = min(c["sm_min_mhz"] for c in got)
+    pw = [c["power_w_median"] for c in got if c.get("power_w_median") is not None]
+    if pw:
+        out["power_w_median"] = statistics.median(pw)
+    out["reasons"] = sorted({r for c in got for r in c["reasons"]})
+    out["samples"] = sum(c["samples"] for c in got)
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -484,9 +586,11 @@ def run_precision(args, dist):
     errors = [dict(step=0, **force_errors(torch, lj, L, qd))]
     ctx = lj.Context(dist.local, stream=torch.cuda.current_stream())
     prm = lj.make_md_params(DT, RC, RS - RC, L, precision="mixed", record_every=100)
-    records, ms, rebuilds = [], 0.0, 0
+    records, ms, rebuilds, clock_samples = [], 0.0, 0, []
     for seg in range(10):
-        recs, st = ctx.md_run(qd, pd, prm, 100)
+        with ClockSampler(dist.local) as cs:
+            recs, st = ctx.md_run(qd, pd, prm, 100)
+        clock_samples.append(cs.summary())
         ms += st["ms_total"]
         rebuilds += st["rebuilds"]
         records += [(r[0] + 100 * seg, r[1], r[2]) for r in recs if seg == 0 or r[0] > 0]
@@ -508,6 +612,7 @@ def run_precision(args, dist):
             "global_rel_force_error": max(e["global_rel"] for e in errors),
             "force_errors": errors, "energy_drift_rel": drift,
             "energies": [{"step": r[0], "kinetic": r[1], "potential": r[2]} for r in records],
+            "clocks": merge_clocks(clock_samples),
             "note": "the cut, unshifted potential (the reference's) jumps when pairs cross "
                     "rc, so total energy drifts in FP64 too; force errors are against the "
                     "engine's FP64 path on the same positions"}
@@ -535,7 +640,8 @@ def run_large(args, dist):
         ctx = lj.Context(dist.local, stream=torch.cuda.current_stream())
         prm = lj.make_md_params(DT, RC, RS - RC, L, precision=prec, record_every=steps,
                                 rebuild_every=20)
-        recs, st = ctx.md_run(qd, pd, prm, steps)
+        with ClockSampler(dist.local) as cs:
+            recs, st = ctx.md_run(qd, pd, prm, steps)
         ctx.build_list(qd, RS, box=L, kinds=("half",))
         _, P, _ = ctx.list_info("half")
         ctx.close()
@@ -545,7 +651,8 @@ def run_large(args, dist):
                      "gpairs": P / (ms * 1e-3) / 1e9, "hbm_gbs": step_bytes / (ms * 1e-3) / 1e9,
                      "hbm_frac": step_bytes / (ms * 1e-3) / 1e9 / hbm,
                      "rebuilds": st["rebuilds"], "pairs_half": P,
-                     "energy_first_last": [recs[0][1] + recs[0][2], recs[-1][1] + recs[-1][2]]}
+                     "energy_first_last": [recs[0][1] + recs[0][2], recs[-1][1] + recs[-1][2]],
+                     "clocks": cs.summary()}
         del qd, pd
         torch.cuda.empty_cache()
     out["mixed_over_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
@@ -580,7 +687,9 @@ def run_batch(args, dist):
     qd, pd = torch.from_numpy(q).to(dev), torch.from_numpy(p).to(dev)
     prm = lj.make_md_params(DT, 2.5, 0.3, 1.0, precision="mixed", record_every=steps)
     ctx = lj.Context(dist.local, stream=torch.cuda.current_stream())
-    en, st, shapes = ctx.batch_run(qd, pd, np.array(offs, np.int32), np.array(boxes), prm, steps)
+    with ClockSampler(dist.local) as cs:
+        en, st, shapes = ctx.batch_run(qd, pd, np.array(offs, np.int32), np.array(boxes), prm,
+                                       steps)
     ctx.close()
     # half-list pairs within rc + skin per replica, counted once on the device
     pairs = 0
@@ -604,6 +713,7 @@ def run_batch(args, dist):
             "size_classes": [{"rows": int(s[0]), "lanes": int(s[1]), "entries_in_flight": int(s[2])}
                              for s in shapes if s[0] > 0],
             "energy_change_rel_max": float(np.max(np.abs(e1 - e0) / np.abs(e0))),
+            "clocks": cs.summary(),
             "note": "graph-captured step chunks with flag-guarded on-device rebuilds; per-class "
                     "gather shapes timed at start-up"}
 
