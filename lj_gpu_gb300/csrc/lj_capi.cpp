@@ -382,6 +382,7 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
     if (o->precision == LJ_PREC_MIXED && method == LJ_METHOD_SCATTER_HALF) {
       LJ_CUDA(ctx, ctx->fscratch.ensure(4 * (size_t)n), "alloc");
       L.fscratch = ctx->fscratch.ptr;
+      L.scratch_zeroed = 1;  // the image pass below clears it
     }
     if (L.kernel == 3 && L.aniso) L.kernel = 2;
     if (L.kernel == 3) {

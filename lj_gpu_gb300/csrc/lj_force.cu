@@ -263,7 +263,8 @@ template <bool SOA>
 __global__ void __launch_bounds__(256) k_fixed_image(const Particles P, int n,
                                                      FixedAxis ax, FixedAxis ay, FixedAxis az,
                                                      const unsigned long long* open_key,
-                                                     int4* __restrict__ out) {
+                                                     int4* __restrict__ out,
+                                                     float4* __restrict__ zero_acc) {
   // the pair kernel that follows may launch now (it waits for this grid)
   asm volatile("griddepcontrol.launch_dependents;");
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -271,6 +272,9 @@ __global__ void __launch_bounds__(256) k_fixed_image(const Particles P, int n,
   if (open_key) ax = ay = az = pow2_axis(open_frame_exp(*open_key));
   const double3 q = load_q<SOA>(P, i);
   out[i] = make_int4(to_fixed(q.x, ax), to_fixed(q.y, ay), to_fixed(q.z, az), 0);
+  // the mixed scatter's force accumulator, cleared here instead of by a
+  // separate memset launch
+  if (zero_acc) zero_acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 template <bool SOA>
@@ -938,6 +942,9 @@ __global__ void __launch_bounds__(256) k_scatter_mixed_u(const Particles P, cons
                                                          const int4* __restrict__ qfix,
                                                          float4* __restrict__ facc,
                                                          const MixedConsts K0) {
+  // Launched as a programmatic dependent of the image pass, which also
+  // clears facc: nothing the stream wrote is read before that grid finished.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const MixedConsts K = PBC ? K0 : frame_consts(K0);
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / G;
@@ -1003,6 +1010,9 @@ __global__ void __launch_bounds__(256) k_scatter_mixed_u(const Particles P, cons
     ay.add(sy);
     az.add(sz);
   }
+  // the kick may be scheduled once every block is here (it still waits for
+  // this grid to finish before reading facc)
+  asm volatile("griddepcontrol.launch_dependents;");
   float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
   if (G > 1) {
     group_reduce_comp<G>(hx, lx);
@@ -1016,6 +1026,9 @@ template <bool SOA>
 __global__ void __launch_bounds__(256) k_kick_from_scratch(const Particles P, int n,
                                                            const float* __restrict__ facc,
                                                            const MixedConsts K0) {
+  // may be launched as a programmatic dependent of the scatter: the sums
+  // are read only after that grid has finished
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const MixedConsts K = frame_consts(K0);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -1146,12 +1159,13 @@ cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s) {
   const int n = L.csr.n;
   if (n == 0) return cudaSuccess;
   const int blocks = (n + 255) / 256;
+  float4* acc = reinterpret_cast<float4*>(L.fscratch);
   if (L.part.soa)
     k_fixed_image<true><<<blocks, 256, 0, s>>>(L.part, n, L.axis[0], L.axis[1], L.axis[2],
-                                              L.open_key, L.qfix);
+                                              L.open_key, L.qfix, acc);
   else
     k_fixed_image<false><<<blocks, 256, 0, s>>>(L.part, n, L.axis[0], L.axis[1], L.axis[2],
-                                               L.open_key, L.qfix);
+                                               L.open_key, L.qfix, acc);
   return cudaGetLastError();
 }
 
@@ -1252,7 +1266,7 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
       default: return cudaErrorInvalidValue;
     }
   }
-  if (!gather) {
+  if (!gather && !L.scratch_zeroed) {
     cudaError_t e = cudaMemsetAsync(L.fscratch, 0, sizeof(float) * 4 * (size_t)n, s);
     if (e != cudaSuccess) return e;
   }
@@ -1264,12 +1278,10 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
           constexpr int G = decltype(g)::value;
           float4* fa = reinterpret_cast<float4*>(L.fscratch);
           if (L.aniso)
-            k_scatter_mixed_u<G, U, P.value, S.value, true>
-                <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, fa, K);
-          else
-            k_scatter_mixed_u<G, U, P.value, S.value, false>
-                <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, fa, K);
-          return cudaGetLastError();
+            return launch_dependent(k_scatter_mixed_u<G, U, P.value, S.value, true>, blocks,
+                                    block, s, L.part, L.csr, L.qfix, fa, K);
+          return launch_dependent(k_scatter_mixed_u<G, U, P.value, S.value, false>, blocks,
+                                  block, s, L.part, L.csr, L.qfix, fa, K);
         });
       });
     };
@@ -1283,9 +1295,10 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
     }
     if (e != cudaSuccess) return e;
     const int kb = (n + 255) / 256;
-    if (soa) k_kick_from_scratch<true><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
-    else k_kick_from_scratch<false><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
-    return cudaGetLastError();
+    if (soa) return launch_dependent(k_kick_from_scratch<true>, kb, 256, s, L.part, n,
+                                     static_cast<const float*>(L.fscratch), K);
+    return launch_dependent(k_kick_from_scratch<false>, kb, 256, s, L.part, n,
+                            static_cast<const float*>(L.fscratch), K);
   }
   cudaError_t e = dispatch_lanes(L.lanes, [&](auto g) {
     return dispatch_bools(pbc, soa, [&](auto P, auto S) {

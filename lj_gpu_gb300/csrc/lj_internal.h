@@ -81,6 +81,10 @@ struct ForceLaunch {
   // mixed precision only
   int4* qfix;      // n entries, written by the fixed-image pass
   float* fscratch; // 4 n floats, one float4 per particle (scatter-half mixed only)
+  // launch_fixed_image zeroes fscratch (when set) with the image, and
+  // launch_force then skips its own clear; callers that write the image some
+  // other way leave this 0
+  int scratch_zeroed;
   FixedAxis axis[3];
   double unit[3];  // length per fixed unit on each axis
   int aniso;       // axes with different units
