@@ -78,6 +78,29 @@ __device__ __forceinline__ void kick_p(const Particles& P, int i, double fx, dou
   }
 }
 
+// The kick of a gather row whose G lanes all hold the compensated sums
+// (hi, lo) per axis.  With G >= 4 lanes 0, 1, 2 each apply one axis: one
+// FP64 FMA instruction per warp instead of three (FP64 issue is charged per
+// warp instruction, whatever the active lanes), with the same per-axis
+// arithmetic as kick_p.
+template <bool SOA, int G>
+__device__ __forceinline__ void kick_group(const Particles& P, int i, int lane, bool valid,
+                                           float hx, float lx, float hy, float ly, float hz,
+                                           float lz, const double* s) {
+  if (G < 4) {
+    if (valid && lane == 0) kick_p<SOA>(P, i, widen_f32(hx + lx), widen_f32(hy + ly),
+                                        widen_f32(hz + lz), s);
+    return;
+  }
+  if (!valid || lane > 2) return;
+  const float v = lane == 0 ? hx + lx : (lane == 1 ? hy + ly : hz + lz);
+  const double sc = lane == 0 ? s[0] : (lane == 1 ? s[1] : s[2]);
+  double* a;
+  if (SOA) a = (lane == 0 ? P.px : (lane == 1 ? P.py : P.pz)) + i;
+  else a = P.p + rec(P, i) + lane;
+  *a = fma(widen_f32(v), sc, *a);
+}
+
 template <bool SOA>
 __device__ __forceinline__ void red_p(const Particles& P, int i, double fx, double fy,
                                       double fz) {
@@ -369,8 +392,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const C
     group_reduce_comp<G>(hy, ly);
     group_reduce_comp<G>(hz, lz);
   }
-  if (valid && lane == 0)
-    kick_p<SOA>(P, i, widen_f32(hx + lx), widen_f32(hy + ly), widen_f32(hz + lz), K.fscale);
+  kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale);
 }
 
 // Unrolled mixed gather (kernel 2).  The row loop runs to the longest row of
@@ -485,8 +507,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
     group_reduce_comp<G>(hy, ly);
     group_reduce_comp<G>(hz, lz);
   }
-  if (valid && lane == 0)
-    kick_p<SOA>(P, i, widen_f32(hx + lx), widen_f32(hy + ly), widen_f32(hz + lz), K.fscale);
+  kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale);
 }
 
 // Batched mixed gather: as k_gather_mixed_u, with every constant that depends
@@ -599,8 +620,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
     group_reduce_comp<G>(hy, ly);
     group_reduce_comp<G>(hz, lz);
   }
-  if (valid && lane == 0)
-    kick_p<false>(P, i, widen_f32(hx + lx), widen_f32(hy + ly), widen_f32(hz + lz), K.fscale);
+  kick_group<false, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale);
 }
 
 // Cell-tiled mixed gather (kernel 3).  One CTA per cell: it copies the
@@ -714,8 +734,7 @@ __global__ void __launch_bounds__(kTiledThreads) k_gather_mixed_tiled(
       group_reduce_comp<G>(hy, ly);
       group_reduce_comp<G>(hz, lz);
     }
-    if (valid && lane == 0)
-      kick_p<SOA>(P, i, widen_f32(hx + lx), widen_f32(hy + ly), widen_f32(hz + lz), K.fscale);
+    kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale);
   }
 }
 
