@@ -59,22 +59,38 @@ __device__ __forceinline__ void add_p(const Particles& P, int i, double fx, doub
   }
 }
 
+// v * 2^k exactly, by adding k to the exponent field: integer instructions
+// only (FP64 issue is scarce on this part).  Zero, subnormal, inf/NaN and
+// results that would leave the normal range take ldexp.
+__device__ __forceinline__ double scale_pow2(double v, int k) {
+  const long long b = __double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e == 0 || e == 0x7ff || e + k <= 0 || e + k >= 0x7ff) return ldexp(v, k);
+  return __longlong_as_double(b + (long long)k * (1ll << 52));
+}
+
 // p_i = fma(f, s, p_i) per component: the single FP64 operation the mixed
-// path spends per particle and axis.
+// path spends per particle and axis (s scaled by 2^fexp when fexp != 0).
 template <bool SOA>
 __device__ __forceinline__ void kick_p(const Particles& P, int i, double fx, double fy,
-                                       double fz, const double* s) {
+                                       double fz, const double* s, int fexp = 0) {
+  double s0 = s[0], s1 = s[1], s2 = s[2];
+  if (fexp) {
+    s0 = scale_pow2(s0, fexp);
+    s1 = scale_pow2(s1, fexp);
+    s2 = scale_pow2(s2, fexp);
+  }
   if (SOA) {
-    P.px[i] = fma(fx, s[0], P.px[i]);
-    P.py[i] = fma(fy, s[1], P.py[i]);
-    P.pz[i] = fma(fz, s[2], P.pz[i]);
+    P.px[i] = fma(fx, s0, P.px[i]);
+    P.py[i] = fma(fy, s1, P.py[i]);
+    P.pz[i] = fma(fz, s2, P.pz[i]);
   } else {
     double* b = P.p + rec(P, i);
     double2 xy = *reinterpret_cast<double2*>(b);
-    xy.x = fma(fx, s[0], xy.x);
-    xy.y = fma(fy, s[1], xy.y);
+    xy.x = fma(fx, s0, xy.x);
+    xy.y = fma(fy, s1, xy.y);
     *reinterpret_cast<double2*>(b) = xy;
-    b[2] = fma(fz, s[2], b[2]);
+    b[2] = fma(fz, s2, b[2]);
   }
 }
 
@@ -86,15 +102,16 @@ __device__ __forceinline__ void kick_p(const Particles& P, int i, double fx, dou
 template <bool SOA, int G>
 __device__ __forceinline__ void kick_group(const Particles& P, int i, int lane, bool valid,
                                            float hx, float lx, float hy, float ly, float hz,
-                                           float lz, const double* s) {
+                                           float lz, const double* s, int fexp) {
   if (G < 4) {
     if (valid && lane == 0) kick_p<SOA>(P, i, widen_f32(hx + lx), widen_f32(hy + ly),
-                                        widen_f32(hz + lz), s);
+                                        widen_f32(hz + lz), s, fexp);
     return;
   }
   if (!valid || lane > 2) return;
   const float v = lane == 0 ? hx + lx : (lane == 1 ? hy + ly : hz + lz);
-  const double sc = lane == 0 ? s[0] : (lane == 1 ? s[1] : s[2]);
+  double sc = lane == 0 ? s[0] : (lane == 1 ? s[1] : s[2]);
+  if (fexp) sc = scale_pow2(sc, fexp);
   double* a;
   if (SOA) a = (lane == 0 ? P.px : (lane == 1 ? P.py : P.pz)) + i;
   else a = P.p + rec(P, i) + lane;
@@ -262,6 +279,7 @@ struct MixedConsts {
   float k_hi, k_lo;      // 1/unit^2 split in two floats (isotropic frames)
   float u_hi[3], u_lo[3];  // per-axis unit split in two floats (anisotropic)
   double fscale[3];      // unit * dt per axis (isotropic) or dt (anisotropic)
+  int fexp;              // the kick scales by fscale * 2^fexp (device-chosen open frames)
   Fp64Consts f64;        // for the rare FP64 cutoff decision
   const unsigned long long* open_key;  // device-chosen open-box frame, see frame_consts
 };
@@ -277,7 +295,7 @@ __device__ __forceinline__ MixedConsts frame_consts(const MixedConsts& K0) {
     K.cl2_hi = ldexpf(K0.cl2_hi, 2 * k);
     K.k_hi = ldexpf(K0.k_hi, 2 * k);
     K.k_lo = ldexpf(K0.k_lo, 2 * k);
-    for (int d = 0; d < 3; d++) K.fscale[d] = ldexp(K0.fscale[d], -k);
+    K.fexp = -k;  // fscale is scaled where the kick reads it
   }
   return K;
 }
@@ -392,7 +410,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const C
     group_reduce_comp<G>(hy, ly);
     group_reduce_comp<G>(hz, lz);
   }
-  kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale);
+  kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
 }
 
 // Unrolled mixed gather (kernel 2).  The row loop runs to the longest row of
@@ -507,7 +525,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
     group_reduce_comp<G>(hy, ly);
     group_reduce_comp<G>(hz, lz);
   }
-  kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale);
+  kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
 }
 
 // Batched mixed gather: as k_gather_mixed_u, with every constant that depends
@@ -620,7 +638,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
     group_reduce_comp<G>(hy, ly);
     group_reduce_comp<G>(hz, lz);
   }
-  kick_group<false, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale);
+  kick_group<false, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
 }
 
 // Cell-tiled mixed gather (kernel 3).  One CTA per cell: it copies the
@@ -734,7 +752,7 @@ __global__ void __launch_bounds__(kTiledThreads) k_gather_mixed_tiled(
       group_reduce_comp<G>(hy, ly);
       group_reduce_comp<G>(hz, lz);
     }
-    kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale);
+    kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
   }
 }
 
@@ -1052,7 +1070,7 @@ __global__ void __launch_bounds__(256) k_kick_from_scratch(const Particles P, in
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   kick_p<SOA>(P, i, widen_f32(facc[4 * (size_t)i]), widen_f32(facc[4 * (size_t)i + 1]),
-              widen_f32(facc[4 * (size_t)i + 2]), K.fscale);
+              widen_f32(facc[4 * (size_t)i + 2]), K.fscale, K.fexp);
 }
 
 // ---------------------------------------------------------------------------
