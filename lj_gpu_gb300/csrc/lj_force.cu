@@ -540,26 +540,23 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
   const int g = t / G;
   const int lane = t & (G - 1);
   const bool valid = g < nrows;
-  int cnt = 0, i = 0;
+  int cnt = 0, i = 0, r = 0;
   int64_t k0 = 0;
   int4 xi = make_int4(0, 0, 0, 0);
+  // only the constants of the pair loop are held in registers; the rare FP64
+  // cutoff decision and the kick read the replica table where they need it
   MixedConsts K{};
   if (valid) {
     i = __ldg(rows + g);
     cnt = __ldg(C.np + i);
     k0 = row_start(C, i);
     xi = __ldg(qfix + i);
-    const ReplicaInfo& R = reps[__ldg(rid + i)];
+    r = __ldg(rid + i);
+    const ReplicaInfo& R = reps[r];
     K.k_hi = R.k_hi;
     K.k_lo = R.k_lo;
     K.cl2_lo = R.cl2u_lo;
     K.cl2_hi = R.cl2u_hi;
-    K.f64.cl2_bits = cl2_bits;
-    for (int d = 0; d < 3; d++) {
-      K.f64.len[d] = R.len[d];
-      K.f64.half_bits[d] = R.half_bits[d];
-    }
-    K.fscale[0] = K.fscale[1] = K.fscale[2] = R.unit * dt;
   }
   int cmax = cnt;
 #pragma unroll
@@ -618,8 +615,15 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
 #pragma unroll
       for (int u = 0; u < U; u++) {
         if (!(border & (1u << u))) continue;
-        const double3 d64 = sep_fp64<true>(load_q<false>(P, i), load_q<false>(P, jj[u]), K.f64);
-        if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
+        const ReplicaInfo& R = reps[r];
+        Fp64Consts f64{};
+        f64.cl2_bits = cl2_bits;
+        for (int d = 0; d < 3; d++) {
+          f64.len[d] = R.len[d];
+          f64.half_bits[d] = R.half_bits[d];
+        }
+        const double3 d64 = sep_fp64<true>(load_q<false>(P, i), load_q<false>(P, jj[u]), f64);
+        if (beyond_cutoff(r2_fp64(d64), cl2_bits)) continue;
         const float3 d = sep_mixed<false>(xi, xj[u], K);
         const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
         const float df = df_mixed<false>(r2, K);
@@ -638,7 +642,9 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
     group_reduce_comp<G>(hy, ly);
     group_reduce_comp<G>(hz, lz);
   }
-  kick_group<false, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
+  const double kf = valid ? reps[r].unit * dt : 0.0;
+  const double fs[3] = {kf, kf, kf};
+  kick_group<false, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, fs, 0);
 }
 
 // Cell-tiled mixed gather (kernel 3).  One CTA per cell: it copies the
