@@ -479,10 +479,10 @@ def run_ours(args, dist, density=DENSITY):
     alg = pair_kernel_bytes(method, layout, P, N)
     achieved = alg / (t_pair_ms * 1e-3) / 1e9
     # DRAM traffic per launch from the committed ncu capture of this kernel on
-    # this workload (the AoS gather at rho 0.5); other workloads and kernels
-    # have none
-    prof = "force_mixed_gather_aos_108k_rho0.5.txt"
-    matches = density == DENSITY and layout == "aos" and method == "gather"
+    # this workload (the AoS and SoA gathers at rho 0.5); other workloads and
+    # kernels have none
+    prof = f"force_mixed_gather_{layout}_108k_rho0.5.txt"
+    matches = density == DENSITY and method == "gather"
     traffic = profiled_traffic(prof) if matches else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
