@@ -737,11 +737,29 @@ def cpu_baseline(q, L, P, sample_calls=5):
     t1 = time.perf_counter()
     ol.force_sorted_aos(q, p, *half, cl2=RC * RC, dt=DT, box=L, calls=1)
     t_single = time.perf_counter() - t1
+    t2 = time.perf_counter()
+    ol.force_sorted_soa(q, p, *half, cl2=RC * RC, dt=DT, box=L, calls=1)
+    t_single_soa = time.perf_counter() - t2
     return {"value": P * sample_calls / t / 1e9, "unit": UNIT, "cores": threads,
-            "kind": "port",
+            "kind": "port", "cpu": cpu_model(), "nproc": os.cpu_count(),
             "sample": f"{sample_calls} full force calls of the 108,000-particle system, "
                       "OpenMP gather over the full list (project-written parallelisation)",
-            "single_thread_force_sorted": P / t_single / 1e9}
+            "single_thread_force_sorted": P / t_single / 1e9,
+            "single_thread_force_sorted_soa": P / t_single_soa / 1e9}
+
+
+def cpu_model():
+    """The host CPU as lscpu names it (architecture and model)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+    except (OSError, subprocess.SubprocessError):
+        out = ""
+    info = {}
+    for line in out.splitlines():
+        k, _, v = line.partition(":")
+        info[k.strip()] = v.strip()
+    parts = [info.get("Architecture"), info.get("Vendor ID"), info.get("Model name")]
+    return ", ".join(x for x in parts if x) or None
 
 
 def run_reference(args, dist):
@@ -770,6 +788,7 @@ def run_reference(args, dist):
         "config": {"workload": WORKLOAD, "N": q.shape[0], "pairs_half": P,
                    "step": "one force call", "parallelism": "host cores"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "cpu": cpu_model(), "nproc": os.cpu_count(),
                          "sample": "every step is one full force call of the workload "
                                    "(C restatement of the reference routine, OpenMP gather)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
