@@ -59,6 +59,35 @@ __device__ __forceinline__ void add_p(const Particles& P, int i, double fx, doub
   }
 }
 
+// p_i[axis] += v (one component; several lanes may each apply one).
+template <bool SOA>
+__device__ __forceinline__ void add_p_axis(const Particles& P, int i, int axis, double v) {
+  double* a;
+  if (SOA) a = (axis == 0 ? P.px : (axis == 1 ? P.py : P.pz)) + i;
+  else a = P.p + rec(P, i) + axis;
+  *a += v;
+}
+
+// Sums x, y and z over the 32 lanes of a warp with 6 FP64 adds instead of
+// 15 (the FP64 pipe charges every warp instruction in full).  The halves of
+// the warp split the components as the sums narrow: after the offset-16 step
+// the lower half carries x and y and the upper half z, after the offset-8
+// step lanes with bit 3 clear carry x and the others y.  Returns this lane's
+// total: x in lanes 0-7, y in lanes 8-15, z in lanes 16-31.
+__device__ __forceinline__ double warp_reduce3_fp64(double x, double y, double z, int lane) {
+  const bool up = (lane & 16) != 0, b3 = (lane & 8) != 0;
+  double s1 = up ? z : x, s2 = up ? 0.0 : y;
+  const double o1 = up ? x : z, o2 = up ? y : 0.0;
+  s1 += __shfl_xor_sync(kFullMask, o1, 16);
+  s2 += __shfl_xor_sync(kFullMask, o2, 16);
+  double keep = (up || !b3) ? s1 : s2;
+  const double send = (up || b3) ? s1 : s2;
+  keep += __shfl_xor_sync(kFullMask, send, 8);
+#pragma unroll
+  for (int off = 4; off > 0; off >>= 1) keep += __shfl_xor_sync(kFullMask, keep, off);
+  return keep;
+}
+
 // v * 2^k exactly, by adding k to the exponent field: integer instructions
 // only (FP64 issue is scarce on this part).  Zero, subnormal, inf/NaN and
 // results that would leave the normal range take ldexp.
@@ -836,10 +865,8 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_gather_fp64_c(
     }
   }
   if (lane < qn) fp64_pair_acc<PBC, SOA>(P, qi, q[lane], K.f64, fx, fy, fz);
-  fx = group_reduce_fp64<32>(fx);
-  fy = group_reduce_fp64<32>(fy);
-  fz = group_reduce_fp64<32>(fz);
-  if (lane == 0) add_p<SOA>(P, i, fx, fy, fz);
+  const double total = warp_reduce3_fp64(fx, fy, fz, lane);
+  if ((lane & 7) == 0 && lane < 24) add_p_axis<SOA>(P, i, lane >> 3, total);
 }
 
 // Compacted FP64 scatter over the half list (kernel 2).  A warp owns 32
