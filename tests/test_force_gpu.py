@@ -101,7 +101,8 @@ def test_fp64_every_lane_width(engine, lanes):
 
 
 @pytest.mark.parametrize("name", list(SYSTEMS))
-@pytest.mark.parametrize("method,kernel", [("gather", 1), ("gather", 2), ("scatter", 1)])
+@pytest.mark.parametrize("method,kernel", [("gather", 1), ("gather", 2), ("scatter", 1),
+                                           ("scatter", 2)])
 @pytest.mark.parametrize("layout", ["aos", "soa"])
 def test_mixed_error_bounds(engine, name, method, kernel, layout):
     q, box, half = system(name)
@@ -117,12 +118,13 @@ def test_mixed_error_bounds(engine, name, method, kernel, layout):
 def test_mixed_every_lane_width(engine, lanes):
     q, box, half = system("pbc_rho1")
     ref = oracle_p(q, half, box, 1, 0.005)
-    for kernel, unrolls in ((1, [0]), (2, [2, 4, 8])):
+    for method, kernel, unrolls in (("gather", 1, [0]), ("gather", 2, [2, 4, 8]),
+                                    ("scatter", 2, [1, 2, 4, 8])):
         for unroll in unrolls:
-            got = run_engine(engine, q, half, box, "mixed", "gather", "aos", 1, 0.005, lanes=lanes,
+            got = run_engine(engine, q, half, box, "mixed", method, "aos", 1, 0.005, lanes=lanes,
                              kernel=kernel, unroll=unroll)
             e = ol.rel_errors(got, ref)
-            assert e["max_rel_rms"] <= MIXED_TOL["max_rel_rms"], (kernel, unroll, e)
+            assert e["max_rel_rms"] <= MIXED_TOL["max_rel_rms"], (method, kernel, unroll, e)
 
 
 def test_mixed_anisotropic_box(engine):
@@ -573,7 +575,7 @@ def test_random_systems_every_path(engine, seed):
                              kernel=kernel)
             assert ol.rel_errors(got, ref)["max_rel"] <= FP64_TOL, (seed, method, kernel)
         for method, kernel, unroll in (("gather", 1, 0), ("gather", 2, 4), ("gather", 4, 4),
-                                       ("scatter", 1, 0)):
+                                       ("scatter", 1, 0), ("scatter", 2, 4)):
             got = run_engine(engine, q, half, box, "mixed", method, "soa" if seed % 2 else "aos",
                              1, 0.005, ctx=ctx, kernel=kernel, unroll=unroll)
             e = ol.rel_errors(got, ref)
