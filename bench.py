@@ -295,6 +295,22 @@ def profiled_traffic(name):
     return None
 
 
+def profiled_metric(name, metric):
+    """One metric value (a number) from the `- `metric`: value unit` lines of an
+    ncu summary under profiles/."""
+    f = ROOT / "profiles" / name
+    if not f.exists():
+        return None
+    key = f"- `{metric}`:"
+    for line in f.read_text().splitlines():
+        if line.startswith(key):
+            try:
+                return float(line[len(key):].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
 # FP64 add / FMA issue rate measured on this pool's GB300 (one op per lane):
 # 503 G/s, i.e. ~1.0 TFLOP/s counting an FMA as two
 FP64_PEAK_OPS = 503e9
@@ -494,6 +510,13 @@ def run_ours(args, dist, density=DENSITY):
                 "force_call_bytes": algorithmic_bytes(method, layout, P, N),
                 "force_call_frac": algorithmic_bytes(method, layout, P, N)
                 / head["s_per_call"] / 1e9 / hbm}
+    if traffic:
+        # the pipe that bounds this kernel (random 16-B gathers through L1),
+        # from the same capture: wavefronts as a fraction of the pipe's peak
+        l1 = profiled_metric(prof, "l1tex__data_pipe_lsu_wavefronts.avg.pct_of_peak_sustained_elapsed")
+        dram = profiled_metric(prof, "gpu__dram_throughput.avg.pct_of_peak_sustained_elapsed")
+        roofline["l1_data_pipe_frac"] = l1 / 100 if l1 is not None else None
+        roofline["dram_throughput_frac"] = dram / 100 if dram is not None else None
     fp = results[best_fp64]
     fp_m, fp_l = best_fp64.split("/")[1], best_fp64.split("/")[2]
     if fp_m == "auto":
