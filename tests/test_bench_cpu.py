@@ -75,3 +75,30 @@ def test_dist_max_and_sum_over_two_gloo_ranks():
         assert p.exitcode == 0
     # every rank sees the slowest rank's time and the job total
     assert got == [(0, 2.0, 3.0), (1, 2.0, 3.0)]
+
+
+def test_bench_helpers():
+    """Host helpers behind the bench line: the roofline figures read from the
+    committed ncu summaries, the per-step byte model and the clock merge."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    for layout, alg in (("aos", 43_200_000), ("soa", 41_472_000)):
+        name = f"force_mixed_gather_{layout}_108k_rho0.5.txt"
+        traffic = bench.profiled_traffic(name)
+        l1 = bench.profiled_metric(
+            name, "l1tex__data_pipe_lsu_wavefronts.avg.pct_of_peak_sustained_elapsed")
+        assert traffic is not None and 0.8 < traffic / alg < 1.1, (layout, traffic)
+        assert l1 is not None and 0 < l1 <= 100
+        assert bench.pair_kernel_bytes("gather", layout, 4_212_000, 108_000) == alg
+    assert bench.profiled_metric("force_mixed_gather_aos_108k_rho0.5.txt", "no_such_metric") is None
+    # one MD step: the force call's gather over 2P entries plus 104 B and the
+    # drift's 112 B per particle, plus the rows written by rebuilds
+    assert bench.md_step_bytes(10, 2, 0.0) == 4 * 20 + 216 * 2
+    assert bench.md_step_bytes(10, 2, 0.5) == 4 * 20 + 216 * 2 + 4 * 20 * 0.5
+    merged = bench.merge_clocks([
+        {"sm_mhz": 2070, "sm_min_mhz": 2000, "sm_max_mhz": 2070, "reasons": [], "samples": 5},
+        {"sm_mhz": 2050, "sm_min_mhz": 1950, "sm_max_mhz": 2070, "reasons": ["sw_power_cap"],
+         "samples": 3},
+        {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}])
+    assert merged["samples"] == 8 and merged["sm_min_mhz"] == 1950
+    assert merged["reasons"] == ["sw_power_cap"] and merged["sm_mhz"] == 2060
