@@ -52,7 +52,14 @@ enum {
 };
 
 /* ---- enumerations ------------------------------------------------------- */
-enum { LJ_PREC_FP64 = 0, LJ_PREC_MIXED = 1 };
+/* LJ_PREC_FP64: the reference's FP64 arithmetic.
+ * LJ_PREC_MIXED: FP64 positions, momenta and kick; pair terms in two-float
+ *   (float-float) arithmetic from 42-bit fixed-point separations, with
+ *   compensated sums: per-particle force error about 1e-9 relative to FP64.
+ * LJ_PREC_MIXED_FP32: as MIXED with single FP32 pair terms (faster; its
+ *   per-particle error reaches ~1e-4 on particles whose pair terms cancel,
+ *   ~1e-6 of the RMS force). */
+enum { LJ_PREC_FP64 = 0, LJ_PREC_MIXED = 1, LJ_PREC_MIXED_FP32 = 2 };
 enum { LJ_LIST_HALF = 0, LJ_LIST_FULL = 1 };
 enum { LJ_WHERE_HOST = 0, LJ_WHERE_DEVICE = 1 };
 enum {
@@ -67,7 +74,7 @@ typedef struct lj_force_opts {
   double cl2;         /* squared cutoff (reference CL2); r2 > cl2 is skipped  */
   double box[3];      /* periodic box lengths, used when periodic != 0        */
   int32_t periodic;   /* 0: open boundaries (the reference), 1: minimum image */
-  int32_t precision;  /* LJ_PREC_FP64 or LJ_PREC_MIXED                        */
+  int32_t precision;  /* LJ_PREC_FP64, LJ_PREC_MIXED or LJ_PREC_MIXED_FP32     */
   int32_t method;     /* LJ_METHOD_*                                          */
   int32_t lanes;      /* lanes per i-particle, 0 = default, else 1,2,4,..,32  */
   int32_t block;      /* threads per block, 0 = default, else 64..256         */

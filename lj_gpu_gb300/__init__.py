@@ -27,12 +27,14 @@ LJ_ERR_TIMEOUT = 6
 LJ_ERR_NO_LIST = 7
 LJ_ERR_UNSUPPORTED = 8
 
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_MIXED_FP32 = 0, 1, 2
 LIST_HALF, LIST_FULL = 0, 1
 WHERE_HOST, WHERE_DEVICE = 0, 1
 METHOD_AUTO, METHOD_GATHER_FULL, METHOD_SCATTER_HALF = 0, 1, 2
 
-_PRECISION = {"fp64": PREC_FP64, "mixed": PREC_MIXED}
+# "mixed": two-float pair terms (per-particle error ~1e-9 of FP64);
+# "mixed_fp32": single FP32 pair terms (faster, ~1e-6 of the RMS force)
+_PRECISION = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "mixed_fp32": PREC_MIXED_FP32}
 _METHOD = {"auto": METHOD_AUTO, "gather": METHOD_GATHER_FULL, "scatter": METHOD_SCATTER_HALF}
 _KIND = {"half": LIST_HALF, "full": LIST_FULL}
 

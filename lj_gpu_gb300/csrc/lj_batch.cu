@@ -45,7 +45,8 @@ __global__ void __launch_bounds__(256) k_batch_drift(double* __restrict__ q,
   qi[0] = x;
   qi[1] = y;
   qi[2] = z;
-  const int4 X = make_int4(to_fixed(x, R.ax[0]), to_fixed(y, R.ax[1]), to_fixed(z, R.ax[2]), 0);
+  const int4 X = pack_image(to_fixed_fine(x, R.ax[0]), to_fixed_fine(y, R.ax[1]),
+                            to_fixed_fine(z, R.ax[2]));
   qfix[i] = X;
   const int4 r = qref[i];
   const float dx = (float)wrap_sub(X.x, r.x) * R.unit_f[0];
@@ -61,8 +62,8 @@ __global__ void k_batch_image(const double* __restrict__ q, int n,
   if (i >= n) return;
   const ReplicaInfo& R = reps[rid[i]];
   const double* b = q + 4 * (size_t)i;
-  qfix[i] = make_int4(to_fixed(b[0], R.ax[0]), to_fixed(b[1], R.ax[1]), to_fixed(b[2], R.ax[2]),
-                      0);
+  qfix[i] = pack_image(to_fixed_fine(b[0], R.ax[0]), to_fixed_fine(b[1], R.ax[1]),
+                       to_fixed_fine(b[2], R.ax[2]));
 }
 
 __global__ void k_batch_copy_ref(const int4* __restrict__ qfix, int4* __restrict__ qref, int n,
@@ -112,7 +113,7 @@ __global__ void __launch_bounds__(256) k_batch_energy(
       const double* qj = q + 4 * (size_t)j;
       double d[3];
       for (int x = 0; x < 3; x++) d[x] = min_image_fp64(qj[x] - qi[x], R.len[x], R.half_bits[x]);
-      in = !(fma(d[2], d[2], fma(d[1], d[1], d[0] * d[0])) > cl2);
+      in = !(fma(d[2], d[2], fma(d[0], d[0], d[1] * d[1])) > cl2);
     }
     if (!in) continue;
     float inv = 1.0f / r2;
@@ -198,12 +199,12 @@ cudaError_t batch_rebuild(BatchState& b, const double* q, double sl2, cudaStream
 }
 
 cudaError_t batch_kick(BatchState& b, const Particles& part, const std::vector<SizeClass>& cls,
-                       double dt, double cl2, cudaStream_t s) {
+                       double dt, double cl2, bool ff, cudaStream_t s) {
   const Csr c{b.n, 0, b.cnt.ptr, nullptr, b.rows.ptr, (int64_t)b.maxrow, 1};
   for (const SizeClass& k : cls) {
     cudaError_t e = launch_force_batch(part, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                        b.classrows.ptr + k.first, k.count, dt, cl2, k.lanes,
-                                       k.unroll, k.vec, s);
+                                       k.unroll, k.vec, ff, s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -223,8 +224,9 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "bad batch arguments");
   if ((reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(p)) & 15u)
     return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "q and p must be 16-byte aligned");
-  if (prm->precision != LJ_PREC_MIXED)
+  if (prm->precision != LJ_PREC_MIXED && prm->precision != LJ_PREC_MIXED_FP32)
     return lj_fail(ctx, LJ_ERR_UNSUPPORTED, "the batch runs the mixed path");
+  const bool ff = prm->precision == LJ_PREC_MIXED;  // two-float pair terms
   if (!(prm->dt > 0.0) || !(prm->rc > 0.0) || !(prm->skin >= 0.0))
     return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "dt, rc must be > 0 and skin >= 0");
   if (offsets[0] != 0 || offsets[n_replicas] != n_total)
@@ -264,7 +266,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
       F.box.len[d] = bx[d];
       F.box.half[d] = 0.5 * bx[d];
     }
-    make_fixed_frame(F, 0.0);
+    make_fixed_frame(F);
     const double u = F.unit[0], u2 = u * u;
     for (int d = 0; d < 3; d++) {
       I.ax[d] = F.axis[d];
@@ -277,10 +279,17 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     }
     split(1.0 / u2, I.k_hi, I.k_lo);
     const double cl2u = prm->rc * prm->rc / u2, sl2u = rs * rs / u2;
-    I.cl2u_lo = (float)(cl2u * (1 - 4e-6));
-    I.cl2u_hi = (float)(cl2u * (1 + 4e-6));
-    I.sl2u_lo = (float)(sl2u * (1 - 4e-6));
-    I.sl2u_hi = (float)(sl2u * (1 + 4e-6));
+    // cutoff and list bands: FP32 arithmetic plus the coarse quantum, and for
+    // two-float terms the float comparison plus the fine quantum
+    const double bc = cutoff_band(std::sqrt(cl2u), kCoarseQuantumErr, kBandFp32);
+    const double bf = cutoff_band(std::sqrt(cl2u), kCoarseQuantumErr / 1024.0, kBandFF);
+    const double bs = cutoff_band(std::sqrt(sl2u), kCoarseQuantumErr, kBandFp32);
+    I.cl2u_lo = (float)(cl2u * (1 - bc));
+    I.cl2u_hi = (float)(cl2u * (1 + bc));
+    I.cl2f_lo = (float)(cl2u * (1 - bf));
+    I.cl2f_hi = (float)(cl2u * (1 + bf));
+    I.sl2u_lo = (float)(sl2u * (1 - bs));
+    I.sl2u_hi = (float)(sl2u * (1 + bs));
     I.unit = u;
     I.cell_base = ncells;
     I.offset = off;
@@ -374,12 +383,12 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
       for (const auto& sh : shapes) {
         cudaError_t e = launch_force_batch(tp, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                            b.classrows.ptr + k.first, k.count, prm->dt, cl2,
-                                           sh[0], sh[1], sh[2] != 0, s);
+                                           sh[0], sh[1], sh[2] != 0, ff, s);
         cudaEventRecord(e0, s);
         for (int rep = 0; rep < 3 && e == cudaSuccess; rep++)
           e = launch_force_batch(tp, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                  b.classrows.ptr + k.first, k.count, prm->dt, cl2, sh[0], sh[1],
-                                 sh[2] != 0, s);
+                                 sh[2] != 0, ff, s);
         cudaEventRecord(e1, s);
         if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
           cudaEventDestroy(e0);
@@ -416,7 +425,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if ((e = batch_rebuild(b, q, sl2, s))) return e;
-    return batch_kick(b, part, cls, kick_dt, cl2, s);
+    return batch_kick(b, part, cls, kick_dt, cl2, ff, s);
   };
   int32_t nrec = 0;
   auto record = [&](int64_t stepno) -> int {
@@ -471,7 +480,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     if (ce != cudaSuccess) return lj_fail(ctx, LJ_ERR_CUDA, "graph instantiate");
   }
   const int every = prm->record_every > 0 ? prm->record_every : nsteps;
-  if (nsteps > 0) B_CUDA(ctx, batch_kick(b, part, cls, 0.5 * prm->dt, cl2, s), "kick");
+  if (nsteps > 0) B_CUDA(ctx, batch_kick(b, part, cls, 0.5 * prm->dt, cl2, ff, s), "kick");
   int64_t done = 0;
   while (done < nsteps) {
     const int64_t stop = std::min<int64_t>(nsteps, (done / every + 1) * every);
@@ -487,7 +496,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
       return lj_fail(ctx, LJ_ERR_LIST_OVERFLOW, "a neighbour row exceeded %d entries", b.maxrow);
     if (stop % every == 0 || stop == nsteps)
       if ((rc = record(stop))) return rc;
-    if (stop < nsteps) B_CUDA(ctx, batch_kick(b, part, cls, 0.5 * prm->dt, cl2, s), "kick");
+    if (stop < nsteps) B_CUDA(ctx, batch_kick(b, part, cls, 0.5 * prm->dt, cl2, ff, s), "kick");
     done = stop;
   }
   B_CUDA(ctx, cudaEventRecord(t1, s), "event");

@@ -68,7 +68,8 @@ bool pow2_lanes(int v) { return v == 1 || v == 2 || v == 4 || v == 8 || v == 16 
 
 int check_opts(lj_ctx* ctx, const lj_force_opts* o) {
   if (!o) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "opts is NULL");
-  if (!(o->precision == LJ_PREC_FP64 || o->precision == LJ_PREC_MIXED))
+  if (!(o->precision == LJ_PREC_FP64 || o->precision == LJ_PREC_MIXED ||
+        o->precision == LJ_PREC_MIXED_FP32))
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown precision %d", o->precision);
   if (o->method < LJ_METHOD_AUTO || o->method > LJ_METHOD_SCATTER_HALF)
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown method %d", o->method);
@@ -109,7 +110,7 @@ Periodic make_periodic(const lj_force_opts* o) {
 //   FP64 gather   : kernel 2 (compacted, one warp per row)
 int default_lanes(int precision, int method, int kernel, int64_t entries, int n) {
   const double avg = n > 0 ? (double)entries / n : 0.0;
-  if (kernel >= 2 && precision == LJ_PREC_MIXED) return avg <= 24 ? 2 : 4;
+  if (kernel >= 2 && precision != LJ_PREC_FP64) return avg <= 24 ? 2 : 4;
   if (precision == LJ_PREC_FP64 && method == LJ_METHOD_SCATTER_HALF) return avg <= 12 ? 2 : 4;
   if (avg <= 12) return 2;
   if (avg <= 24) return 4;
@@ -339,14 +340,16 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
   L.cl2 = o->cl2;
   L.precision = o->precision;
   L.method = method;
-  const bool tiled_ok = ctx->tiled.valid && o->precision == LJ_PREC_MIXED &&
+  const bool mixed = o->precision != LJ_PREC_FP64;
+  // The cell-tiled gather (kernel 3, FP32 pair terms only) runs only when
+  // asked for or chosen by lj_autotune_aos; it needs the tiled rows
+  // lj_list_build leaves behind.
+  const bool tiled_ok = ctx->tiled.valid && o->precision == LJ_PREC_MIXED_FP32 &&
                         method == LJ_METHOD_GATHER_FULL && ctx->full.n == n;
-  // The cell-tiled gather (kernel 3) runs only when asked for or chosen by
-  // lj_autotune_aos; it needs the tiled rows lj_list_build leaves behind.
   L.kernel = o->kernel ? o->kernel : 2;  // unrolled gather / scatter (mixed), compacted (FP64)
   if (L.kernel == 3 && !tiled_ok) L.kernel = 2;  // no tiled list: unrolled gather
-  if (L.kernel == 4 && !(o->precision == LJ_PREC_MIXED && method == LJ_METHOD_GATHER_FULL &&
-                         ctx->full.avalid && ctx->full.n == n))
+  if (L.kernel == 4 && !(mixed && method == LJ_METHOD_GATHER_FULL && ctx->full.avalid &&
+                         ctx->full.n == n))
     L.kernel = 2;  // no aligned copy: scalar index loads
   // the mixed scatter has kernels 1 (simple) and 2 (unrolled, vector atomics)
   if (L.kernel > 2 && method == LJ_METHOD_SCATTER_HALF) L.kernel = 2;
@@ -355,6 +358,9 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kernel 4 takes 4 entries per lane (unroll 0 or 4)");
   if (L.kernel == 2 && !(L.unroll == 1 || L.unroll == 2 || L.unroll == 4 || L.unroll == 8))
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be 1, 2, 4 or 8");
+  if (o->precision == LJ_PREC_MIXED && (L.kernel == 2 || method == LJ_METHOD_SCATTER_HALF) &&
+      !(L.unroll == 2 || L.unroll == 4))
+    return fail(ctx, LJ_ERR_UNSUPPORTED, "two-float pair terms take unroll 2 or 4");
   if (L.kernel == 3 && !(L.unroll == 2 || L.unroll == 4))
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be 2 or 4 for kernel 3");
   L.lanes = o->lanes ? o->lanes : default_lanes(o->precision, method, L.kernel, l.entries, l.n);
@@ -364,23 +370,30 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
   }
   L.block = o->block ? o->block : 128;
   if (n == 0) return LJ_OK;
-  const bool fixed = o->precision == LJ_PREC_MIXED || L.kernel == 2;
+  const bool fixed = mixed || L.kernel == 2;
   cudaEvent_t* tv = timing_slot(ctx);
   if (tv) LJ_CUDA(ctx, cudaEventRecord(tv[0], ctx->stream), "event");
   if (fixed) {
     LJ_CUDA(ctx, ctx->qfix.ensure((size_t)n), "alloc");
     L.qfix = ctx->qfix.ptr;
     if (!L.box.on) {
-      // the fixed-point frame of an open box follows the largest |coordinate|;
-      // the kernels read it on the device (no host round trip per call)
-      LJ_CUDA(ctx, ctx->maxabs.ensure(1), "alloc");
-      LJ_CUDA(ctx, launch_max_abs(part, n, ctx->maxabs.ptr, ctx->stream), "max_abs");
-      make_device_frame(L, reinterpret_cast<const unsigned long long*>(ctx->maxabs.ptr));
+      // the fixed-point frame of an open box follows the per-axis bounds of
+      // the coordinates; the kernels read it on the device (no host round
+      // trip per call)
+      LJ_CUDA(ctx, ctx->oframe.ensure(kOpenFrameWords), "alloc");
+      if (!ctx->oframe_armed) {
+        LJ_CUDA(ctx, launch_open_frame_init(ctx->oframe.ptr, ctx->stream), "frame init");
+        ctx->oframe_armed = true;
+      }
+      LJ_CUDA(ctx, launch_open_bounds(part, n, ctx->oframe.ptr, ctx->stream), "bounds");
+      make_device_frame(L, ctx->oframe.ptr);
     } else {
-      make_fixed_frame(L, 0.0);
+      make_fixed_frame(L);
     }
-    if (o->precision == LJ_PREC_MIXED && method == LJ_METHOD_SCATTER_HALF) {
-      LJ_CUDA(ctx, ctx->fscratch.ensure(4 * (size_t)n), "alloc");
+    if (mixed && method == LJ_METHOD_SCATTER_HALF) {
+      // one float4 per particle (FP32 terms) or two (two-float terms)
+      const size_t per = o->precision == LJ_PREC_MIXED ? 8 : 4;
+      LJ_CUDA(ctx, ctx->fscratch.ensure(per * (size_t)n), "alloc");
       L.fscratch = ctx->fscratch.ptr;
       L.scratch_zeroed = 1;  // the image pass below clears it
     }
@@ -884,7 +897,7 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
   F.part.soa = 0;
   F.part.q = q;
   F.csr.n = n;
-  double max_abs = 0.0;
+  double open_lo[3] = {0, 0, 0}, open_hi[3] = {0, 0, 0};
   if (box) {
     g.periodic = 1;
     for (int d = 0; d < 3; d++) {
@@ -915,7 +928,8 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
         lo[d] = key_to_double(~k6[3 + d]);
         if (!std::isfinite(lo[d]) || !std::isfinite(hi[d]))
           return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "non-finite position");
-        max_abs = std::max(max_abs, std::max(std::fabs(lo[d]), std::fabs(hi[d])));
+        open_lo[d] = lo[d];
+        open_hi[d] = hi[d];
       }
     }
     // at most ~2 n cells overall, every side >= rs
@@ -928,7 +942,14 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
     }
   }
   g.ncells = g.nc[0] * g.nc[1] * g.nc[2];
-  make_fixed_frame(F, max_abs);
+  make_fixed_frame(F);
+  if (!box && n > 0) {
+    // the open frame the force calls choose on the device, for these bounds
+    int kf;
+    long long org[3];
+    host_open_frame(open_lo, open_hi, &kf, org);
+    make_open_frame(F, kf, org);
+  }
   LJ_CUDA(ctx, ctx->qfix.ensure((size_t)std::max(n, 1)), "alloc");
   F.qfix = ctx->qfix.ptr;
   LJ_CUDA(ctx, ctx->b_cell.ensure((size_t)n), "alloc");
@@ -1082,17 +1103,19 @@ int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts
   // candidate launch shapes
   struct Cand { int method, kernel, lanes, unroll, block; };
   std::vector<Cand> cands;
-  const bool mixed = opts->precision == LJ_PREC_MIXED;
+  const bool mixed = opts->precision != LJ_PREC_FP64;
+  const bool ff = opts->precision == LJ_PREC_MIXED;  // two-float pair terms
   const bool try_gather = ctx->full.valid && opts->method != LJ_METHOD_SCATTER_HALF;
   const bool try_scatter = ctx->half.valid && opts->method != LJ_METHOD_GATHER_FULL;
   for (int block : {128, 256}) {
     if (try_gather) {
       if (mixed) {
-        if (ctx->tiled.valid && block == 128)
+        if (!ff && ctx->tiled.valid && block == 128)
           for (int g : {2, 4, 8})
             for (int u : {2, 4}) cands.push_back({LJ_METHOD_GATHER_FULL, 3, g, u, 128});
         for (int g : {2, 4, 8})
-          for (int u : {2, 4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 2, g, u, block});
+          for (int u : {2, 4, 8})
+            if (!(ff && u == 8)) cands.push_back({LJ_METHOD_GATHER_FULL, 2, g, u, block});
         if (ctx->full.avalid)
           for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 4, g, 4, block});
         for (int g : {4, 8, 16}) cands.push_back({LJ_METHOD_GATHER_FULL, 1, g, 0, block});
@@ -1107,7 +1130,8 @@ int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts
       if (mixed)
         for (int g : {2, 4, 8})
           for (int u : {2, 4}) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, g, u, block});
-      for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_SCATTER_HALF, 1, g, 0, block});
+      if (!ff)  // two-float scatters always run kernel 2
+        for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_SCATTER_HALF, 1, g, 0, block});
     }
   }
   if (cands.empty()) return fail(ctx, LJ_ERR_NO_LIST, "no list for the requested method");

@@ -7,9 +7,9 @@
 //     comparisons are done on the IEEE bit patterns with integer compares and
 //     the division is a Newton-Raphson reciprocal seeded by the FP32 MUFU.
 //   * The mixed kernels never touch FP64 per pair: positions are read from a
-//     32-bit fixed-point image (see to_fixed), so the minimum image is plain
-//     two's-complement wrap-around and dx is exact before its one rounding to
-//     FP32.
+//     42-bit fixed-point image (see pack_image), so the minimum image is plain
+//     two's-complement wrap-around and dx is exact, as an integer, before
+//     any floating-point rounding.
 #pragma once
 
 #include <cstdint>
@@ -73,34 +73,37 @@ __device__ __forceinline__ bool rcp_fp64_in_range(double r2) {
 
 // ---------------------------------------------------------------------------
 // Fixed-point position frame for the mixed path.
-//   periodic: X = floor(x * 2^32 / L) mod 2^32, so (Xj - Xi) as int32 is the
-//             minimum-image separation in units of L / 2^32 -- wrap-around
-//             int32 arithmetic does the minimum image exactly;
-//   open:     X = trunc(x * 2^k), with 2^k chosen on the host from the largest
-//             |coordinate| so that every |Xj - Xi| < 2^31 (nothing wraps).
+//
+// Every coordinate is held as a 42-bit fixed-point number X (fine units).
+// The position image of a particle is one int4:
+//   x, y, z: X >> 10 per axis (32-bit "coarse" units), w: the three low
+//   10-bit fields, X & 1023 of x in bits 0-9, of y in bits 10-19, of z in
+//   bits 20-29.
+// Coarse-only consumers (list builders, FP32 screening, the FP32 pair
+// kernels) read x, y, z; the two-float pair kernels also read w.
+//
+//   periodic: X = floor(x * 2^42 / L) mod 2^42, so the coarse difference
+//             (Xj - Xi) >> 10 taken as wrapping int32 is the minimum-image
+//             separation in units of L / 2^32, and adding the difference of
+//             the low fields gives it in units of L / 2^42;
+//   open:     X = trunc(x 2^kf) - trunc(o 2^kf) with o the per-axis minimum
+//             coordinate and 2^kf chosen from the largest per-axis extent
+//             (open_frame_kf), so X stays within [-1, 2^40 + 1] and the
+//             quantum follows the system's size, not its distance from the
+//             origin.
 // The conversion is done with integer instructions only: x = m 2^(E-1075),
-// scale = mult 2^-sigma with mult in [2^63, 2^64), and X is 32 bits of the
-// 128-bit product m * mult taken at bit 1075 + sigma - E.
+// scale = mult 2^-sigma with mult in [2^63, 2^64), and X is 64 bits of the
+// 128-bit product m * mult taken at bit 1075 + sigma - E - 10.
 // ---------------------------------------------------------------------------
 struct FixedAxis {
-  unsigned long long mult;  // scale mantissa, top bit set
-  int sigma;                // scale = mult * 2^-sigma
+  unsigned long long mult;  // coarse scale mantissa, top bit set
+  int sigma;                // coarse scale = mult * 2^-sigma (fine = coarse * 2^10)
   int pad;
 };
 
-// Open boxes: exponent k of the fixed-point scale 2^k chosen from the largest
-// |coordinate| (key: its IEEE bits, as k_max_abs leaves them): |x| < 2^e and
-// k = 30 - e keep |X| <= 2^30, so every difference fits in int32.  k is held
-// in [-60, 50] so the FP32 pair constants (which scale by 2^2k) stay finite
-// and normal.  Must equal the host's choice in make_fixed_frame.
-__host__ __device__ __forceinline__ int open_frame_exp(unsigned long long key) {
-  const int be = (int)((key >> 52) & 0x7ffull);
-  const int e = key == 0ull ? 1 : (be == 0 ? -1021 : be - 1022);  // frexp exponent
-  const int k = 30 - e;
-  return k < -60 ? -60 : (k > 50 ? 50 : k);
-}
+constexpr int kFineBits = 10;  // fine units per coarse unit: 2^10
 
-// The axis of scale 2^k (mult 2^63, sigma 63 - k).
+// The coarse axis of scale 2^k (mult 2^63, sigma 63 - k).
 __host__ __device__ __forceinline__ FixedAxis pow2_axis(int k) {
   FixedAxis a;
   a.mult = 1ull << 63;
@@ -109,21 +112,102 @@ __host__ __device__ __forceinline__ FixedAxis pow2_axis(int k) {
   return a;
 }
 
-__device__ __forceinline__ int to_fixed(double x, const FixedAxis& ax) {
+// 64 bits of the 128-bit product m * mult starting at bit sh (0 beyond it).
+__device__ __forceinline__ unsigned long long prod_bits(unsigned long long m,
+                                                        unsigned long long mult, int sh) {
+  const unsigned long long lo = m * mult;
+  const unsigned long long hi = __umul64hi(m, mult);
+  if (sh >= 128) return 0ull;
+  if (sh >= 64) return hi >> (sh - 64);
+  if (sh > 0) return (lo >> sh) | (hi << (64 - sh));
+  if (sh > -64) return lo << (-sh);
+  return 0ull;
+}
+
+// x in fine units, truncated toward zero, as a wrapping 64-bit integer.
+__device__ __forceinline__ long long to_fixed_fine(double x, const FixedAxis& ax) {
   const unsigned long long b = (unsigned long long)dbits(x);
   const int e = (int)((b >> 52) & 0x7ffull);
   unsigned long long m = b & 0x000fffffffffffffull;
   if (e != 0) m |= 0x0010000000000000ull;
-  const int sh = 1075 + ax.sigma - (e != 0 ? e : 1);
-  const unsigned long long lo = m * ax.mult;
-  const unsigned long long hi = __umul64hi(m, ax.mult);
-  unsigned v;
-  if (sh >= 128) v = 0u;
-  else if (sh >= 64) v = (unsigned)(hi >> (sh - 64));
-  else if (sh > 0) v = (unsigned)((lo >> sh) | (hi << (64 - sh)));
-  else if (sh > -32) v = (unsigned)(lo << (-sh));
-  else v = 0u;
-  return (b >> 63) ? -(int)v : (int)v;
+  const int sh = 1075 + ax.sigma - (e != 0 ? e : 1) - kFineBits;
+  const unsigned long long v = prod_bits(m, ax.mult, sh);
+  return (b >> 63) ? (long long)(0ull - v) : (long long)v;
+}
+
+// The image int4 of three fine coordinates.
+__device__ __forceinline__ int4 pack_image(long long X, long long Y, long long Z) {
+  const unsigned w = ((unsigned)X & 1023u) | (((unsigned)Y & 1023u) << 10) |
+                     (((unsigned)Z & 1023u) << 20);
+  return make_int4((int)(X >> kFineBits), (int)(Y >> kFineBits), (int)(Z >> kFineBits), (int)w);
+}
+
+// Coarse coordinate only (32 bits of the fine value above the low field).
+__device__ __forceinline__ int to_fixed(double x, const FixedAxis& ax) {
+  return (int)(to_fixed_fine(x, ax) >> kFineBits);
+}
+
+// ---------------------------------------------------------------------------
+// Relative half-width of the band around a cutoff (or search) sphere inside
+// which an FP32 comparison of r2 is not trusted and the pair is re-decided
+// in FP64: `base` (rounding of the FP32 r2 and of the band edges) plus the
+// largest r2 error the position quantum allows, |dr2| <= 2 sqrt(3) rc q +
+// 3 q^2 for a separation error of at most q per axis, relative to rc^2.
+// rc and q are in the same units (coarse fixed units, or lengths).
+__host__ __device__ __forceinline__ double cutoff_band(double rc, double q, double base) {
+  if (!(rc > 0.0)) return base;
+  return base + (3.4641016151377544 * rc * q + 3.0 * q * q) / (rc * rc);
+}
+constexpr double kBandFp32 = 4e-6;  // FP32 r2 from rounded FP32 separations
+constexpr double kBandFF = 6e-7;    // two-float r2 rounded to float vs float edges
+// separation error per axis of the coarse image (X >> 10 of both ends), in
+// coarse units; the fine image's is kCoarseQuantumErr / 1024
+constexpr double kCoarseQuantumErr = 2.0;
+
+// ---------------------------------------------------------------------------
+// Open-box frame chosen on the device.  A bounds pass (k_open_bounds) folds
+// every coordinate into per-axis min / max keys; its last block turns them
+// into the frame below, in the same device words, and re-arms the keys for
+// the next call.  Word layout (kOpenFrameWords x 8 bytes):
+//   [0..2] min keys, [3..5] max keys (order-preserving u64 of the doubles),
+//   [6] blocks done, [8] fine exponent kf, [9..11] origin per axis in fine
+//   units (trunc(min_a 2^kf)).
+// ---------------------------------------------------------------------------
+constexpr int kOpenFrameWords = 16;
+constexpr int kOfMin = 0, kOfMax = 3, kOfDone = 6, kOfExp = 8, kOfOrigin = 9;
+
+// Order-preserving map of a double's bits to u64 (and back).
+__host__ __device__ __forceinline__ unsigned long long order_key(unsigned long long b) {
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ __forceinline__ unsigned long long order_unkey(unsigned long long k) {
+  return (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+}
+
+// frexp exponent of |v| from its bits (v = f 2^e, f in [0.5, 1)); 1 for zero
+// and for non-finite values a large exponent.
+__host__ __device__ __forceinline__ int frexp_exp_bits(unsigned long long b) {
+  const int be = (int)((b >> 52) & 0x7ffull);
+  if ((b & 0x7fffffffffffffffull) == 0ull) return 1;
+  if (be == 0x7ff) return 2000;
+  return be == 0 ? -1021 : be - 1022;
+}
+
+// Fine exponent kf of an open frame from the largest |coordinate| (bits
+// amax_bits) and the largest per-axis extent (bits ext_bits, max - min, an
+// extent below 2^e_ext).  kf = 40 - e_ext keeps every origin-relative X in
+// [-1, 2^40 + 1] after truncation, so coarse differences (X >> 10) stay
+// within +-(2^30 + 1) (int32, and exact as floats once their low 8 bits are
+// cleared); |x| 2^kf < 2^61 keeps the 64-bit conversion exact.  kf is held
+// in [-20, 60] so the FP32 pair constants, which scale by 2^(2 (kf - 10)),
+// stay finite and normal.
+__host__ __device__ __forceinline__ int open_frame_kf(unsigned long long amax_bits,
+                                                      unsigned long long ext_bits) {
+  const int e_ext = frexp_exp_bits(ext_bits);
+  const int e_abs = frexp_exp_bits(amax_bits);
+  int kf = 40 - e_ext;
+  if (kf > 61 - e_abs) kf = 61 - e_abs;
+  return kf < -20 ? -20 : (kf > 60 ? 60 : kf);
 }
 
 // Periodic wrap of a coordinate into [0, len) with one shift and one FP64

@@ -83,7 +83,9 @@ struct lj_ctx {
   // scratch
   ljg::DevBuf<int4> qfix;
   ljg::DevBuf<float> fscratch;
-  ljg::DevBuf<double> maxabs;
+  // open-box frame words (kOpenFrameWords), armed once by k_open_frame_init
+  ljg::DevBuf<long long> oframe;
+  bool oframe_armed = false;
   ljg::DevBuf<int32_t> err2;
   ljg::DevBuf<int32_t> tmp_i32a, tmp_i32b;
   ljg::DevBuf<int64_t> tmp_off;

@@ -1,1198 +1,11 @@
-// lj_force.cu -- Lennard-Jones neighbour-list force kernels for sm_103a.
-//
-// One force call is the kick p_i += sum_j df(r_ij) (q_j - q_i) with
-// df = (24 r^-8 - 48 r^-14) dt for r2 <= cl2, the arithmetic of
-// cpu_ref/force_aos.cpp:206-218 and cuda/kernel.cuh:22-31.
-//
-// Work mapping: a group of G lanes (G = 1..32, a power of two) owns one
-// i-particle and strides through its CSR row; the group's partial sums are
-// combined with xor shuffles (the role of warp_segment_reduce,
-// cuda/device_util.cuh:12-19, generalised to sub-warp groups).
-//
-//   FP64 gather (full list):   row sums only, one plain RMW of p_i.
-//   FP64 scatter (half list):  p_j -= f with RED.F64, p_i += row sum with one
-//                              atomic per row (the _with_aar kernels).
-//   mixed gather / scatter:    positions from the 32-bit fixed image, FP32
-//                              pair math with Kahan-compensated sums, FP64
-//                              only in the final p += F dt.
-#include <cfloat>
-#include <cmath>
-#include <cstring>
-#include <type_traits>
-
-#include "lj_cells.cuh"
-#include "lj_gb300.h"
-#include "lj_internal.h"
+// lj_force.cu -- force-call entry of the kernels in lj_force_kernels.cuh:
+// frames and position images, the FP64 force paths, force_pair, and the
+// dispatch of the mixed paths to their own translation units.
+#include "lj_force_kernels.cuh"
 
 namespace ljg {
-namespace {
 
-// ---------------------------------------------------------------------------
-// particle access
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ size_t rec(const Particles& P, int i) {
-  return (size_t)i * (size_t)(P.stride ? P.stride : 4);
-}
-
-template <bool SOA>
-__device__ __forceinline__ double3 load_q(const Particles& P, int i) {
-  if (SOA) return make_double3(__ldg(P.qx + i), __ldg(P.qy + i), __ldg(P.qz + i));
-  const double* b = P.q + rec(P, i);
-  const double2 xy = __ldg(reinterpret_cast<const double2*>(b));
-  return make_double3(xy.x, xy.y, __ldg(b + 2));
-}
-
-template <bool SOA>
-__device__ __forceinline__ void add_p(const Particles& P, int i, double fx, double fy,
-                                      double fz) {
-  if (SOA) {
-    P.px[i] += fx;
-    P.py[i] += fy;
-    P.pz[i] += fz;
-  } else {
-    double* b = P.p + rec(P, i);
-    double2 xy = *reinterpret_cast<double2*>(b);
-    xy.x += fx;
-    xy.y += fy;
-    *reinterpret_cast<double2*>(b) = xy;
-    b[2] += fz;
-  }
-}
-
-// p_i[axis] += v (one component; several lanes may each apply one).
-template <bool SOA>
-__device__ __forceinline__ void add_p_axis(const Particles& P, int i, int axis, double v) {
-  double* a;
-  if (SOA) a = (axis == 0 ? P.px : (axis == 1 ? P.py : P.pz)) + i;
-  else a = P.p + rec(P, i) + axis;
-  *a += v;
-}
-
-// Sums x, y and z over the 32 lanes of a warp with 6 FP64 adds instead of
-// 15 (the FP64 pipe charges every warp instruction in full).  The halves of
-// the warp split the components as the sums narrow: after the offset-16 step
-// the lower half carries x and y and the upper half z, after the offset-8
-// step lanes with bit 3 clear carry x and the others y.  Returns this lane's
-// total: x in lanes 0-7, y in lanes 8-15, z in lanes 16-31.
-__device__ __forceinline__ double warp_reduce3_fp64(double x, double y, double z, int lane) {
-  const bool up = (lane & 16) != 0, b3 = (lane & 8) != 0;
-  double s1 = up ? z : x, s2 = up ? 0.0 : y;
-  const double o1 = up ? x : z, o2 = up ? y : 0.0;
-  s1 += __shfl_xor_sync(kFullMask, o1, 16);
-  s2 += __shfl_xor_sync(kFullMask, o2, 16);
-  double keep = (up || !b3) ? s1 : s2;
-  const double send = (up || b3) ? s1 : s2;
-  keep += __shfl_xor_sync(kFullMask, send, 8);
-#pragma unroll
-  for (int off = 4; off > 0; off >>= 1) keep += __shfl_xor_sync(kFullMask, keep, off);
-  return keep;
-}
-
-// v * 2^k exactly, by adding k to the exponent field: integer instructions
-// only (FP64 issue is scarce on this part).  Zero, subnormal, inf/NaN and
-// results that would leave the normal range take ldexp.
-__device__ __forceinline__ double scale_pow2(double v, int k) {
-  const long long b = __double_as_longlong(v);
-  const int e = (int)((b >> 52) & 0x7ff);
-  if (e == 0 || e == 0x7ff || e + k <= 0 || e + k >= 0x7ff) return ldexp(v, k);
-  return __longlong_as_double(b + (long long)k * (1ll << 52));
-}
-
-// p_i = fma(f, s, p_i) per component: the single FP64 operation the mixed
-// path spends per particle and axis (s scaled by 2^fexp when fexp != 0).
-template <bool SOA>
-__device__ __forceinline__ void kick_p(const Particles& P, int i, double fx, double fy,
-                                       double fz, const double* s, int fexp = 0) {
-  double s0 = s[0], s1 = s[1], s2 = s[2];
-  if (fexp) {
-    s0 = scale_pow2(s0, fexp);
-    s1 = scale_pow2(s1, fexp);
-    s2 = scale_pow2(s2, fexp);
-  }
-  if (SOA) {
-    P.px[i] = fma(fx, s0, P.px[i]);
-    P.py[i] = fma(fy, s1, P.py[i]);
-    P.pz[i] = fma(fz, s2, P.pz[i]);
-  } else {
-    double* b = P.p + rec(P, i);
-    double2 xy = *reinterpret_cast<double2*>(b);
-    xy.x = fma(fx, s0, xy.x);
-    xy.y = fma(fy, s1, xy.y);
-    *reinterpret_cast<double2*>(b) = xy;
-    b[2] = fma(fz, s2, b[2]);
-  }
-}
-
-// The kick of a gather row whose G lanes all hold the compensated sums
-// (hi, lo) per axis.  With G >= 4 lanes 0, 1, 2 each apply one axis: one
-// FP64 FMA instruction per warp instead of three (FP64 issue is charged per
-// warp instruction, whatever the active lanes), with the same per-axis
-// arithmetic as kick_p.
-template <bool SOA, int G>
-__device__ __forceinline__ void kick_group(const Particles& P, int i, int lane, bool valid,
-                                           float hx, float lx, float hy, float ly, float hz,
-                                           float lz, const double* s, int fexp) {
-  if (G < 4) {
-    if (valid && lane == 0) kick_p<SOA>(P, i, widen_f32(hx + lx), widen_f32(hy + ly),
-                                        widen_f32(hz + lz), s, fexp);
-    return;
-  }
-  if (!valid || lane > 2) return;
-  const float v = lane == 0 ? hx + lx : (lane == 1 ? hy + ly : hz + lz);
-  double sc = lane == 0 ? s[0] : (lane == 1 ? s[1] : s[2]);
-  if (fexp) sc = scale_pow2(sc, fexp);
-  double* a;
-  if (SOA) a = (lane == 0 ? P.px : (lane == 1 ? P.py : P.pz)) + i;
-  else a = P.p + rec(P, i) + lane;
-  *a = fma(widen_f32(v), sc, *a);
-}
-
-template <bool SOA>
-__device__ __forceinline__ void red_p(const Particles& P, int i, double fx, double fy,
-                                      double fz) {
-  if (SOA) {
-    atomicAdd(P.px + i, fx);
-    atomicAdd(P.py + i, fy);
-    atomicAdd(P.pz + i, fz);
-  } else {
-    double* b = P.p + rec(P, i);
-    atomicAdd(b + 0, fx);
-    atomicAdd(b + 1, fy);
-    atomicAdd(b + 2, fz);
-  }
-}
-
-__device__ __forceinline__ double flip_sign(double x) {
-  return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
-}
-
-// Constants of one launch, kept in registers / constant bank.
-struct Fp64Consts {
-  double c24, c48;  // 24 dt, 48 dt
-  long long cl2_bits;
-  double len[3];
-  long long half_bits[3];
-};
-
-// Separation q_j - q_i with the minimum image, FP64 (same expression on every
-// path so FP64 and mixed kernels agree on the cutoff mask).
-template <bool PBC>
-__device__ __forceinline__ double3 sep_fp64(const double3& qi, const double3& qj,
-                                            const Fp64Consts& k) {
-  double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
-  if (PBC) {
-    dx = min_image_fp64(dx, k.len[0], k.half_bits[0]);
-    dy = min_image_fp64(dy, k.len[1], k.half_bits[1]);
-    dz = min_image_fp64(dz, k.len[2], k.half_bits[2]);
-  }
-  return make_double3(dx, dy, dz);
-}
-
-__device__ __forceinline__ double r2_fp64(const double3& d) {
-  return fma(d.z, d.z, fma(d.y, d.y, d.x * d.x));
-}
-
-// true when the reference would skip the pair (r2 > CL2); NaN is not skipped,
-// exactly as `if (r2 > CL2) continue;` behaves.
-__device__ __forceinline__ bool beyond_cutoff(double r2, long long cl2_bits) {
-  const long long b = dbits(r2);
-  return b > cl2_bits && b <= 0x7ff0000000000000ll;
-}
-
-// df of the reference formula, with dt folded into the constants.
-__device__ __forceinline__ double df_fp64(double r2, const Fp64Consts& k) {
-  const double inv = rcp_fp64_in_range(r2) ? rcp_fp64(r2) : 1.0 / r2;
-  const double r6 = inv * inv * inv;
-  return (r6 * inv) * fma(-k.c48, r6, k.c24);
-}
-
-// ---------------------------------------------------------------------------
-// FP64 gather over the full list
-// ---------------------------------------------------------------------------
-template <int G, bool PBC, bool SOA>
-__global__ void __launch_bounds__(256) k_gather_fp64(const Particles P, const Csr C,
-                                                     const Fp64Consts K) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = t / G;
-  const int lane = t & (G - 1);
-  const bool valid = i < C.n;
-  int cnt = 0, k0 = 0;
-  double3 qi = make_double3(0, 0, 0);
-  if (valid) {
-    cnt = __ldg(C.np + i);
-    k0 = __ldg(C.ptr + i);
-    qi = load_q<SOA>(P, i);
-  }
-  double fx = 0.0, fy = 0.0, fz = 0.0;
-  for (int k = lane; k < cnt; k += G) {
-    const int j = __ldg(C.list + k0 + k);
-    const double3 d = sep_fp64<PBC>(qi, load_q<SOA>(P, j), K);
-    const double r2 = r2_fp64(d);
-    if (beyond_cutoff(r2, K.cl2_bits)) continue;
-    const double df = df_fp64(r2, K);
-    fx = fma(df, d.x, fx);
-    fy = fma(df, d.y, fy);
-    fz = fma(df, d.z, fz);
-  }
-  if (G > 1) {
-    fx = group_reduce_fp64<G>(fx);
-    fy = group_reduce_fp64<G>(fy);
-    fz = group_reduce_fp64<G>(fz);
-  }
-  if (valid && lane == 0) add_p<SOA>(P, i, fx, fy, fz);
-}
-
-// ---------------------------------------------------------------------------
-// FP64 scatter over the half list
-// ---------------------------------------------------------------------------
-template <int G, bool PBC, bool SOA>
-__global__ void __launch_bounds__(256) k_scatter_fp64(const Particles P, const Csr C,
-                                                      const Fp64Consts K) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = t / G;
-  const int lane = t & (G - 1);
-  const bool valid = i < C.n;
-  int cnt = 0, k0 = 0;
-  double3 qi = make_double3(0, 0, 0);
-  if (valid) {
-    cnt = __ldg(C.np + i);
-    k0 = __ldg(C.ptr + i);
-    qi = load_q<SOA>(P, i);
-  }
-  double fx = 0.0, fy = 0.0, fz = 0.0;
-  for (int k = lane; k < cnt; k += G) {
-    const int j = __ldg(C.list + k0 + k);
-    const double3 d = sep_fp64<PBC>(qi, load_q<SOA>(P, j), K);
-    const double r2 = r2_fp64(d);
-    if (beyond_cutoff(r2, K.cl2_bits)) continue;
-    const double ndf = flip_sign(df_fp64(r2, K));
-    const double jx = ndf * d.x, jy = ndf * d.y, jz = ndf * d.z;
-    fx -= jx;
-    fy -= jy;
-    fz -= jz;
-    red_p<SOA>(P, j, jx, jy, jz);
-  }
-  if (G > 1) {
-    fx = group_reduce_fp64<G>(fx);
-    fy = group_reduce_fp64<G>(fy);
-    fz = group_reduce_fp64<G>(fz);
-  }
-  if (valid && lane == 0) red_p<SOA>(P, i, fx, fy, fz);
-}
-
-// ---------------------------------------------------------------------------
-// force_pair on the device: unsorted pair array, both ends by atomics
-// ---------------------------------------------------------------------------
-template <bool PBC>
-__global__ void __launch_bounds__(256) k_pairs_fp64(const Particles P, const int32_t* ip,
-                                                    const int32_t* jp, int64_t npairs,
-                                                    const Fp64Consts K) {
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npairs;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const int i = __ldg(ip + k), j = __ldg(jp + k);
-    const double3 d = sep_fp64<PBC>(load_q<false>(P, i), load_q<false>(P, j), K);
-    const double r2 = r2_fp64(d);
-    if (beyond_cutoff(r2, K.cl2_bits)) continue;
-    const double df = df_fp64(r2, K);
-    const double fx = df * d.x, fy = df * d.y, fz = df * d.z;
-    red_p<false>(P, i, fx, fy, fz);
-    red_p<false>(P, j, flip_sign(fx), flip_sign(fy), flip_sign(fz));
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Mixed precision
-// ---------------------------------------------------------------------------
-struct MixedConsts {
-  float cl2_lo, cl2_hi;  // r2 (pair units) certainly inside / possibly inside
-  float k_hi, k_lo;      // 1/unit^2 split in two floats (isotropic frames)
-  float u_hi[3], u_lo[3];  // per-axis unit split in two floats (anisotropic)
-  double fscale[3];      // unit * dt per axis (isotropic) or dt (anisotropic)
-  int fexp;              // the kick scales by fscale * 2^fexp (device-chosen open frames)
-  Fp64Consts f64;        // for the rare FP64 cutoff decision
-  const unsigned long long* open_key;  // device-chosen open-box frame, see frame_consts
-};
-
-// Constants of the frame in use.  With an open box whose frame is chosen on
-// the device (scale 2^k from the largest |coordinate|), the host built them
-// for k = 0; every frame-dependent one scales exactly by a power of two.
-__device__ __forceinline__ MixedConsts frame_consts(const MixedConsts& K0) {
-  MixedConsts K = K0;
-  if (K0.open_key) {
-    const int k = open_frame_exp(*K0.open_key);
-    K.cl2_lo = ldexpf(K0.cl2_lo, 2 * k);
-    K.cl2_hi = ldexpf(K0.cl2_hi, 2 * k);
-    K.k_hi = ldexpf(K0.k_hi, 2 * k);
-    K.k_lo = ldexpf(K0.k_lo, 2 * k);
-    K.fexp = -k;  // fscale is scaled where the kick reads it
-  }
-  return K;
-}
-
-template <bool SOA>
-__global__ void __launch_bounds__(256) k_fixed_image(const Particles P, int n,
-                                                     FixedAxis ax, FixedAxis ay, FixedAxis az,
-                                                     const unsigned long long* open_key,
-                                                     int4* __restrict__ out,
-                                                     float4* __restrict__ zero_acc) {
-  // the pair kernel that follows may launch now (it waits for this grid)
-  asm volatile("griddepcontrol.launch_dependents;");
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (open_key) ax = ay = az = pow2_axis(open_frame_exp(*open_key));
-  const double3 q = load_q<SOA>(P, i);
-  out[i] = make_int4(to_fixed(q.x, ax), to_fixed(q.y, ay), to_fixed(q.z, az), 0);
-  // the mixed scatter's force accumulator, cleared here instead of by a
-  // separate memset launch
-  if (zero_acc) zero_acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-}
-
-template <bool SOA>
-__global__ void __launch_bounds__(256) k_max_abs(const Particles P, int n,
-                                                 unsigned long long* out) {
-  unsigned long long m = 0ull;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double3 q = load_q<SOA>(P, i);
-    const unsigned long long bx = (unsigned long long)dbits(q.x) & 0x7fffffffffffffffull;
-    const unsigned long long by = (unsigned long long)dbits(q.y) & 0x7fffffffffffffffull;
-    const unsigned long long bz = (unsigned long long)dbits(q.z) & 0x7fffffffffffffffull;
-    m = max(m, max(bx, max(by, bz)));
-  }
-  for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(kFullMask, m, off));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
-}
-
-// Separation in pair units: fixed units (isotropic frame) or length
-// (anisotropic frame, unit applied per axis as a two-float product).
-template <bool ANISO>
-__device__ __forceinline__ float3 sep_mixed(const int4& a, const int4& b,
-                                            const MixedConsts& k) {
-  float dx = (float)wrap_sub(b.x, a.x);
-  float dy = (float)wrap_sub(b.y, a.y);
-  float dz = (float)wrap_sub(b.z, a.z);
-  if (ANISO) {
-    dx = fmaf(dx, k.u_hi[0], dx * k.u_lo[0]);
-    dy = fmaf(dy, k.u_hi[1], dy * k.u_lo[1]);
-    dz = fmaf(dz, k.u_hi[2], dz * k.u_lo[2]);
-  }
-  return make_float3(dx, dy, dz);
-}
-
-// Pair inside the cutoff?  Decided in FP32 away from the cutoff surface; for
-// the few pairs within a relative 4e-6 of it, recomputed in FP64 from the
-// FP64 positions with the FP64 kernels' expression, so the mixed mask is the
-// FP64 mask.
-template <bool PBC, bool SOA>
-__device__ __forceinline__ bool inside_mixed(float r2, const Particles& P, int i, int j,
-                                             const MixedConsts& k) {
-  if (r2 <= k.cl2_lo) return true;
-  if (!(r2 <= k.cl2_hi)) return false;
-  const double3 d = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, j), k.f64);
-  return !beyond_cutoff(r2_fp64(d), k.f64.cl2_bits);
-}
-
-// df / dt in pair units (24 r^-8 - 48 r^-14, r^-2 rescaled by 1/unit^2)
-template <bool ANISO>
-__device__ __forceinline__ float df_mixed(float r2, const MixedConsts& k) {
-  float inv;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
-  inv = fmaf(inv, fmaf(-r2, inv, 1.0f), inv);
-  if (!ANISO) inv = fmaf(inv, k.k_hi, inv * k.k_lo);
-  const float r6 = inv * inv * inv;
-  return (r6 * inv) * fmaf(-48.0f, r6, 24.0f);
-}
-
-template <int G, bool PBC, bool SOA, bool ANISO>
-__global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const Csr C,
-                                                      const int4* __restrict__ qfix,
-                                                      const MixedConsts K0) {
-  // a periodic frame is fixed on the host; an open one may come from the device
-  const MixedConsts K = PBC ? K0 : frame_consts(K0);
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = t / G;
-  const int lane = t & (G - 1);
-  const bool valid = i < C.n;
-  int cnt = 0, k0 = 0;
-  int4 xi = make_int4(0, 0, 0, 0);
-  if (valid) {
-    cnt = __ldg(C.np + i);
-    k0 = __ldg(C.ptr + i);
-    xi = __ldg(qfix + i);
-  }
-  KahanF ax, ay, az;
-  ax.init();
-  ay.init();
-  az.init();
-  for (int k = lane; k < cnt; k += G) {
-    const int j = __ldg(C.list + k0 + k);
-    const float3 d = sep_mixed<ANISO>(xi, __ldg(qfix + j), K);
-    const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-    if (!inside_mixed<PBC, SOA>(r2, P, i, j, K)) continue;
-    const float df = df_mixed<ANISO>(r2, K);
-    ax.add(df * d.x);
-    ay.add(df * d.y);
-    az.add(df * d.z);
-  }
-  float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
-  if (G > 1) {
-    group_reduce_comp<G>(hx, lx);
-    group_reduce_comp<G>(hy, ly);
-    group_reduce_comp<G>(hz, lz);
-  }
-  kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
-}
-
-// Unrolled mixed gather (kernel 2).  The row loop runs to the longest row of
-// the warp, so every lane takes part in every iteration (no divergence, warp
-// votes are safe); each lane issues U independent index loads and U position
-// gathers before any arithmetic, which keeps U x 32 gathers in flight per
-// warp; the next step's indices load while this step's positions are in
-// flight, so the index -> position chain is exposed once per row, not once
-// per step.  Pairs outside the cutoff are masked with a select, not a branch.  The
-// U terms of one step are summed in FP32 and the step sum enters the Kahan
-// accumulator, so compensation costs 12/U operations per pair.
-// Accepts padded rows (C.ptr == nullptr, row i at i * C.stride).  VEC
-// (U == 4, rows on 16-byte boundaries and readable to a multiple of 4): lane
-// l of a row takes the 4 consecutive entries base + 4 l .. + 3 with one
-// 16-byte load, which quarters the index-load instructions and the L1
-// wavefronts they cost (a 32-lane scalar index load touches one line per row).
-template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC = false>
-__global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const Csr C,
-                                                        const int4* __restrict__ qfix,
-                                                        const MixedConsts K0) {
-  static_assert(!VEC || U == 4, "vector index loads take 4 entries per lane");
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = t / G;
-  const int lane = t & (G - 1);
-  // Launched as a programmatic dependent of the image pass: nothing the
-  // stream wrote before may be read until the preceding grid has finished.
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  // a periodic frame is fixed on the host; an open one may come from the device
-  const MixedConsts K = PBC ? K0 : frame_consts(K0);
-  const bool valid = i < C.n;
-  int cnt = 0;
-  int64_t k0 = 0;
-  int4 xi = make_int4(0, 0, 0, 0);
-  if (valid) {
-    cnt = __ldg(C.np + i);
-    k0 = row_start(C, i);
-    xi = __ldg(qfix + i);
-  }
-  int cmax = cnt;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
-  KahanF ax, ay, az;
-  ax.init();
-  ay.init();
-  az.init();
-  // entry of step `base` taken by (lane, u)
-  auto entry = [&](int base, int u) { return VEC ? base + 4 * lane + u : base + lane + u * G; };
-  auto load_idx = [&](int base, int* jn) {
-    if (VEC) {
-      int4 v = make_int4(0, 0, 0, 0);
-      if (entry(base, 0) < cnt)
-        v = __ldg(reinterpret_cast<const int4*>(C.list + k0 + entry(base, 0)));
-      jn[0] = v.x;
-      jn[1] = v.y;
-      jn[2] = v.z;
-      jn[3] = v.w;
-    } else {
-#pragma unroll
-      for (int u = 0; u < U; u++)
-        jn[u] = entry(base, u) < cnt ? __ldg(C.list + k0 + entry(base, u)) : 0;
-    }
-  };
-  int jn[U];
-  load_idx(0, jn);
-  for (int base = 0; base < cmax; base += G * U) {
-    int jj[U];
-    bool ok[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      ok[u] = entry(base, u) < cnt;
-      jj[u] = ok[u] ? jn[u] : 0;
-    }
-    int4 xj[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
-    load_idx(base + G * U, jn);
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    unsigned border = 0u;
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
-      const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-      const bool in = ok[u] && r2 <= K.cl2_lo;
-      if (ok[u] && r2 > K.cl2_lo && r2 <= K.cl2_hi) border |= 1u << u;
-      float df = df_mixed<ANISO>(r2, K);
-      df = in ? df : 0.0f;
-      sx = fmaf(df, d.x, sx);
-      sy = fmaf(df, d.y, sy);
-      sz = fmaf(df, d.z, sz);
-    }
-    if (__any_sync(kFullMask, border != 0u)) {
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        if (!(border & (1u << u))) continue;
-        const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, jj[u]), K.f64);
-        if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
-        const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
-        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-        const float df = df_mixed<ANISO>(r2, K);
-        sx = fmaf(df, d.x, sx);
-        sy = fmaf(df, d.y, sy);
-        sz = fmaf(df, d.z, sz);
-      }
-    }
-    ax.add(sx);
-    ay.add(sy);
-    az.add(sz);
-  }
-  float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
-  if (G > 1) {
-    group_reduce_comp<G>(hx, lx);
-    group_reduce_comp<G>(hy, ly);
-    group_reduce_comp<G>(hz, lz);
-  }
-  kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
-}
-
-// Batched mixed gather: as k_gather_mixed_u, with every constant that depends
-// on the box (unit, cutoff in fixed units, FP64 image shift) read per row
-// from the row's replica.  Groups walk the row list of one size class.
-template <int G, int U, bool VEC>
-__global__ void __launch_bounds__(256) k_gather_mixed_batch(
-    const Particles P, const Csr C, const int4* __restrict__ qfix, const int32_t* __restrict__ rid,
-    const ReplicaInfo* __restrict__ reps, const int32_t* __restrict__ rows, int nrows, double dt,
-    long long cl2_bits) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int g = t / G;
-  const int lane = t & (G - 1);
-  const bool valid = g < nrows;
-  int cnt = 0, i = 0, r = 0;
-  int64_t k0 = 0;
-  int4 xi = make_int4(0, 0, 0, 0);
-  // only the constants of the pair loop are held in registers; the rare FP64
-  // cutoff decision and the kick read the replica table where they need it
-  MixedConsts K{};
-  if (valid) {
-    i = __ldg(rows + g);
-    cnt = __ldg(C.np + i);
-    k0 = row_start(C, i);
-    xi = __ldg(qfix + i);
-    r = __ldg(rid + i);
-    const ReplicaInfo& R = reps[r];
-    K.k_hi = R.k_hi;
-    K.k_lo = R.k_lo;
-    K.cl2_lo = R.cl2u_lo;
-    K.cl2_hi = R.cl2u_hi;
-  }
-  int cmax = cnt;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
-  KahanF ax, ay, az;
-  ax.init();
-  ay.init();
-  az.init();
-  static_assert(!VEC || U == 4, "vector index loads take 4 entries per lane");
-  // entry of step `base` taken by (lane, u); VEC as in k_gather_mixed_u
-  auto entry = [&](int base, int u) { return VEC ? base + 4 * lane + u : base + lane + u * G; };
-  auto load_idx = [&](int base, int* jn) {
-    if (VEC) {
-      int4 v = make_int4(0, 0, 0, 0);
-      if (entry(base, 0) < cnt)
-        v = __ldg(reinterpret_cast<const int4*>(C.list + k0 + entry(base, 0)));
-      jn[0] = v.x;
-      jn[1] = v.y;
-      jn[2] = v.z;
-      jn[3] = v.w;
-    } else {
-#pragma unroll
-      for (int u = 0; u < U; u++)
-        jn[u] = entry(base, u) < cnt ? __ldg(C.list + k0 + entry(base, u)) : 0;
-    }
-  };
-  int jn[U];
-  load_idx(0, jn);
-  for (int base = 0; base < cmax; base += G * U) {
-    int jj[U];
-    bool ok[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      ok[u] = entry(base, u) < cnt;
-      jj[u] = ok[u] ? jn[u] : 0;
-    }
-    int4 xj[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
-    load_idx(base + G * U, jn);
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    unsigned border = 0u;
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const float3 d = sep_mixed<false>(xi, xj[u], K);
-      const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-      const bool in = ok[u] && r2 <= K.cl2_lo;
-      if (ok[u] && r2 > K.cl2_lo && r2 <= K.cl2_hi) border |= 1u << u;
-      float df = df_mixed<false>(r2, K);
-      df = in ? df : 0.0f;
-      sx = fmaf(df, d.x, sx);
-      sy = fmaf(df, d.y, sy);
-      sz = fmaf(df, d.z, sz);
-    }
-    if (__any_sync(kFullMask, border != 0u)) {
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        if (!(border & (1u << u))) continue;
-        const ReplicaInfo& R = reps[r];
-        Fp64Consts f64{};
-        f64.cl2_bits = cl2_bits;
-        for (int d = 0; d < 3; d++) {
-          f64.len[d] = R.len[d];
-          f64.half_bits[d] = R.half_bits[d];
-        }
-        const double3 d64 = sep_fp64<true>(load_q<false>(P, i), load_q<false>(P, jj[u]), f64);
-        if (beyond_cutoff(r2_fp64(d64), cl2_bits)) continue;
-        const float3 d = sep_mixed<false>(xi, xj[u], K);
-        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-        const float df = df_mixed<false>(r2, K);
-        sx = fmaf(df, d.x, sx);
-        sy = fmaf(df, d.y, sy);
-        sz = fmaf(df, d.z, sz);
-      }
-    }
-    ax.add(sx);
-    ay.add(sy);
-    az.add(sz);
-  }
-  float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
-  if (G > 1) {
-    group_reduce_comp<G>(hx, lx);
-    group_reduce_comp<G>(hy, ly);
-    group_reduce_comp<G>(hz, lz);
-  }
-  const double kf = valid ? reps[r].unit * dt : 0.0;
-  const double fs[3] = {kf, kf, kf};
-  kick_group<false, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, fs, 0);
-}
-
-// Cell-tiled mixed gather (kernel 3).  One CTA per cell: it copies the
-// fixed-point positions of its (up to 27) neighbour cells -- contiguous runs of
-// the cell-ordered image -- into shared memory, then walks the rows of its
-// own particles, whose entries are 16-bit indices into that tile.  Every
-// position a pair needs is read from shared memory; the list bytes halve.
-// Arithmetic, masking, compensation and the FP64 kick are those of
-// k_gather_mixed_u.
-constexpr int kTiledThreads = 128;
-
-template <int G, int U, bool PBC, bool SOA>
-__global__ void __launch_bounds__(kTiledThreads) k_gather_mixed_tiled(
-    const Particles P, const TiledList T, const int4* __restrict__ cq, const MixedConsts K0) {
-  // a periodic frame is fixed on the host; an open one may come from the device
-  const MixedConsts K = PBC ? K0 : frame_consts(K0);
-  extern __shared__ int4 tile[];
-  __shared__ int nstart[27], ncount[27];
-  __shared__ int nnb, centre;
-  const int c = blockIdx.x;
-  if (threadIdx.x < 27) {
-    CellGrid g{};
-    g.nc[0] = T.gnc[0];
-    g.nc[1] = T.gnc[1];
-    g.nc[2] = T.gnc[2];
-    g.ncells = T.ncells;
-    g.periodic = T.periodic;
-    int count;
-    const int c2 = neighbour_cell_at(c, g, threadIdx.x, &count);
-    if (c2 >= 0) {
-      const int64_t a = __ldg(T.start + c2), b = __ldg(T.start + c2 + 1);
-      nstart[threadIdx.x] = (int)a;
-      ncount[threadIdx.x] = (int)(b - a);
-      if (c2 == c) centre = threadIdx.x;
-    }
-    if (threadIdx.x == 0) nnb = count;
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, wl = threadIdx.x & 31;
-  for (int nb = warp; nb < nnb; nb += kTiledThreads / 32)
-    for (int t = wl; t < ncount[nb]; t += 32) tile[(nb << T.maxc_shift) + t] = __ldg(cq + nstart[nb] + t);
-  __syncthreads();
-  const int s0 = nstart[centre], s1 = s0 + ncount[centre];
-  const int lane = threadIdx.x & (G - 1);
-  const unsigned mask = (1u << T.maxc_shift) - 1u;
-  for (int base = s0; base < s1; base += kTiledThreads / G) {
-    const int s = base + threadIdx.x / G;
-    const bool valid = s < s1;
-    int cnt = 0, i = 0;
-    int4 xi = make_int4(0, 0, 0, 0);
-    const uint16_t* row = T.rows;
-    if (valid) {
-      cnt = __ldg(T.cnt + s);
-      i = __ldg(T.order + s);
-      xi = tile[(centre << T.maxc_shift) + (s - s0)];
-      row = T.rows + (size_t)s * (size_t)T.maxrow;
-    }
-    int cmax = cnt;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-      cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
-    KahanF ax, ay, az;
-    ax.init();
-    ay.init();
-    az.init();
-    for (int kb = 0; kb < cmax; kb += G * U) {
-      unsigned loc[U];
-      bool ok[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const int k = kb + lane + u * G;
-        ok[u] = k < cnt;
-        loc[u] = ok[u] ? (unsigned)__ldg(row + k) : 0u;
-      }
-      float sx = 0.f, sy = 0.f, sz = 0.f;
-      unsigned border = 0u;
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const float3 d = sep_mixed<false>(xi, tile[loc[u]], K);
-        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-        const bool in = ok[u] && r2 <= K.cl2_lo;
-        if (ok[u] && r2 > K.cl2_lo && r2 <= K.cl2_hi) border |= 1u << u;
-        float df = df_mixed<false>(r2, K);
-        df = in ? df : 0.0f;
-        sx = fmaf(df, d.x, sx);
-        sy = fmaf(df, d.y, sy);
-        sz = fmaf(df, d.z, sz);
-      }
-      if (__any_sync(kFullMask, border != 0u)) {
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-          if (!(border & (1u << u))) continue;
-          const int j = __ldg(T.order + nstart[loc[u] >> T.maxc_shift] + (int)(loc[u] & mask));
-          const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, j), K.f64);
-          if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
-          const float3 d = sep_mixed<false>(xi, tile[loc[u]], K);
-          const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-          const float df = df_mixed<false>(r2, K);
-          sx = fmaf(df, d.x, sx);
-          sy = fmaf(df, d.y, sy);
-          sz = fmaf(df, d.z, sz);
-        }
-      }
-      ax.add(sx);
-      ay.add(sy);
-      az.add(sz);
-    }
-    float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
-    if (G > 1) {
-      group_reduce_comp<G>(hx, lx);
-      group_reduce_comp<G>(hy, ly);
-      group_reduce_comp<G>(hz, lz);
-    }
-    kick_group<SOA, G>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
-  }
-}
-
-template <bool SOA>
-__global__ void __launch_bounds__(256) k_fixed_image_sorted(const Particles P, int n,
-                                                            const int32_t* __restrict__ order,
-                                                            FixedAxis ax, FixedAxis ay,
-                                                            FixedAxis az,
-                                                            const unsigned long long* open_key,
-                                                            int4* __restrict__ cq) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  if (open_key) ax = ay = az = pow2_axis(open_frame_exp(*open_key));
-  const double3 q = load_q<SOA>(P, __ldg(order + s));
-  cq[s] = make_int4(to_fixed(q.x, ax), to_fixed(q.y, ay), to_fixed(q.z, az), 0);
-}
-
-// Compacted FP64 gather (kernel 2).  One warp per row.  Candidates are
-// screened in FP32 from the fixed-point image (cheap), the survivors (inside
-// the cutoff or within 4e-6 of it) are queued in shared memory, and the FP64
-// arithmetic runs on full batches of 32 queued pairs, so the FP64 pipe --
-// the bottleneck of this path on GB300 -- does not idle on pairs beyond the
-// cutoff or on the ragged end of a strided row.  The exact FP64 mask is
-// applied to every queued pair.
-constexpr int kCompactWarps = 4;
-
-template <bool PBC, bool SOA>
-__device__ __forceinline__ void fp64_pair_acc(const Particles& P, const double3& qi, int j,
-                                              const Fp64Consts& k, double& fx, double& fy,
-                                              double& fz) {
-  const double3 d = sep_fp64<PBC>(qi, load_q<SOA>(P, j), k);
-  const double r2 = r2_fp64(d);
-  if (beyond_cutoff(r2, k.cl2_bits)) return;
-  const double df = df_fp64(r2, k);
-  fx = fma(df, d.x, fx);
-  fy = fma(df, d.y, fy);
-  fz = fma(df, d.z, fz);
-}
-
-template <bool PBC, bool SOA, bool ANISO>
-__global__ void __launch_bounds__(32 * kCompactWarps) k_gather_fp64_c(
-    const Particles P, const Csr C, const int4* __restrict__ qfix, const MixedConsts K0) {
-  // a periodic frame is fixed on the host; an open one may come from the device
-  const MixedConsts K = PBC ? K0 : frame_consts(K0);
-  __shared__ int queue[kCompactWarps][64];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * kCompactWarps + w;
-  if (i >= C.n) return;  // warp-uniform
-  int* q = queue[w];
-  const int cnt = __ldg(C.np + i), k0 = __ldg(C.ptr + i);
-  const int4 xi = __ldg(qfix + i);
-  const double3 qi = load_q<SOA>(P, i);
-  const unsigned lt = (1u << lane) - 1u;
-  double fx = 0.0, fy = 0.0, fz = 0.0;
-  int qn = 0;
-  for (int base = 0; base < cnt; base += 32) {
-    const int k = base + lane;
-    bool cand = false;
-    int j = 0;
-    if (k < cnt) {
-      j = __ldg(C.list + k0 + k);
-      const float3 d = sep_mixed<ANISO>(xi, __ldg(qfix + j), K);
-      cand = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x)) <= K.cl2_hi;
-    }
-    const unsigned b = __ballot_sync(kFullMask, cand);
-    if (cand) q[qn + __popc(b & lt)] = j;
-    qn += __popc(b);
-    __syncwarp();
-    if (qn >= 32) {
-      fp64_pair_acc<PBC, SOA>(P, qi, q[lane], K.f64, fx, fy, fz);
-      __syncwarp();
-      if (lane < qn - 32) q[lane] = q[lane + 32];
-      qn -= 32;
-      __syncwarp();
-    }
-  }
-  if (lane < qn) fp64_pair_acc<PBC, SOA>(P, qi, q[lane], K.f64, fx, fy, fz);
-  const double total = warp_reduce3_fp64(fx, fy, fz, lane);
-  if ((lane & 7) == 0 && lane < 24) add_p_axis<SOA>(P, i, lane >> 3, total);
-}
-
-// Compacted FP64 scatter over the half list (kernel 2).  A warp owns 32
-// consecutive rows; their entries are contiguous (the context keeps a compact
-// CSR), so the warp sweeps them flat, 32 entries per step, each lane finding
-// its entry's row by a shuffle binary search over the rows' start offsets.
-// Candidates are screened in FP32 from the fixed-point image; survivors are
-// queued as (i, j) in shared memory and the FP64 arithmetic runs on full
-// batches of 32.  Both ends are updated with RED.F64 (p_i += f, p_j -= f), so
-// a batch may span rows and no lane waits for a row to end.
-constexpr int kScatterWarps = 4;
-
-template <bool PBC, bool SOA>
-__device__ __forceinline__ void fp64_pair_red(const Particles& P, int i, int j,
-                                              const Fp64Consts& k) {
-  const double3 d = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, j), k);
-  const double r2 = r2_fp64(d);
-  if (beyond_cutoff(r2, k.cl2_bits)) return;
-  const double df = df_fp64(r2, k);
-  const double fx = df * d.x, fy = df * d.y, fz = df * d.z;
-  red_p<SOA>(P, i, fx, fy, fz);
-  red_p<SOA>(P, j, flip_sign(fx), flip_sign(fy), flip_sign(fz));
-}
-
-// R rows per warp (32, 16, 8 or 4): fewer rows per warp give more warps,
-// which the FP64 pipe needs for latency hiding on lists of ~1e5 rows, but a
-// larger share of partly filled last batches.
-template <bool PBC, bool SOA, bool ANISO, int R = 32>
-__global__ void __launch_bounds__(32 * kScatterWarps) k_scatter_fp64_c(
-    const Particles P, const Csr C, const int4* __restrict__ qfix, const MixedConsts K0) {
-  static_assert(R == 4 || R == 8 || R == 16 || R == 32, "rows per warp");
-  // a periodic frame is fixed on the host; an open one may come from the device
-  const MixedConsts K = PBC ? K0 : frame_consts(K0);
-  __shared__ int2 queue[kScatterWarps][64];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r0 = (blockIdx.x * kScatterWarps + w) * R;
-  if (r0 >= C.n) return;  // warp-uniform
-  const int nrows = min(R, C.n - r0);
-  int2* q = queue[w];
-  // start offset of row r0 + lane (rows past the end start at e1)
-  const int my_start = lane < nrows ? __ldg(C.ptr + r0 + lane) : 0x7fffffff;
-  const int e0 = __shfl_sync(kFullMask, my_start, 0);
-  const int last = nrows - 1;
-  const int e1 = __shfl_sync(kFullMask, my_start, last) + __ldg(C.np + r0 + last);
-  const unsigned lt = (1u << lane) - 1u;
-  int qn = 0;
-  for (int base = e0; base < e1; base += 32) {
-    const int k = base + lane;
-    // row of entry k: the largest r with start(r) <= k (all lanes search, so
-    // every shuffle is executed by the full warp; r + step stays below 32)
-    int r = 0;
-#pragma unroll
-    for (int step = R / 2; step > 0; step >>= 1) {
-      const int s = __shfl_sync(kFullMask, my_start, r + step);
-      if (s <= k) r += step;
-    }
-    bool cand = false;
-    const int i = r0 + r;
-    int j = 0;
-    if (k < e1) {
-      j = __ldg(C.list + k);
-      const float3 d = sep_mixed<ANISO>(__ldg(qfix + i), __ldg(qfix + j), K);
-      cand = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x)) <= K.cl2_hi;
-    }
-    const unsigned b = __ballot_sync(kFullMask, cand);
-    if (cand) q[qn + __popc(b & lt)] = make_int2(i, j);
-    qn += __popc(b);
-    __syncwarp();
-    if (qn >= 32) {
-      const int2 e = q[lane];
-      fp64_pair_red<PBC, SOA>(P, e.x, e.y, K.f64);
-      __syncwarp();
-      if (lane < qn - 32) q[lane] = q[lane + 32];
-      qn -= 32;
-      __syncwarp();
-    }
-  }
-  if (lane < qn) {
-    const int2 e = q[lane];
-    fp64_pair_red<PBC, SOA>(P, e.x, e.y, K.f64);
-  }
-}
-
-// Mixed scatter: FP32 partial forces per particle in a scratch array
-// (compensation lost on the j side), then one FP64 kick per particle.
-template <int G, bool PBC, bool SOA, bool ANISO>
-__global__ void __launch_bounds__(256) k_scatter_mixed(const Particles P, const Csr C,
-                                                       const int4* __restrict__ qfix,
-                                                       float* __restrict__ facc,
-                                                       const MixedConsts K0) {
-  // a periodic frame is fixed on the host; an open one may come from the device
-  const MixedConsts K = PBC ? K0 : frame_consts(K0);
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = t / G;
-  const int lane = t & (G - 1);
-  const bool valid = i < C.n;
-  int cnt = 0, k0 = 0;
-  int4 xi = make_int4(0, 0, 0, 0);
-  if (valid) {
-    cnt = __ldg(C.np + i);
-    k0 = __ldg(C.ptr + i);
-    xi = __ldg(qfix + i);
-  }
-  KahanF ax, ay, az;
-  ax.init();
-  ay.init();
-  az.init();
-  for (int k = lane; k < cnt; k += G) {
-    const int j = __ldg(C.list + k0 + k);
-    const float3 d = sep_mixed<ANISO>(xi, __ldg(qfix + j), K);
-    const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-    if (!inside_mixed<PBC, SOA>(r2, P, i, j, K)) continue;
-    const float df = df_mixed<ANISO>(r2, K);
-    const float fx = df * d.x, fy = df * d.y, fz = df * d.z;
-    ax.add(fx);
-    ay.add(fy);
-    az.add(fz);
-    atomicAdd(facc + 4 * (size_t)j + 0, -fx);
-    atomicAdd(facc + 4 * (size_t)j + 1, -fy);
-    atomicAdd(facc + 4 * (size_t)j + 2, -fz);
-  }
-  float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
-  if (G > 1) {
-    group_reduce_comp<G>(hx, lx);
-    group_reduce_comp<G>(hy, ly);
-    group_reduce_comp<G>(hz, lz);
-  }
-  if (valid && lane == 0) {
-    atomicAdd(facc + 4 * (size_t)i + 0, hx + lx);
-    atomicAdd(facc + 4 * (size_t)i + 1, hy + ly);
-    atomicAdd(facc + 4 * (size_t)i + 2, hz + lz);
-  }
-}
-
-// Unrolled mixed scatter over the half list (mixed kernel 2): the traversal
-// of k_gather_mixed_u (G lanes per row, U entries in flight, next indices
-// prefetched, FP32 step sums into a Kahan accumulator for i), each pair's
-// reaction on j added with one 16-byte vector atomic (float4 RED), so a pair
-// costs one position gather and one atomic -- half the gathers of the full
-// gather.  j-side sums are plain FP32 and their order varies run to run.
-template <int G, int U, bool PBC, bool SOA, bool ANISO>
-__global__ void __launch_bounds__(256) k_scatter_mixed_u(const Particles P, const Csr C,
-                                                         const int4* __restrict__ qfix,
-                                                         float4* __restrict__ facc,
-                                                         const MixedConsts K0) {
-  // Launched as a programmatic dependent of the image pass, which also
-  // clears facc: nothing the stream wrote is read before that grid finished.
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  const MixedConsts K = PBC ? K0 : frame_consts(K0);
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = t / G;
-  const int lane = t & (G - 1);
-  const bool valid = i < C.n;
-  int cnt = 0;
-  int64_t k0 = 0;
-  int4 xi = make_int4(0, 0, 0, 0);
-  if (valid) {
-    cnt = __ldg(C.np + i);
-    k0 = row_start(C, i);
-    xi = __ldg(qfix + i);
-  }
-  int cmax = cnt;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
-  KahanF ax, ay, az;
-  ax.init();
-  ay.init();
-  az.init();
-  int jn[U];
-#pragma unroll
-  for (int u = 0; u < U; u++) {
-    const int k = lane + u * G;
-    jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
-  }
-  for (int base = 0; base < cmax; base += G * U) {
-    int jj[U];
-    bool ok[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      ok[u] = base + lane + u * G < cnt;
-      jj[u] = ok[u] ? jn[u] : 0;
-    }
-    int4 xj[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const int k = base + G * U + lane + u * G;
-      jn[u] = k < cnt ? __ldg(C.list + k0 + k) : 0;
-    }
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
-      const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-      bool in = ok[u] && r2 <= K.cl2_lo;
-      if (ok[u] && r2 > K.cl2_lo && r2 <= K.cl2_hi) {  // rare: decided in FP64
-        const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, jj[u]), K.f64);
-        in = !beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits);
-      }
-      if (in) {
-        const float df = df_mixed<ANISO>(r2, K);
-        const float fx = df * d.x, fy = df * d.y, fz = df * d.z;
-        sx += fx;
-        sy += fy;
-        sz += fz;
-        atomicAdd(facc + jj[u], make_float4(-fx, -fy, -fz, 0.f));
-      }
-    }
-    ax.add(sx);
-    ay.add(sy);
-    az.add(sz);
-  }
-  // the kick may be scheduled once every block is here (it still waits for
-  // this grid to finish before reading facc)
-  asm volatile("griddepcontrol.launch_dependents;");
-  float hx = ax.s, lx = -ax.c, hy = ay.s, ly = -ay.c, hz = az.s, lz = -az.c;
-  if (G > 1) {
-    group_reduce_comp<G>(hx, lx);
-    group_reduce_comp<G>(hy, ly);
-    group_reduce_comp<G>(hz, lz);
-  }
-  if (valid && lane == 0) atomicAdd(facc + i, make_float4(hx + lx, hy + ly, hz + lz, 0.f));
-}
-
-template <bool SOA>
-__global__ void __launch_bounds__(256) k_kick_from_scratch(const Particles P, int n,
-                                                           const float* __restrict__ facc,
-                                                           const MixedConsts K0) {
-  // may be launched as a programmatic dependent of the scatter: the sums
-  // are read only after that grid has finished
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  const MixedConsts K = frame_consts(K0);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  kick_p<SOA>(P, i, widen_f32(facc[4 * (size_t)i]), widen_f32(facc[4 * (size_t)i + 1]),
-              widen_f32(facc[4 * (size_t)i + 2]), K.fscale, K.fexp);
-}
-
-// ---------------------------------------------------------------------------
-// host side
-// ---------------------------------------------------------------------------
-Fp64Consts make_fp64_consts(const Periodic& box, double dt, double cl2) {
-  Fp64Consts k{};
-  k.c24 = 24.0 * dt;
-  k.c48 = 48.0 * dt;
-  long long b;
-  std::memcpy(&b, &cl2, sizeof b);
-  k.cl2_bits = b;
-  for (int d = 0; d < 3; d++) {
-    k.len[d] = box.on ? box.len[d] : 0.0;
-    const double h = box.on ? box.half[d] : 0.0;
-    std::memcpy(&b, &h, sizeof b);
-    k.half_bits[d] = b;
-  }
-  return k;
-}
-
-void split_float(double v, float& hi, float& lo) {
-  hi = (float)v;
-  lo = (float)(v - (double)hi);
-}
-
-MixedConsts make_mixed_consts(const ForceLaunch& L) {
-  MixedConsts k{};
-  k.f64 = make_fp64_consts(L.box, L.dt, L.cl2);
-  // pair units: fixed units (isotropic) or length (anisotropic)
-  const double u2 = L.aniso ? 1.0 : L.unit[0] * L.unit[0];
-  const double cl2u = L.cl2 / u2;
-  k.cl2_lo = (float)(cl2u * (1.0 - 4e-6));
-  k.cl2_hi = (float)(cl2u * (1.0 + 4e-6));
-  split_float(L.aniso ? 1.0 : 1.0 / u2, k.k_hi, k.k_lo);
-  for (int d = 0; d < 3; d++) {
-    split_float(L.unit[d], k.u_hi[d], k.u_lo[d]);
-    k.fscale[d] = L.aniso ? L.dt : L.unit[d] * L.dt;
-  }
-  k.open_key = L.open_key;
-  return k;
-}
-
-// Launches `kfn` as a programmatic dependent of the previous kernel on `s`:
-// its blocks may be scheduled while that kernel drains, and the kernel itself
-// executes griddepcontrol.wait before reading anything the stream produced.
-template <typename... KArgs, typename... Args>
-cudaError_t launch_dependent(void (*kfn)(KArgs...), int blocks, int block, cudaStream_t s,
-                             Args... args) {
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3(blocks);
-  cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kfn, args...);
-}
-
-template <typename F>
-cudaError_t dispatch_lanes(int lanes, F&& f) {
-  switch (lanes) {
-    case 1: return f(std::integral_constant<int, 1>{});
-    case 2: return f(std::integral_constant<int, 2>{});
-    case 4: return f(std::integral_constant<int, 4>{});
-    case 8: return f(std::integral_constant<int, 8>{});
-    case 16: return f(std::integral_constant<int, 16>{});
-    case 32: return f(std::integral_constant<int, 32>{});
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-template <bool A, bool B, typename F>
-cudaError_t with_bools(F&& f) {
-  return f(std::integral_constant<bool, A>{}, std::integral_constant<bool, B>{});
-}
-
-template <typename F>
-cudaError_t dispatch_bools(bool a, bool b, F&& f) {
-  if (a) return b ? with_bools<true, true>(f) : with_bools<true, false>(f);
-  return b ? with_bools<false, true>(f) : with_bools<false, false>(f);
-}
-
-}  // namespace
-
-void make_fixed_frame(ForceLaunch& L, double max_abs) {
+void make_fixed_frame(ForceLaunch& L) {
   auto axis_for = [](double scale, FixedAxis& ax) {
     int e;
     std::frexp(scale, &e);  // scale = f 2^e, f in [0.5, 1)
@@ -1208,21 +21,36 @@ void make_fixed_frame(ForceLaunch& L, double max_abs) {
     }
     L.aniso = !(L.box.len[0] == L.box.len[1] && L.box.len[1] == L.box.len[2]);
   } else {
-    // |X| <= 2^30 for every particle keeps |Xj - Xi| < 2^31 (open_frame_exp)
-    unsigned long long key;
-    std::memcpy(&key, &max_abs, sizeof key);
-    const int k = open_frame_exp(key & 0x7fffffffffffffffull);
+    // the frame of coarse exponent 0; the kernels rescale it by the device's
+    // choice (L.open_frame)
     for (int d = 0; d < 3; d++) {
-      axis_for(std::ldexp(1.0, k), L.axis[d]);
-      L.unit[d] = std::ldexp(1.0, -k);
+      L.axis[d] = pow2_axis(0);
+      L.unit[d] = 1.0;
     }
     L.aniso = 0;
   }
+  for (int d = 0; d < 3; d++) L.origin[d] = 0;
 }
 
-void make_device_frame(ForceLaunch& L, const unsigned long long* key) {
-  make_fixed_frame(L, std::ldexp(1.0, 29));  // the k = 0 frame
-  L.open_key = key;
+void make_open_frame(ForceLaunch& L, int kf, const long long* origin) {
+  for (int d = 0; d < 3; d++) {
+    L.axis[d] = pow2_axis(kf - kFineBits);
+    L.unit[d] = std::ldexp(1.0, kFineBits - kf);
+    L.origin[d] = origin[d];
+  }
+  L.aniso = 0;
+  L.open_frame = nullptr;
+}
+
+void make_device_frame(ForceLaunch& L, const long long* words) {
+  make_fixed_frame(L);
+  L.open_frame = words;
+}
+
+void host_open_frame(const double* mn, const double* mx, int* kf, long long* origin) {
+  long long k;
+  open_frame_from_bounds(mn, mx, &k, origin);
+  *kf = (int)k;
 }
 
 cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s) {
@@ -1230,23 +58,27 @@ cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   const int blocks = (n + 255) / 256;
   float4* acc = reinterpret_cast<float4*>(L.fscratch);
+  const int acc_len = acc ? (L.precision == LJ_PREC_MIXED ? 2 : 1) : 0;
+  const ImageFrame f0 = host_image_frame(L);
   if (L.part.soa)
-    k_fixed_image<true><<<blocks, 256, 0, s>>>(L.part, n, L.axis[0], L.axis[1], L.axis[2],
-                                              L.open_key, L.qfix, acc);
+    k_fixed_image<true><<<blocks, 256, 0, s>>>(L.part, n, f0, L.open_frame, L.qfix, acc, acc_len);
   else
-    k_fixed_image<false><<<blocks, 256, 0, s>>>(L.part, n, L.axis[0], L.axis[1], L.axis[2],
-                                               L.open_key, L.qfix, acc);
+    k_fixed_image<false><<<blocks, 256, 0, s>>>(L.part, n, f0, L.open_frame, L.qfix, acc, acc_len);
   return cudaGetLastError();
 }
 
-cudaError_t launch_max_abs(const Particles& part, int n, double* out, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
-  if (e != cudaSuccess || n == 0) return e;
+cudaError_t launch_open_frame_init(long long* words, cudaStream_t s) {
+  k_open_frame_init<<<1, 32, 0, s>>>(reinterpret_cast<unsigned long long*>(words));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_open_bounds(const Particles& part, int n, long long* words, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
   int blocks = (n + 255) / 256;
-  if (blocks > 1024) blocks = 1024;
-  auto* o = reinterpret_cast<unsigned long long*>(out);
-  if (part.soa) k_max_abs<true><<<blocks, 256, 0, s>>>(part, n, o);
-  else k_max_abs<false><<<blocks, 256, 0, s>>>(part, n, o);
+  if (blocks > 152 * 4) blocks = 152 * 4;
+  auto* w = reinterpret_cast<unsigned long long*>(words);
+  if (part.soa) k_open_bounds<true><<<blocks, 256, 0, s>>>(part, n, w);
+  else k_open_bounds<false><<<blocks, 256, 0, s>>>(part, n, w);
   return cudaGetLastError();
 }
 
@@ -1306,96 +138,9 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s) {
     });
   }
   const MixedConsts K = make_mixed_consts(L);
-  if (gather && L.kernel == 2) {
-    auto launch_u = [&](auto u) -> cudaError_t {
-      constexpr int U = decltype(u)::value;
-      return dispatch_lanes(L.lanes, [&](auto g) {
-        return dispatch_bools(pbc, soa, [&](auto P, auto S) {
-          constexpr int G = decltype(g)::value;
-          const int4* qf = L.qfix;
-          if (U == 4 && L.csr.aligned4) {
-            if (L.aniso)
-              return launch_dependent(k_gather_mixed_u<G, 4, P.value, S.value, true, true>,
-                                      blocks, block, s, L.part, L.csr, qf, K);
-            return launch_dependent(k_gather_mixed_u<G, 4, P.value, S.value, false, true>, blocks,
-                                    block, s, L.part, L.csr, qf, K);
-          }
-          if (L.aniso)
-            return launch_dependent(k_gather_mixed_u<G, U, P.value, S.value, true>, blocks,
-                                    block, s, L.part, L.csr, qf, K);
-          return launch_dependent(k_gather_mixed_u<G, U, P.value, S.value, false>, blocks, block,
-                                  s, L.part, L.csr, qf, K);
-        });
-      });
-    };
-    switch (L.unroll) {
-      case 1: return launch_u(std::integral_constant<int, 1>{});
-      case 2: return launch_u(std::integral_constant<int, 2>{});
-      case 4: return launch_u(std::integral_constant<int, 4>{});
-      case 8: return launch_u(std::integral_constant<int, 8>{});
-      default: return cudaErrorInvalidValue;
-    }
-  }
-  if (!gather && !L.scratch_zeroed) {
-    cudaError_t e = cudaMemsetAsync(L.fscratch, 0, sizeof(float) * 4 * (size_t)n, s);
-    if (e != cudaSuccess) return e;
-  }
-  if (!gather && L.kernel == 2) {
-    auto launch_su = [&](auto u) -> cudaError_t {
-      constexpr int U = decltype(u)::value;
-      return dispatch_lanes(L.lanes, [&](auto g) {
-        return dispatch_bools(pbc, soa, [&](auto P, auto S) {
-          constexpr int G = decltype(g)::value;
-          float4* fa = reinterpret_cast<float4*>(L.fscratch);
-          if (L.aniso)
-            return launch_dependent(k_scatter_mixed_u<G, U, P.value, S.value, true>, blocks,
-                                    block, s, L.part, L.csr, L.qfix, fa, K);
-          return launch_dependent(k_scatter_mixed_u<G, U, P.value, S.value, false>, blocks,
-                                  block, s, L.part, L.csr, L.qfix, fa, K);
-        });
-      });
-    };
-    cudaError_t e;
-    switch (L.unroll) {
-      case 1: e = launch_su(std::integral_constant<int, 1>{}); break;
-      case 2: e = launch_su(std::integral_constant<int, 2>{}); break;
-      case 4: e = launch_su(std::integral_constant<int, 4>{}); break;
-      case 8: e = launch_su(std::integral_constant<int, 8>{}); break;
-      default: return cudaErrorInvalidValue;
-    }
-    if (e != cudaSuccess) return e;
-    const int kb = (n + 255) / 256;
-    if (soa) return launch_dependent(k_kick_from_scratch<true>, kb, 256, s, L.part, n,
-                                     static_cast<const float*>(L.fscratch), K);
-    return launch_dependent(k_kick_from_scratch<false>, kb, 256, s, L.part, n,
-                            static_cast<const float*>(L.fscratch), K);
-  }
-  cudaError_t e = dispatch_lanes(L.lanes, [&](auto g) {
-    return dispatch_bools(pbc, soa, [&](auto P, auto S) {
-      constexpr int G = decltype(g)::value;
-      if (gather) {
-        if (L.aniso)
-          k_gather_mixed<G, P.value, S.value, true>
-              <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, K);
-        else
-          k_gather_mixed<G, P.value, S.value, false>
-              <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, K);
-      } else {
-        if (L.aniso)
-          k_scatter_mixed<G, P.value, S.value, true>
-              <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, L.fscratch, K);
-        else
-          k_scatter_mixed<G, P.value, S.value, false>
-              <<<blocks, block, 0, s>>>(L.part, L.csr, L.qfix, L.fscratch, K);
-      }
-      return cudaGetLastError();
-    });
-  });
-  if (e != cudaSuccess || gather) return e;
-  const int kb = (n + 255) / 256;
-  if (soa) k_kick_from_scratch<true><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
-  else k_kick_from_scratch<false><<<kb, 256, 0, s>>>(L.part, n, L.fscratch, K);
-  return cudaGetLastError();
+  if (L.precision == LJ_PREC_MIXED)  // two-float pair terms
+    return gather ? launch_mixed_ff_gather(L, K, s) : launch_mixed_ff_scatter(L, K, s);
+  return launch_mixed_fp32(L, K, s);
 }
 
 cudaError_t launch_fixed_image_sorted(const ForceLaunch& L, const int32_t* order, int4* cq,
@@ -1403,73 +148,12 @@ cudaError_t launch_fixed_image_sorted(const ForceLaunch& L, const int32_t* order
   const int n = L.csr.n;
   if (n == 0) return cudaSuccess;
   const int blocks = (n + 255) / 256;
+  const ImageFrame f0 = host_image_frame(L);
   if (L.part.soa)
-    k_fixed_image_sorted<true><<<blocks, 256, 0, s>>>(L.part, n, order, L.axis[0], L.axis[1],
-                                                      L.axis[2], L.open_key, cq);
+    k_fixed_image_sorted<true><<<blocks, 256, 0, s>>>(L.part, n, order, f0, L.open_frame, cq);
   else
-    k_fixed_image_sorted<false><<<blocks, 256, 0, s>>>(L.part, n, order, L.axis[0], L.axis[1],
-                                                       L.axis[2], L.open_key, cq);
+    k_fixed_image_sorted<false><<<blocks, 256, 0, s>>>(L.part, n, order, f0, L.open_frame, cq);
   return cudaGetLastError();
-}
-
-cudaError_t launch_force_tiled(const ForceLaunch& L, const TiledList& T, const int4* cq,
-                               cudaStream_t s) {
-  if (T.ncells == 0 || T.n == 0) return cudaSuccess;
-  const MixedConsts K = make_mixed_consts(L);
-  if (L.aniso) return cudaErrorNotSupported;
-  const size_t smem = sizeof(int4) * 27 * ((size_t)1 << T.maxc_shift);
-  const bool pbc = L.box.on != 0, soa = L.part.soa != 0;
-  auto go = [&](auto u) -> cudaError_t {
-    constexpr int U = decltype(u)::value;
-    return dispatch_lanes(L.lanes, [&](auto g) {
-      return dispatch_bools(pbc, soa, [&](auto P, auto S) {
-        constexpr int G = decltype(g)::value;
-        auto kfn = k_gather_mixed_tiled<G, U, P.value, S.value>;
-        if (smem > 48 * 1024) {
-          cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)smem);
-          if (e != cudaSuccess) return e;
-        }
-        kfn<<<T.ncells, kTiledThreads, smem, s>>>(L.part, T, cq, K);
-        return cudaGetLastError();
-      });
-    });
-  };
-  switch (L.unroll) {
-    case 2: return go(std::integral_constant<int, 2>{});
-    case 4: return go(std::integral_constant<int, 4>{});
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* qfix,
-                               const int32_t* rid, const ReplicaInfo* reps,
-                               const int32_t* rows, int nrows, double dt, double cl2, int lanes,
-                               int unroll, bool vec, cudaStream_t s) {
-  if (vec && (unroll != 4 || c.ptr || c.stride % 4 != 0)) return cudaErrorInvalidValue;
-  if (nrows <= 0) return cudaSuccess;
-  long long cl2_bits;
-  std::memcpy(&cl2_bits, &cl2, sizeof cl2_bits);
-  const int block = 128;
-  const int blocks = (int)(((long long)nrows * lanes + block - 1) / block);
-  auto go = [&](auto u) -> cudaError_t {
-    constexpr int U = decltype(u)::value;
-    return dispatch_lanes(lanes, [&](auto g) {
-      constexpr int G = decltype(g)::value;
-      if (U == 4 && vec)
-        k_gather_mixed_batch<G, 4, true>
-            <<<blocks, block, 0, s>>>(part, c, qfix, rid, reps, rows, nrows, dt, cl2_bits);
-      else
-        k_gather_mixed_batch<G, U, false>
-            <<<blocks, block, 0, s>>>(part, c, qfix, rid, reps, rows, nrows, dt, cl2_bits);
-      return cudaGetLastError();
-    });
-  };
-  switch (unroll) {
-    case 2: return go(std::integral_constant<int, 2>{});
-    case 4: return go(std::integral_constant<int, 4>{});
-    default: return cudaErrorInvalidValue;
-  }
 }
 
 cudaError_t launch_force_pairs(const Particles& part, int n, const int32_t* ip,

@@ -56,8 +56,9 @@ struct ReplicaInfo {
   long long half_bits[3];
   float unit_f[3];          // length per fixed unit
   float k_hi, k_lo;         // 1 / unit^2, split in two floats
-  float cl2u_lo, cl2u_hi;   // cutoff^2 in fixed units^2, -/+ a relative 4e-6
-  float sl2u_lo, sl2u_hi;   // list radius^2 in fixed units^2, -/+ 4e-6
+  float cl2u_lo, cl2u_hi;   // cutoff^2 in fixed units^2, -/+ the FP32 band
+  float cl2f_lo, cl2f_hi;   // the same, -/+ the band of two-float pair terms
+  float sl2u_lo, sl2u_hi;   // list radius^2 in fixed units^2, -/+ the FP32 band
   double unit;              // length per fixed unit (FP64)
   double inv_w[3];          // cells per unit length
   int nc[3];
@@ -72,7 +73,7 @@ struct ForceLaunch {
   Periodic box;
   double dt;
   double cl2;
-  int precision;   // LJ_PREC_*
+  int precision;   // LJ_PREC_* (LJ_PREC_MIXED: two-float pair terms)
   int method;      // LJ_METHOD_GATHER_FULL / LJ_METHOD_SCATTER_HALF (resolved)
   int lanes;       // 1..32
   int block;       // threads per block
@@ -86,21 +87,27 @@ struct ForceLaunch {
   // other way leave this 0
   int scratch_zeroed;
   FixedAxis axis[3];
-  double unit[3];  // length per fixed unit on each axis
+  long long origin[3];  // fine-unit origin subtracted from every coordinate
+  double unit[3];  // length per coarse fixed unit on each axis
   int aniso;       // axes with different units
-  // Open boxes: device word holding the largest |coordinate| (IEEE bits,
-  // written by launch_max_abs on the same stream).  When set, the kernels
-  // derive the fixed-point frame from it (see open_frame_exp) and the host
-  // frame above is the k = 0 frame they rescale; no host round trip.
-  const unsigned long long* open_key;
+  // Open boxes: the device frame words (kOpenFrameWords long longs written
+  // by launch_open_bounds on the same stream).  When set, the kernels take
+  // the fixed-point frame from them and the host frame above is the coarse
+  // exponent 0 frame they rescale; no host round trip.
+  const long long* open_frame;
 };
 
-// Fills axis[] / unit[] / aniso for a periodic box, or for an open box from
-// the largest coordinate magnitude (max_abs).
-void make_fixed_frame(ForceLaunch& L, double max_abs);
-// Open box with the frame chosen on the device from *key (launch_max_abs):
-// sets L.open_key and the k = 0 host frame the kernels rescale.
-void make_device_frame(ForceLaunch& L, const unsigned long long* key);
+// Fills axis[] / unit[] / aniso for a periodic box, or the coarse exponent 0
+// frame of an open box.
+void make_fixed_frame(ForceLaunch& L);
+// Open box with the frame chosen on the device (launch_open_bounds into
+// words): sets L.open_frame and the exponent 0 host frame the kernels rescale.
+void make_device_frame(ForceLaunch& L, const long long* words);
+// The open frame the device would choose for these per-axis bounds: fine
+// exponent kf (coarse unit 2^(10 - kf)) and fine origins.
+void host_open_frame(const double* mn, const double* mx, int* kf, long long* origin);
+// An open frame chosen on the host (host_open_frame) into L.
+void make_open_frame(ForceLaunch& L, int kf, const long long* origin);
 
 // Cell-tiled full list (built with the list, see lj_nlist.cu): particles in
 // cell order (order[s], cells [start[c], start[c+1])), and for every slot s a
@@ -131,7 +138,7 @@ cudaError_t launch_force_tiled(const ForceLaunch& L, const TiledList& T, const i
 cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* qfix,
                                const int32_t* rid, const ReplicaInfo* reps,
                                const int32_t* rows, int nrows, double dt, double cl2, int lanes,
-                               int unroll, bool vec, cudaStream_t s);
+                               int unroll, bool vec, bool ff, cudaStream_t s);
 
 // Launchers (return cudaError_t of the launch)
 cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s);
@@ -139,8 +146,11 @@ cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s);
 cudaError_t launch_force_pairs(const Particles& part, int n, const int32_t* ip,
                                const int32_t* jp, int64_t npairs, const Periodic& box,
                                double dt, double cl2, cudaStream_t s);
-// Largest |coordinate| over all particles, written to *out (device double).
-cudaError_t launch_max_abs(const Particles& part, int n, double* out, cudaStream_t s);
+// Open-box frame words (kOpenFrameWords long longs): launch_open_frame_init
+// once after allocating them, then launch_open_bounds before every image
+// pass (it leaves the frame in the words and re-arms them).
+cudaError_t launch_open_frame_init(long long* words, cudaStream_t s);
+cudaError_t launch_open_bounds(const Particles& part, int n, long long* words, cudaStream_t s);
 
 // ---- list kernels (lj_list.cu) ----
 // Validation; writes into err[0] a nonzero code and err[1] the first bad

@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(256) k_md_drift(double* __restrict__ q,
   z = wrap_into_box(fma(pz, dt, z), lz);
   *reinterpret_cast<double2*>(qi) = xy;
   qi[2] = z;
-  const int4 x = make_int4(to_fixed(xy.x, ax), to_fixed(xy.y, ay), to_fixed(z, az), 0);
+  const int4 x = pack_image(to_fixed_fine(xy.x, ax), to_fixed_fine(xy.y, ay),
+                            to_fixed_fine(z, az));
   qfix[i] = x;
   const int4 r = qref[i];
   const float dx = (float)wrap_sub(x.x, r.x) * ux, dy = (float)wrap_sub(x.y, r.y) * uy,
@@ -118,7 +119,7 @@ __global__ void __launch_bounds__(256) k_md_potential(const double* __restrict__
       if (FP64) {
         double d[3];
         for (int x = 0; x < 3; x++) d[x] = min_image_fp64(qj[x] - qi[x], len[x], hb[x]);
-        const double r2 = fma(d[2], d[2], fma(d[1], d[1], d[0] * d[0]));
+        const double r2 = fma(d[2], d[2], fma(d[0], d[0], d[1] * d[1]));
         if (r2 > cl2) continue;
         const double ir6 = 1.0 / (r2 * r2 * r2);
         u += 4.0 * ir6 * (ir6 - 1.0);
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(256) k_md_potential(const double* __restrict__
         if (!in && r2 <= cl2u_hi) {
           double d[3];
           for (int x = 0; x < 3; x++) d[x] = min_image_fp64(qj[x] - qi[x], len[x], hb[x]);
-          in = !(fma(d[2], d[2], fma(d[1], d[1], d[0] * d[0])) > cl2);
+          in = !(fma(d[2], d[2], fma(d[0], d[0], d[1] * d[1])) > cl2);
         }
         if (!in) continue;
         float inv = 1.0f / r2;
@@ -272,7 +273,8 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "q and p must be 16-byte aligned");
   if (!(prm->dt > 0.0) || !(prm->rc > 0.0) || !(prm->skin >= 0.0))
     return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "dt, rc must be > 0 and skin >= 0");
-  if (prm->precision != LJ_PREC_MIXED && prm->precision != LJ_PREC_FP64)
+  if (prm->precision != LJ_PREC_MIXED && prm->precision != LJ_PREC_MIXED_FP32 &&
+      prm->precision != LJ_PREC_FP64)
     return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown precision");
   const double rs = prm->rc + prm->skin;
   for (int d = 0; d < 3; d++)
@@ -292,7 +294,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     MD_CUDA(ctx, cudaStreamSynchronize(nullptr), "sync");
     s = m.own_stream;
   }
-  const bool mixed = prm->precision == LJ_PREC_MIXED;
+  const bool mixed = prm->precision != LJ_PREC_FP64;
 
   // ---- buffers and constants -------------------------------------------
   m.n = n;
@@ -353,7 +355,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   K.lanes = mixed ? 4 : 4;
   K.block = 128;
   K.qfix = m.qfix.ptr;
-  make_fixed_frame(K, 0.0);
+  make_fixed_frame(K);
   ForceLaunch Kfull = K, Khalf = K;
   Kfull.dt = prm->dt;
   Khalf.dt = 0.5 * prm->dt;
@@ -418,11 +420,12 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     const double u2 = K.unit[0] * K.unit[0];
     const double cl2u = K.cl2 / u2;
     const float khi = (float)(1.0 / u2), klo = (float)(1.0 / u2 - (double)khi);
+    const double band = cutoff_band(std::sqrt(cl2u), kCoarseQuantumErr, kBandFp32);
     const Csr c = K.csr;
     if (mixed && !K.aniso)
       k_md_potential<false><<<grid1(n, 256), 256, 0, s>>>(
           q, m.qfix.ptr, c, K.box.len[0], K.box.len[1], K.box.len[2], khi, klo,
-          (float)(cl2u * (1 - 4e-6)), (float)(cl2u * (1 + 4e-6)), K.cl2, m.energy.ptr + 1);
+          (float)(cl2u * (1 - band)), (float)(cl2u * (1 + band)), K.cl2, m.energy.ptr + 1);
     else
       k_md_potential<true><<<grid1(n, 256), 256, 0, s>>>(
           q, m.qfix.ptr, c, K.box.len[0], K.box.len[1], K.box.len[2], 0.f, 0.f, 0.f, 0.f, K.cl2,

@@ -13,11 +13,14 @@
 //             CSR equals the reference's
 //
 // Membership is decided in FP32 from the exact int32 fixed-point separation;
-// candidates within a relative 4e-6 of the search sphere are re-decided in
-// FP64 with the reference's expression (dx = q_i - q_j), so the list is the
-// reference's list without spending FP64 on every candidate.  Verlet lists
-// of the MD and batch loops (whose users apply the cutoff) skip that
-// re-decision and keep every candidate below the upper edge of the band.
+// candidates within a band of the search sphere (FP32 rounding plus the
+// position quantum, cutoff_band) are re-decided in FP64 with the reference's
+// expression (dx = q_i - q_j), so the list is the reference's list without
+// spending FP64 on every candidate.  Verlet lists of the MD and batch loops
+// (whose users apply the cutoff) skip that re-decision and keep every
+// candidate below the upper edge of the band.
+#include <algorithm>
+#include <cmath>
 #include <type_traits>
 
 #include "lj_cells.cuh"
@@ -80,7 +83,8 @@ struct BuildConsts {
   double sl2;
 };
 
-// The reference's membership test (makepair: dx = q_i - q_j, r2 < SL2), FP64.
+// The reference's membership test (makepair: dx = q_i - q_j, r2 < SL2), FP64,
+// with r2 contracted into fused multiply-adds as the reference's build does.
 __device__ __forceinline__ bool within_fp64(const double* q, int i, int j, const BuildConsts& k) {
   const double* a = q + 4 * (size_t)i;
   const double* b = q + 4 * (size_t)j;
@@ -89,7 +93,7 @@ __device__ __forceinline__ bool within_fp64(const double* q, int i, int j, const
     d[x] = a[x] - b[x];
     if (k.periodic) d[x] = min_image_fp64(d[x], k.len[x], k.half_bits[x]);
   }
-  const double r2 = fma(d[2], d[2], fma(d[1], d[1], d[0] * d[0]));
+  const double r2 = fma(d[2], d[2], fma(d[0], d[0], d[1] * d[1]));
   return r2 < k.sl2;
 }
 
@@ -148,7 +152,7 @@ struct BuildStage {
 // ROWS_FULL / ROWS_HALF, slot-indexed 16-bit local indices (walk position
 // << maxc_shift | slot in that cell) for ROWS_LOCAL.  EXACT: the reference's
 // membership (FP64 re-decision near the sphere); otherwise every candidate
-// with FP32 r2 < sl2_hi, a superset by at most a relative 4e-6.
+// with FP32 r2 < sl2_hi, a superset by at most the relative band.
 template <int MODE, bool ANISO, bool EXACT>
 __device__ __forceinline__ void build_cell_rows(int c, int cell_base, const CellGrid& g,
                                                 const int64_t* __restrict__ start,
@@ -412,8 +416,12 @@ BuildConsts make_build_consts(const BuildArgs& a) {
   BuildConsts k{};
   const double u2 = a.aniso ? 1.0 : a.unit[0] * a.unit[0];
   const double sl2u = a.search * a.search / u2;
-  k.sl2_lo = (float)(sl2u * (1.0 - 4e-6));
-  k.sl2_hi = (float)(sl2u * (1.0 + 4e-6));
+  // FP32 r2 from the coarse image: arithmetic band plus the coarse quantum
+  const double umax = std::max(a.unit[0], std::max(a.unit[1], a.unit[2]));
+  const double band = cutoff_band(std::sqrt(sl2u), kCoarseQuantumErr * (a.aniso ? umax : 1.0),
+                                  kBandFp32);
+  k.sl2_lo = (float)(sl2u * (1.0 - band));
+  k.sl2_hi = (float)(sl2u * (1.0 + band));
   for (int d = 0; d < 3; d++) {
     k.u_hi[d] = (float)a.unit[d];
     k.u_lo[d] = (float)(a.unit[d] - (double)k.u_hi[d]);

@@ -31,7 +31,7 @@ struct BuildArgs {
   const int32_t* cell;
   int want_half, want_full;
   // 0: membership exactly r2 < search^2 in FP64 (the reference's list);
-  // 1: a superset that may add pairs within a relative 4e-6 outside the
+  // 1: a superset that may add pairs within the FP32 band outside the
   //    sphere (Verlet lists whose users apply the cutoff themselves)
   int superset;
 };

@@ -4,9 +4,10 @@
 // running inside a host that owns every allocation (a pooled allocator the
 // engine cannot see, a real-time loop where cudaMalloc's implicit device
 // synchronisation is not allowed, or a plugin host that forbids its plugins
-// to allocate).  The regular mixed path keeps its scratch (the 32-bit
-// fixed-point position image) in a buffer the context allocates; this entry
-// point keeps that scratch in a fixed, file-scope device array instead.
+// to allocate).  The regular mixed path keeps its scratch (the fixed-point
+// position image and, for open boxes, the frame words) in buffers the
+// context allocates; this entry point keeps that scratch in a fixed,
+// file-scope device array instead.
 //
 // Limits and sharing:
 //   * at most kNoAllocMaxParticles particles (16 MiB of scratch, held by
@@ -15,8 +16,11 @@
 //     calls that overlap on the GPU (different streams, or different host
 //     threads on one device) race and must be ordered by the caller;
 //   * the first call on each device resolves the array's device address
-//     with cudaGetSymbolAddress; make that first call before any stream
-//     capture on that device.
+//     with cudaGetSymbolAddress and arms the open-box frame words with one
+//     small kernel on the caller's stream; make that first call before any
+//     stream capture on that device;
+//   * the list is not validated (the reference's kernels do not validate
+//     theirs either): every index must be in [0, n).
 #include <mutex>
 
 #include "lj_gb300.h"
@@ -27,21 +31,24 @@ namespace {
 
 constexpr int kNoAllocMaxParticles = 1 << 20;
 constexpr size_t kImageBytes = sizeof(int4) * (size_t)kNoAllocMaxParticles;
-constexpr size_t kScratchBytes = kImageBytes + 256;  // + the open-box extent word
+constexpr size_t kScratchBytes = kImageBytes + 256;  // + the open-box frame words
 
-// The scratch: fixed-point image of q, then one 8-byte word for the largest
-// |coordinate| (open boundaries only).  Host code must not use this symbol's
-// name as an address: it is a host-side stand-in.  The device address comes
-// from cudaGetSymbolAddress below.
+// The scratch: fixed-point image of q, then the open-box frame words
+// (kOpenFrameWords long longs, open boundaries only).  Host code must not use
+// this symbol's name as an address: it is a host-side stand-in.  The device
+// address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+static_assert(sizeof(long long) * kOpenFrameWords <= kScratchBytes - kImageBytes,
+              "frame words fit behind the image");
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 void* g_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device (set-up on the
-// first call per device).
-cudaError_t scratch_address(void** out) {
+// Device address of g_noalloc_scratch on the current device.  Set-up on the
+// first call per device: the address lookup and the arming of the frame
+// words (a kernel on stream s, ahead of that call's own work).
+cudaError_t scratch_address(void** out, cudaStream_t s) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -50,6 +57,9 @@ cudaError_t scratch_address(void** out) {
   if (!g_scratch_addr[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    e = launch_open_frame_init(
+        reinterpret_cast<long long*>(static_cast<unsigned char*>(p) + kImageBytes), s);
     if (e != cudaSuccess) return e;
     g_scratch_addr[dev] = p;
   }
@@ -72,11 +82,11 @@ extern "C" int lj_force_mixed_noalloc_aos(const double* q, double* p, int32_t n,
     return LJ_ERR_INVALID_ARGUMENT;
   if ((reinterpret_cast<uintptr_t>(q) & 15u) || (reinterpret_cast<uintptr_t>(p) & 15u))
     return LJ_ERR_INVALID_ARGUMENT;
-  if (!(cl2 >= 0.0) || !(dt == dt)) return LJ_ERR_INVALID_ARGUMENT;
+  if (!(cl2 >= 0.0) || !(dt - dt == 0.0)) return LJ_ERR_INVALID_ARGUMENT;  // dt finite
   if (n == 0) return LJ_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   void* base = nullptr;
-  if (scratch_address(&base) != cudaSuccess) return LJ_ERR_CUDA;
+  if (scratch_address(&base, s) != cudaSuccess) return LJ_ERR_CUDA;
   ForceLaunch L{};
   L.part.soa = 0;
   L.part.q = q;
@@ -102,18 +112,16 @@ extern "C" int lj_force_mixed_noalloc_aos(const double* q, double* p, int32_t n,
   L.lanes = 4;
   L.block = 128;
   L.qfix = static_cast<int4*>(base);
-  double max_abs = 0.0;
   if (!L.box.on) {
-    // largest |coordinate| into the extent word (zeroed first), read back
-    double* word = reinterpret_cast<double*>(static_cast<unsigned char*>(base) + kImageBytes);
-    if (launch_max_abs(L.part, n, word, s) != cudaSuccess) return LJ_ERR_CUDA;
-    if (cudaMemcpyAsync(&max_abs, word, sizeof max_abs, cudaMemcpyDeviceToHost, s) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-      return LJ_ERR_CUDA;
-    if (!(max_abs - max_abs == 0.0)) return LJ_ERR_INVALID_ARGUMENT;  // inf / NaN
+    // the open frame from the coordinates' bounds, chosen on the device into
+    // the frame words behind the image (no host round trip)
+    long long* words =
+        reinterpret_cast<long long*>(static_cast<unsigned char*>(base) + kImageBytes);
+    if (launch_open_bounds(L.part, n, words, s) != cudaSuccess) return LJ_ERR_CUDA;
+    make_device_frame(L, words);
+  } else {
+    make_fixed_frame(L);
   }
-  make_fixed_frame(L, max_abs);
   if (launch_fixed_image(L, s) != cudaSuccess) return LJ_ERR_CUDA;
   return launch_force(L, s) == cudaSuccess ? LJ_OK : LJ_ERR_CUDA;
 }

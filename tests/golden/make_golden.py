@@ -1,6 +1,6 @@
 """Regenerates the golden fixtures in this directory from the reference itself.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout>
 
 Needs the reference sources (read-only) and an x86-64 host: it builds the
 reference's own cpu_ref routines with oracle/Makefile (`make ref`, outputs in
@@ -82,7 +82,7 @@ def run_reference(layout, q, box_len):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="the reference checkout")
     a = ap.parse_args()
     ref = Path(a.ref)
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF={ref}"], check=True)

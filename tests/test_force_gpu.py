@@ -2,8 +2,10 @@
 
 FP64 path: <= 1e-12 relative per particle (norm of the 3-vector) against the
 oracle's force_sorted (cpu_ref/force_aos.cpp:192-224 restated).
-Mixed path: one force evaluation against the FP64 oracle with the tolerances
-written in MIXED_TOL.
+Mixed paths: one force evaluation against the FP64 oracle:
+  "mixed" (two-float pair terms): the per-particle bar max_i |dF_i|/|F_i|
+  <= 1e-5 (MIXED_TOL, with a tighter bound on the normalised error);
+  "mixed_fp32" (single FP32 pair terms): normalised bars only (FP32_TOL).
 """
 import numpy as np
 import pytest
@@ -13,8 +15,18 @@ import oracle_lib as ol
 pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12
-# one mixed force evaluation vs FP64: max |dF_i| / rms|F| and ||dF|| / ||F||
-MIXED_TOL = {"max_rel_rms": 1e-5, "global_rel": 2e-6}
+# one two-float force evaluation vs FP64: max |dF_i| / |F_i| per particle, and
+# max |dF_i| / rms|F|
+MIXED_TOL = {"max_rel": 1e-5, "max_rel_rms": 1e-7}
+# one FP32-pair-term evaluation vs FP64: max |dF_i| / rms|F| and ||dF|| / ||F||
+FP32_TOL = {"max_rel_rms": 1e-5, "global_rel": 2e-6}
+TOL = {"mixed": MIXED_TOL, "mixed_fp32": FP32_TOL}
+MIXED_PRECS = list(TOL)
+
+
+def check_mixed(e, prec, *where):
+    for k, tol in TOL[prec].items():
+        assert e[k] <= tol, (where, prec, k, e)
 
 
 def _torch():
@@ -104,27 +116,29 @@ def test_fp64_every_lane_width(engine, lanes):
 @pytest.mark.parametrize("method,kernel", [("gather", 1), ("gather", 2), ("scatter", 1),
                                            ("scatter", 2)])
 @pytest.mark.parametrize("layout", ["aos", "soa"])
-def test_mixed_error_bounds(engine, name, method, kernel, layout):
+@pytest.mark.parametrize("prec", MIXED_PRECS)
+def test_mixed_error_bounds(engine, name, method, kernel, layout, prec):
     q, box, half = system(name)
     dt = 0.005
     ref = oracle_p(q, half, box, 1, dt)
-    got = run_engine(engine, q, half, box, "mixed", method, layout, 1, dt, kernel=kernel)
-    e = ol.rel_errors(got, ref)
-    for k, tol in MIXED_TOL.items():
-        assert e[k] <= tol, (k, e)
+    got = run_engine(engine, q, half, box, prec, method, layout, 1, dt, kernel=kernel)
+    check_mixed(ol.rel_errors(got, ref), prec, name, method, kernel, layout)
 
 
 @pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32])
 def test_mixed_every_lane_width(engine, lanes):
     q, box, half = system("pbc_rho1")
     ref = oracle_p(q, half, box, 1, 0.005)
-    for method, kernel, unrolls in (("gather", 1, [0]), ("gather", 2, [2, 4, 8]),
-                                    ("scatter", 2, [1, 2, 4, 8])):
-        for unroll in unrolls:
-            got = run_engine(engine, q, half, box, "mixed", method, "aos", 1, 0.005, lanes=lanes,
-                             kernel=kernel, unroll=unroll)
-            e = ol.rel_errors(got, ref)
-            assert e["max_rel_rms"] <= MIXED_TOL["max_rel_rms"], (method, kernel, unroll, e)
+    # two-float pair terms take 2 or 4 entries in flight per lane
+    cases = {"mixed": (("gather", 1, [0]), ("gather", 2, [2, 4]), ("scatter", 2, [2, 4])),
+             "mixed_fp32": (("gather", 1, [0]), ("gather", 2, [2, 4, 8]),
+                            ("scatter", 2, [1, 2, 4, 8]))}
+    for prec, runs in cases.items():
+        for method, kernel, unrolls in runs:
+            for unroll in unrolls:
+                got = run_engine(engine, q, half, box, prec, method, "aos", 1, 0.005,
+                                 lanes=lanes, kernel=kernel, unroll=unroll)
+                check_mixed(ol.rel_errors(got, ref), prec, method, kernel, unroll)
 
 
 def test_mixed_anisotropic_box(engine):
@@ -136,19 +150,20 @@ def test_mixed_anisotropic_box(engine):
     half = ol.build_list(q, 3.3, box=box)
     ref = oracle_p(q, half, box, 1, 0.005)
     for method in ("gather", "scatter"):
-        got = run_engine(engine, q, half, box, "mixed", method, "aos", 1, 0.005)
-        e = ol.rel_errors(got, ref)
-        assert e["max_rel_rms"] <= MIXED_TOL["max_rel_rms"], (method, e)
+        for prec in MIXED_PRECS:
+            got = run_engine(engine, q, half, box, prec, method, "aos", 1, 0.005)
+            check_mixed(ol.rel_errors(got, ref), prec, method)
         got64 = run_engine(engine, q, half, box, "fp64", method, "aos", 1, 0.005)
         assert ol.rel_errors(got64, ref)["max_rel"] <= FP64_TOL
 
 
-def test_cutoff_boundary_pairs_follow_fp64_mask(engine):
-    """Isolated pairs at r2 within a few ulp of CL2: the mixed mask must be the
-    FP64 mask (a toggled pair would change F by |f(rc)| ~ 1e-2, i.e. 100 %)."""
-    rng = np.random.default_rng(1)
-    g = 8  # 8^3 pair sites 12 apart: only the planted pairs interact
-    centres = np.stack(np.meshgrid(*[np.arange(g) * 12.0] * 3, indexing="ij"), -1).reshape(-1, 3)
+def planted_pairs(shift=0.0, spacing=12.0, g=8, seed=1, box=None):
+    """g^3 isolated pairs at r2 within a few ulp of CL2 = 9, their centres
+    `spacing` apart and shifted by `shift`; with a box the grid fills it and
+    the pairs straddle its faces where the grid meets them."""
+    rng = np.random.default_rng(seed)
+    centres = np.stack(np.meshgrid(*[np.arange(g) * spacing] * 3, indexing="ij"),
+                       -1).reshape(-1, 3) + shift
     m = centres.shape[0]
     dirs = rng.normal(size=(m, 3))
     dirs /= np.linalg.norm(dirs, axis=1)[:, None]
@@ -156,18 +171,52 @@ def test_cutoff_boundary_pairs_follow_fp64_mask(engine):
     q = np.zeros((2 * m, 4))
     q[0::2, :3] = centres
     q[1::2, :3] = centres + dirs * r[:, None]
-    half = ol.build_list(q, 3.3)
-    assert len(half[2]) == m
-    ref64 = run_engine(engine, q, half, None, "fp64", "gather", "aos", 1, 0.005)
-    inside = np.linalg.norm(ref64[:, :3], axis=1) > 0
-    assert 0 < inside.sum() < 2 * m  # both sides of the surface are exercised
-    for method, kernel in (("gather", 1), ("gather", 2), ("scatter", 1)):
-        got = run_engine(engine, q, half, None, "mixed", method, "aos", 1, 0.005, kernel=kernel)
-        assert np.array_equal(np.linalg.norm(got[:, :3], axis=1) > 0, inside), method
-        assert ol.rel_errors(got, ref64)["max_rel"] <= 1e-5, method
+    if box is not None:
+        q[:, :3] = np.mod(q[:, :3], box)
+    return q
+
+
+def check_planted_mask(engine, q, box):
+    """Every planted pair is masked as the reference's FP64 arithmetic masks
+    it (a toggled pair would change F by |f(rc)| ~ 1e-2, i.e. 100 %), and the
+    forces meet the bars."""
+    half = ol.build_list(q, 3.3, box=box)
+    assert len(half[2]) == q.shape[0] // 2
+    ref = oracle_p(q, half, box, 1, 0.005)
+    inside = np.linalg.norm(ref[:, :3], axis=1) > 0
+    assert 0 < inside.sum() < q.shape[0]  # both sides of the surface are exercised
+    for prec in MIXED_PRECS:
+        for method, kernel in (("gather", 1), ("gather", 2), ("scatter", 1), ("scatter", 2)):
+            got = run_engine(engine, q, half, box, prec, method, "aos", 1, 0.005,
+                             kernel=kernel)
+            assert np.array_equal(np.linalg.norm(got[:, :3], axis=1) > 0, inside), \
+                (prec, method, kernel)
+            assert ol.rel_errors(got, ref)["max_rel"] <= 1e-5, (prec, method, kernel)
     for method in ("gather", "scatter"):
-        got64c = run_engine(engine, q, half, None, "fp64", method, "aos", 1, 0.005, kernel=2)
-        assert ol.rel_errors(got64c, ref64)["max_rel"] <= FP64_TOL, method
+        for kernel in (1, 2):
+            got64 = run_engine(engine, q, half, box, "fp64", method, "aos", 1, 0.005,
+                               kernel=kernel)
+            assert ol.rel_errors(got64, ref)["max_rel"] <= FP64_TOL, (method, kernel)
+
+
+def test_cutoff_boundary_pairs_follow_fp64_mask(engine):
+    check_planted_mask(engine, planted_pairs(), None)
+
+
+@pytest.mark.parametrize("shift", [1e3, 1e4, 1e5, -1e5])
+def test_cutoff_mask_at_large_open_coordinates(engine, shift):
+    """The planted pairs far from the origin: the open frame's quantum follows
+    the system's extent (per-axis origin at the minimum coordinate), so the
+    mask and the forces do not depend on where the system sits."""
+    check_planted_mask(engine, planted_pairs(shift=shift), None)
+
+
+def test_cutoff_mask_in_a_large_periodic_box(engine):
+    """A periodic box of L = 5000 (coarse quantum L / 2^32 = 1.2e-6): pairs
+    on a grid that fills the box, some straddling its faces."""
+    L = 5000.0
+    q = planted_pairs(spacing=L / 16, g=16, seed=3, box=L)
+    check_planted_mask(engine, q, L)
 
 
 def test_stateless_drop_in(engine):
@@ -286,12 +335,14 @@ def test_edge_cases(engine):
     lst = np.arange(1, n, dtype=np.int32)
     half = (npp, ptr, lst)
     ref = oracle_p(q, half, None, 1, 0.001)
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", "mixed", "mixed_fp32"):
         for method, kernel in (("scatter", 1), ("scatter", 2), ("gather", 1), ("gather", 2)):
             got = run_engine(engine, q, half, None, prec, method, "aos", 1, 0.001, kernel=kernel)
             e = ol.rel_errors(got, ref)
             if prec == "fp64":
                 assert e["max_rel"] <= FP64_TOL, (method, e)
+            elif prec == "mixed":
+                check_mixed(e, prec, method, kernel)
             else:
                 assert e["max_rel_rms"] <= 1e-4, (method, e)
 
@@ -374,7 +425,7 @@ def test_non_compact_list_layout(engine):
             assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+@pytest.mark.parametrize("prec", ["mixed", "mixed_fp32", "fp64"])
 def test_autotune_picks_a_valid_shape_and_keeps_results(engine, prec):
     q, box, half = system("pbc_rho1")
     ref = oracle_p(q, half, box, 1, 0.005)
@@ -390,8 +441,10 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(engine, prec):
             pd = dev(np.zeros_like(q))
             ctx.force_aos(qd, pd, o)
             e = ol.rel_errors(host(pd), ref)
-            assert (e["max_rel"] <= FP64_TOL) if prec == "fp64" else \
-                (e["max_rel_rms"] <= MIXED_TOL["max_rel_rms"]), e
+            if prec == "fp64":
+                assert e["max_rel"] <= FP64_TOL, e
+            else:
+                check_mixed(e, prec, o.kernel)
 
 
 def test_interleaved_z_layout(engine):
@@ -402,14 +455,17 @@ def test_interleaved_z_layout(engine):
     z[:, :4] = q
     with engine.Context(0) as ctx:
         ctx.set_list_csr(dev(half[0]), dev(half[1]), dev(half[2]))
-        for prec in ("fp64", "mixed"):
+        for prec in ("fp64", "mixed", "mixed_fp32"):
             zd = dev(z)
             for _ in range(3):
                 ctx.force_z(zd, engine.make_opts(dt=0.005, cl2=9.0, box=box, precision=prec))
             out = host(zd)
             assert np.array_equal(out[:, :4], q)  # positions untouched
             e = ol.rel_errors(out[:, 4:8], ref)
-            assert (e["max_rel"] <= FP64_TOL) if prec == "fp64" else (e["max_rel_rms"] <= 1e-5)
+            if prec == "fp64":
+                assert e["max_rel"] <= FP64_TOL, e
+            else:
+                check_mixed(e, prec)
 
 
 def test_transposed_list_round_trip(engine):
@@ -440,9 +496,9 @@ def test_transposed_list_round_trip(engine):
 @pytest.mark.parametrize("name", list(SYSTEMS))
 @pytest.mark.parametrize("layout", ["aos", "soa"])
 def test_cell_tiled_gather_on_device_built_lists(engine, name, layout):
-    """Kernel 3 (cell-tiled, 16-bit local rows; opt-in or autotuned) runs once
-    the list was built on the device; it must meet the mixed bounds, and
-    kernels 2 and 3 must see exactly the same pairs."""
+    """Kernel 3 (cell-tiled, 16-bit local rows, FP32 pair terms; opt-in or
+    autotuned) runs once the list was built on the device; it must meet the
+    FP32-term bounds, and kernels 2 and 3 must see exactly the same pairs."""
     q, box, half = system(name)
     ref = oracle_p(q, half, box, 1, 0.005)
     with engine.Context(0) as ctx:
@@ -450,7 +506,7 @@ def test_cell_tiled_gather_on_device_built_lists(engine, name, layout):
         ctx.build_list(qd, 3.3, box=box)
         outs = {}
         for kernel, lanes, unroll in ((3, 0, 0), (3, 2, 2), (3, 8, 4), (2, 4, 4)):
-            opts = engine.make_opts(dt=0.005, cl2=9.0, box=box, precision="mixed",
+            opts = engine.make_opts(dt=0.005, cl2=9.0, box=box, precision="mixed_fp32",
                                     method="gather", kernel=kernel, lanes=lanes, unroll=unroll)
             if layout == "aos":
                 pd = dev(np.zeros_like(q))
@@ -463,9 +519,7 @@ def test_cell_tiled_gather_on_device_built_lists(engine, name, layout):
                 got = np.zeros_like(q)
                 for d in range(3):
                     got[:, d] = host(ps[d])
-            e = ol.rel_errors(got, ref)
-            for k, tol in MIXED_TOL.items():
-                assert e[k] <= tol, (kernel, lanes, unroll, k, e)
+            check_mixed(ol.rel_errors(got, ref), "mixed_fp32", kernel, lanes, unroll)
             outs[(kernel, lanes, unroll)] = got
         # same pairs: tiled vs unrolled differ only by FP32 summation order
         # (a few 1e-6 of the rms force); one pair more or less, even at the
@@ -476,7 +530,8 @@ def test_cell_tiled_gather_on_device_built_lists(engine, name, layout):
 
 @pytest.mark.parametrize("name", list(SYSTEMS))
 @pytest.mark.parametrize("layout", ["aos", "soa"])
-def test_vector_index_loads_kernel4(engine, name, layout):
+@pytest.mark.parametrize("prec", MIXED_PRECS)
+def test_vector_index_loads_kernel4(engine, name, layout, prec):
     """Kernel 4 (kernel 2 over the 16-byte-aligned copy of the full list, one
     16-byte index load per lane and step) meets the mixed bounds and sees the
     same pairs as kernel 2 (rows of any length, including rows shorter than
@@ -486,16 +541,16 @@ def test_vector_index_loads_kernel4(engine, name, layout):
     with engine.Context(0) as ctx:
         outs = {}
         for kernel, lanes in ((4, 0), (4, 2), (4, 8), (2, 4)):
-            got = run_engine(engine, q, half, box, "mixed", "gather", layout, 1, 0.005,
+            got = run_engine(engine, q, half, box, prec, "gather", layout, 1, 0.005,
                              lanes=lanes, ctx=ctx, kernel=kernel, unroll=4)
-            e = ol.rel_errors(got, ref)
-            for k, tol in MIXED_TOL.items():
-                assert e[k] <= tol, (kernel, lanes, k, e)
+            check_mixed(ol.rel_errors(got, ref), prec, kernel, lanes)
             outs[(kernel, lanes)] = got
-        assert ol.rel_errors(outs[(4, 0)], outs[(2, 4)])["max_rel_rms"] <= 5e-6
+        same = 1e-8 if prec == "mixed" else 5e-6  # summation order only
+        assert ol.rel_errors(outs[(4, 0)], outs[(2, 4)])["max_rel_rms"] <= same
 
 
-def test_kernel4_measure_uses_the_uploaded_list(engine, fixture_rho05):
+@pytest.mark.parametrize("prec", MIXED_PRECS)
+def test_kernel4_measure_uses_the_uploaded_list(engine, fixture_rho05, prec):
     """lj_measure_aos re-uploads a host list and refreshes the aligned copy
     from it inside the timed region; results match the FP64 oracle's bounds."""
     f = fixture_rho05
@@ -504,14 +559,13 @@ def test_kernel4_measure_uses_the_uploaded_list(engine, fixture_rho05):
         ctx.set_list_csr(*half)
         fnp, fptr, flist = ctx.get_list_csr("full")
         ctx.set_list_csr(fnp, fptr, flist, kind="full")  # host full list
-        opts = engine.make_opts(dt=0.001, cl2=9.0, precision="mixed", method="gather",
+        opts = engine.make_opts(dt=0.001, cl2=9.0, precision=prec, method="gather",
                                 kernel=4, unroll=4)
         p = np.zeros_like(f["q"])
         ctx.measure_aos(np.ascontiguousarray(f["q"]), p, opts, calls=1)
         e = ol.rel_errors(p, ol.force_sorted_aos(f["q"], np.zeros_like(f["q"]), *half,
                                                  dt=0.001, box=None, calls=1))
-        for k, tol in MIXED_TOL.items():
-            assert e[k] <= tol, (k, e)
+        check_mixed(e, prec)
 
 
 def test_launch_option_checks(engine, fixture_rho05):
@@ -525,28 +579,35 @@ def test_launch_option_checks(engine, fixture_rho05):
             with pytest.raises(engine.LJError) as e:
                 ctx.force_aos(qd, pd, opts)
             assert e.value.status == engine.LJ_ERR_INVALID_ARGUMENT, kw
+        # two-float pair terms take 2 or 4 entries in flight per lane
+        for kw in (dict(method="gather", kernel=2, unroll=8), dict(method="scatter", unroll=1)):
+            with pytest.raises(engine.LJError) as e:
+                ctx.force_aos(qd, pd, engine.make_opts(precision="mixed", **kw))
+            assert e.value.status == engine.LJ_ERR_UNSUPPORTED, kw
 
 
 @pytest.mark.parametrize("kernel", [1, 2, 4])
-def test_open_box_frame_follows_the_coordinates(engine, kernel):
-    """Open boxes take their fixed-point frame from the largest |coordinate|,
-    chosen on the device each call: translating the system (a coarser frame)
-    and back within one context keeps every call within the mixed bounds."""
+@pytest.mark.parametrize("prec", MIXED_PRECS)
+def test_open_box_frame_follows_the_coordinates(engine, kernel, prec):
+    """Open boxes take their fixed-point frame from the per-axis bounds of
+    the coordinates, chosen on the device each call: translating the system
+    far from the origin and back within one context keeps every call within
+    the mixed bounds, for both the gather and the scatter."""
     q, box, half = system("open_rho0.5")
     with engine.Context(0) as ctx:
         npp, ptr, lst = half
         ctx.set_list_csr(dev(npp), dev(ptr), dev(lst), kind="half")
-        opts = engine.make_opts(dt=0.001, cl2=9.0, precision="mixed", method="gather",
-                                kernel=kernel, unroll=4 if kernel > 1 else 0)
-        for shift in (0.0, 100.0, 0.0, -37.5):
-            qs = q.copy()
-            qs[:, :3] += shift
-            ref = oracle_p(qs, half, None, 1, 0.001)
-            pd = dev(np.zeros_like(q))
-            ctx.force_aos(dev(qs), pd, opts)
-            e = ol.rel_errors(host(pd), ref)
-            for k, tol in MIXED_TOL.items():
-                assert e[k] <= tol, (shift, k, e)
+        for method in ("gather", "scatter"):
+            k = 2 if method == "scatter" and kernel == 4 else kernel
+            opts = engine.make_opts(dt=0.001, cl2=9.0, precision=prec, method=method,
+                                    kernel=k, unroll=4 if k > 1 else 0)
+            for shift in (0.0, 100.0, 1e3, 1e4, 1e5, 0.0, -37.5, -1e5):
+                qs = q.copy()
+                qs[:, :3] += shift
+                ref = oracle_p(qs, half, None, 1, 0.001)
+                pd = dev(np.zeros_like(q))
+                ctx.force_aos(dev(qs), pd, opts)
+                check_mixed(ol.rel_errors(host(pd), ref), prec, method, shift)
 
 
 @pytest.mark.parametrize("seed", range(6))
@@ -574,13 +635,13 @@ def test_random_systems_every_path(engine, seed):
             got = run_engine(engine, q, half, box, "fp64", method, "aos", 1, 0.005, ctx=ctx,
                              kernel=kernel)
             assert ol.rel_errors(got, ref)["max_rel"] <= FP64_TOL, (seed, method, kernel)
-        for method, kernel, unroll in (("gather", 1, 0), ("gather", 2, 4), ("gather", 4, 4),
-                                       ("scatter", 1, 0), ("scatter", 2, 4)):
-            got = run_engine(engine, q, half, box, "mixed", method, "soa" if seed % 2 else "aos",
-                             1, 0.005, ctx=ctx, kernel=kernel, unroll=unroll)
-            e = ol.rel_errors(got, ref)
-            for k, tol in MIXED_TOL.items():
-                assert e[k] <= tol, (seed, method, kernel, k, e)
+        for prec in MIXED_PRECS:
+            for method, kernel, unroll in (("gather", 1, 0), ("gather", 2, 4), ("gather", 4, 4),
+                                           ("scatter", 1, 0), ("scatter", 2, 4)):
+                got = run_engine(engine, q, half, box, prec, method,
+                                 "soa" if seed % 2 else "aos", 1, 0.005, ctx=ctx, kernel=kernel,
+                                 unroll=unroll)
+                check_mixed(ol.rel_errors(got, ref), prec, seed, method, kernel)
         ctx.build_list(dev(q), 3.3, box=box)
         np_d, ptr_d, lst_d = ctx.get_list_csr("half")
         np_r, ptr_r, lst_r = ol.build_list(q, 3.3, box=box)
