@@ -85,7 +85,11 @@ typedef struct lj_force_opts {
                          3 and 4 fall back to 2 when their list form is
                          missing (see lj_force.cu)                          */
   int32_t unroll;     /* entries per lane in flight (kernel 2), 0 = default   */
-  int32_t reserved;
+  int32_t ff_all;     /* LJ_PREC_MIXED gathers (kernels 2 and 4): 0 = pairs
+                         beyond 2.5 sigma of the first call's positions in
+                         FP32 terms, any pair closer than 2.2 sigma in
+                         two-float terms (the default); 1 = every pair in
+                         two-float terms                                     */
 } lj_force_opts;
 
 /* dt = 0.001, cl2 = 9.0 (cpu_ref/force_aos.cpp:14,31-33), open box, FP64, auto */
@@ -276,7 +280,10 @@ typedef struct lj_md_params {
   int32_t graph_steps;    /* steps per captured CUDA graph (0: 20, 1: no graph) */
   int32_t rebuild_every;  /* 0: rebuild when a particle moved > skin/2 since the
                              last build; k > 0: also every k steps */
-  int32_t reserved[4];
+  int32_t ff_all;         /* LJ_PREC_MIXED: 0 = pairs beyond 2.5 sigma at the
+                             last rebuild in FP32 terms (the default), 1 =
+                             every pair in two-float terms */
+  int32_t reserved[3];
 } lj_md_params;
 
 typedef struct lj_md_record {

@@ -57,12 +57,12 @@ class ForceOpts(C.Structure):
         ("block", C.c_int32),
         ("kernel", C.c_int32),
         ("unroll", C.c_int32),
-        ("reserved", C.c_int32),
+        ("ff_all", C.c_int32),
     ]
 
 
 def make_opts(dt=0.001, cl2=9.0, box=None, precision="fp64", method="auto", lanes=0,
-              block=0, kernel=0, unroll=0) -> ForceOpts:
+              block=0, kernel=0, unroll=0, ff_all=False) -> ForceOpts:
     o = ForceOpts()
     o.dt, o.cl2 = float(dt), float(cl2)
     if box is not None:
@@ -73,6 +73,7 @@ def make_opts(dt=0.001, cl2=9.0, box=None, precision="fp64", method="auto", lane
     o.method = _METHOD[method] if isinstance(method, str) else int(method)
     o.lanes, o.block = int(lanes), int(block)
     o.kernel, o.unroll = int(kernel), int(unroll)
+    o.ff_all = 1 if ff_all else 0
     return o
 
 
@@ -80,7 +81,7 @@ class MdParams(C.Structure):
     _fields_ = [
         ("dt", C.c_double), ("rc", C.c_double), ("skin", C.c_double), ("box", C.c_double * 3),
         ("precision", C.c_int32), ("record_every", C.c_int32), ("graph_steps", C.c_int32),
-        ("rebuild_every", C.c_int32), ("reserved", C.c_int32 * 4),
+        ("rebuild_every", C.c_int32), ("ff_all", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -94,7 +95,7 @@ class MdStats(C.Structure):
 
 
 def make_md_params(dt, rc, skin, box, precision="mixed", record_every=0, graph_steps=0,
-                   rebuild_every=0):
+                   rebuild_every=0, ff_all=False):
     m = MdParams()
     m.dt, m.rc, m.skin = float(dt), float(rc), float(skin)
     b = [float(box)] * 3 if isinstance(box, (int, float)) else [float(v) for v in box]
@@ -102,6 +103,7 @@ def make_md_params(dt, rc, skin, box, precision="mixed", record_every=0, graph_s
     m.precision = _PRECISION[precision] if isinstance(precision, str) else int(precision)
     m.record_every, m.graph_steps = int(record_every), int(graph_steps)
     m.rebuild_every = int(rebuild_every)
+    m.ff_all = 1 if ff_all else 0
     return m
 
 

@@ -80,6 +80,8 @@ int check_opts(lj_ctx* ctx, const lj_force_opts* o) {
   if (o->kernel < 0 || o->kernel > 4)
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kernel must be 0 (default) or 1..4");
   if (o->unroll < 0) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be >= 0");
+  if (o->ff_all != 0 && o->ff_all != 1)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "ff_all must be 0 or 1");
   if (!(o->cl2 >= 0.0) || !std::isfinite(o->dt))
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "cl2 must be >= 0 and dt finite");
   if (o->periodic) {
@@ -176,6 +178,7 @@ int expand_full(lj_ctx* ctx) {
 int build_aligned(lj_ctx* ctx) {
   DevList& f = ctx->full;
   f.avalid = false;
+  f.svalid = f.savalid = false;
   const int n = f.n;
   if (!f.valid || n == 0) return LJ_OK;
   cudaStream_t s = ctx->stream;
@@ -209,6 +212,7 @@ int install_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ptr,
   ctx->half.valid = false;
   ctx->full.valid = false;
   ctx->full.avalid = false;
+  ctx->full.svalid = ctx->full.savalid = false;
   ctx->tiled.valid = false;
   LJ_CUDA(ctx, l.np.ensure((size_t)n), "alloc");
   LJ_CUDA(ctx, l.ptr.ensure((size_t)n), "alloc");
@@ -418,6 +422,28 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
       return LJ_OK;
     }
     LJ_CUDA(ctx, launch_fixed_image(L, ctx->stream), "fixed image");
+    // two-float gathers (kernels 2 and 4) run the near/far split over a
+    // near-first copy of the full list, ordered from these positions the
+    // first time; later positions only change its speed, not its results'
+    // precision (k_gather_mixed_split)
+    if (o->precision == LJ_PREC_MIXED && method == LJ_METHOD_GATHER_FULL && L.kernel == 2 &&
+        !o->ff_all) {
+      DevList& f = ctx->full;
+      const bool al = L.csr.aligned4 != 0;
+      bool& ok = al ? f.savalid : f.svalid;
+      DevBuf<int32_t>& buf = al ? f.salist : f.slist;
+      DevBuf<int32_t>& nn = al ? f.sann : f.snn;
+      if (!ok) {
+        LJ_CUDA(ctx, buf.ensure((size_t)std::max<int64_t>(al ? f.aentries : f.entries, 4)),
+                "alloc");
+        LJ_CUDA(ctx, nn.ensure((size_t)n), "alloc");
+        LJ_CUDA(ctx, launch_partition_near(L, L.csr, buf.ptr, nn.ptr, nullptr, ctx->stream),
+                "near-first rows");
+        ok = true;
+      }
+      L.csr.list = buf.ptr;
+      L.csr.nn = nn.ptr;
+    }
   }
   if (tv) LJ_CUDA(ctx, cudaEventRecord(tv[1], ctx->stream), "event");
   LJ_CUDA(ctx, launch_force(L, ctx->stream), "force launch");
@@ -993,6 +1019,7 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
   ctx->half.valid = false;
   ctx->full.valid = false;
   ctx->full.avalid = false;
+  ctx->full.svalid = ctx->full.savalid = false;
   ctx->tiled.valid = false;
   int full_maxrow = 0;
   LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");

@@ -56,6 +56,11 @@ struct DevList {
   int64_t aentries = 0;
   bool avalid = false;
   Csr acsr() const { return Csr{n, entries, np.ptr, aptr.ptr, alist.ptr, 0, 1}; }
+  // near-first copies of list and alist (k_partition_near, made from the
+  // positions of the first two-float gather after the list changed) with
+  // their near counts; reset whenever the list changes
+  DevBuf<int32_t> slist, snn, salist, sann;
+  bool svalid = false, savalid = false;
 };
 
 struct MdState;  // lj_md.cu

@@ -1,7 +1,8 @@
 // lj_force_ff.cu -- launches of the mixed gathers with two-float pair terms
 // (LJ_PREC_MIXED): the unrolled gather (kernel 2, and kernel 4's 16-byte
-// index loads) and the simple gather (kernel 1).  Two-float terms take 2 or
-// 4 entries in flight per lane.
+// index loads) and the simple gather (kernel 1); near-first rows go to the
+// near/far split (lj_force_split.cu).  Two-float terms take 2 or 4 entries
+// in flight per lane.
 #include "lj_force_kernels.cuh"
 
 namespace ljg {
@@ -25,6 +26,7 @@ cudaError_t launch_mixed_ff_gather(const ForceLaunch& L, const MixedConsts& K, c
       });
     });
   }
+  if (L.csr.nn) return launch_mixed_ff_split(L, K, s);  // near-first rows
   auto go = [&](auto u) -> cudaError_t {
     constexpr int U = decltype(u)::value;
     return dispatch_lanes(L.lanes, [&](auto g) {

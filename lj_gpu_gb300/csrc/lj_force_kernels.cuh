@@ -1,8 +1,8 @@
 // lj_force_kernels.cuh -- the force kernels and their launch helpers, shared
 // by the translation units that instantiate them (lj_force.cu: FP64 paths,
-// images and frames; lj_force_mixed.cu: FP32 pair terms; lj_force_ff.cu and
-// lj_force_ff_scatter.cu: two-float pair terms; lj_force_batch.cu: replica
-// batches and the cell-tiled gather).  Spreading the instantiations over
+// images and frames; lj_force_mixed.cu: FP32 pair terms; lj_force_ff.cu,
+// lj_force_split.cu and lj_force_ff_scatter.cu: two-float pair terms;
+// lj_force_batch.cu: replica batches and the cell-tiled gather).  Spreading the instantiations over
 // several files lets them compile in parallel.
 //
 // One force call is the kick p_i += sum_j df(r_ij) (q_j - q_i) with
@@ -59,6 +59,11 @@ struct MixedConsts {
   // two-float terms: the scatter's j-side sums snap the leading part of each
   // term to multiples of 2^qexp pair units, so float atomics add them exactly
   float snap;            // 1.5 * 2^(23 + qexp): (x + snap) - snap rounds x to that grid
+  // near/far split of two-float gathers (k_gather_mixed_split): FP32 terms
+  // beyond the split radius, with the FP32 cutoff band for those terms
+  float cl2s_lo, cl2s_hi;  // r2 band of FP32 terms (pair units)
+  float near2;           // r2 (pair units) below which a term is always two-float
+  float near_build2;     // r2 (pair units) of the near-first ordering (k_partition_near)
   Fp64Consts f64;        // for the rare FP64 cutoff decision
   const long long* open_frame;  // device-chosen open-box frame, see frame_consts
 };
@@ -351,14 +356,25 @@ __global__ void __launch_bounds__(256) k_pairs_fp64(const Particles P, const int
 // the device (coarse scale 2^k, k = kf - 10), the host built them for k = 0;
 // every frame-dependent one scales exactly by a power of two, and the band
 // follows the quantum.
+// The relative cutoff band in float (per thread: no FP64 issue).
+__device__ __forceinline__ float cutoff_band_f(float rc, float q, float base) {
+  return base + (3.4641016f * rc * q + 3.0f * q * q) / (rc * rc);
+}
+
 __device__ __forceinline__ MixedConsts frame_consts(const MixedConsts& K0) {
   MixedConsts K = K0;
   if (K0.open_frame) {
     const int k = (int)K0.open_frame[kOfExp] - kFineBits;
     const float cl2u = ldexpf(K0.cl2_0, 2 * k);
-    const float band = (float)cutoff_band(sqrtf(cl2u), K0.qerr, K0.band_base);
+    const float rc = sqrtf(cl2u);
+    const float band = cutoff_band_f(rc, K0.qerr, K0.band_base);
     K.cl2_lo = cl2u * (1.0f - band);
     K.cl2_hi = cl2u * (1.0f + band);
+    const float band32 = cutoff_band_f(rc, (float)kCoarseQuantumErr, (float)kBandFp32);
+    K.cl2s_lo = cl2u * (1.0f - band32);
+    K.cl2s_hi = cl2u * (1.0f + band32);
+    K.near2 = ldexpf(K0.near2, 2 * k);
+    K.near_build2 = ldexpf(K0.near_build2, 2 * k);
     K.k_hi = ldexpf(K0.k_hi, 2 * k);
     K.k_lo = ldexpf(K0.k_lo, 2 * k);
     K.snap = ldexpf(K0.snap, k);
@@ -781,6 +797,228 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
     group_reduce_comp<G>(hz, lz);
   }
   kick_group<SOA, G, FF>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
+}
+
+// Two-float gather over a near-first list (kernel 2 with the near/far split,
+// rows ordered by k_partition_near, C.nn[i] near entries first).  The near
+// segment [0, nn) runs the two-float pair terms of k_gather_mixed_u; the far
+// segment [nn, cnt) runs FP32 pair terms from the coarse image (the FP32
+// kernels' arithmetic, with their cutoff band), summed apart in compensated
+// FP32.  A far entry closer than K.near2 -- a pair that moved in since the
+// ordering -- is evaluated in two-float arithmetic all the same, so the
+// ordering only decides the speed, never the precision.  VEC as in
+// k_gather_mixed_u: the far segment starts at nn rounded down to a multiple
+// of 4 with the entries before nn masked.
+template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC>
+__global__ void __launch_bounds__(256) k_gather_mixed_split(const Particles P, const Csr C,
+                                                            const int4* __restrict__ qfix,
+                                                            const MixedConsts K0) {
+  static_assert(!VEC || U == 4, "vector index loads take 4 entries per lane");
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / G;
+  const int lane = t & (G - 1);
+  // launched as a programmatic dependent of the image pass
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const MixedConsts K = PBC ? K0 : frame_consts(K0);
+  const bool valid = i < C.n;
+  int cnt = 0, nn = 0;
+  int64_t k0 = 0;
+  int4 xi = make_int4(0, 0, 0, 0);
+  if (valid) {
+    cnt = __ldg(C.np + i);
+    nn = __ldg(C.nn + i);
+    k0 = row_start(C, i);
+    xi = __ldg(qfix + i);
+  }
+  int li[3];
+  image_lo(xi.w, li[0], li[1], li[2]);
+  RowSums<true> acc;    // two-float terms
+  RowSums<false> acc32;  // FP32 terms of the far segment
+  acc.init();
+  acc32.init();
+  // entry `base` + (lane, u) of a segment starting at entry `from`
+  auto entry = [&](int base, int u) { return VEC ? base + 4 * lane + u : base + lane + u * G; };
+  auto load_idx = [&](int from, int lim, int base, int* jn) {
+    if (VEC) {
+      int4 v = make_int4(0, 0, 0, 0);
+      if (from + entry(base, 0) < lim)
+        v = __ldg(reinterpret_cast<const int4*>(C.list + k0 + from + entry(base, 0)));
+      jn[0] = v.x;
+      jn[1] = v.y;
+      jn[2] = v.z;
+      jn[3] = v.w;
+    } else {
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        jn[u] = from + entry(base, u) < lim ? __ldg(C.list + k0 + from + entry(base, u)) : 0;
+    }
+  };
+  // FP64 re-decision of a pair in the cutoff band (either term type)
+  auto inside64 = [&](int j) {
+    const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, j), K.f64);
+    return !beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits);
+  };
+  // ---- near segment [0, nn): two-float terms
+  {
+    int cmax = nn;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+      cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
+    int jn[U];
+    load_idx(0, nn, 0, jn);
+    for (int base = 0; base < cmax; base += G * U) {
+      int jj[U];
+      bool ok[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        ok[u] = entry(base, u) < nn;
+        jj[u] = ok[u] ? jn[u] : 0;
+      }
+      int4 xj[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
+      load_idx(0, nn, base + G * U, jn);
+      unsigned border = 0u;
+#pragma unroll
+      for (int u = 0; u < U; u++) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, ok[u], border, u);
+      if (__any_sync(kFullMask, border != 0u)) {
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          if ((border & (1u << u)) && inside64(jj[u]))
+            pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 1, true, border, u);
+      }
+    }
+  }
+  // ---- far segment [nn, cnt): FP32 terms
+  {
+    const int from = VEC ? (nn & ~3) : nn;
+    int cmax = cnt - from;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+      cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
+    int jn[U];
+    load_idx(from, cnt, 0, jn);
+    for (int base = 0; base < cmax; base += G * U) {
+      int jj[U];
+      bool ok[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int e = from + entry(base, u);
+        ok[u] = e >= nn && e < cnt;
+        jj[u] = ok[u] ? jn[u] : 0;
+      }
+      int4 xj[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
+      load_idx(from, cnt, base + G * U, jn);
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      unsigned border = 0u, near = 0u;
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
+        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+        const bool close = ok[u] && r2 < K.near2;
+        if (close) near |= 1u << u;
+        const bool in = ok[u] && !close && r2 <= K.cl2s_lo;
+        if (ok[u] && !close && r2 > K.cl2s_lo && r2 <= K.cl2s_hi) border |= 1u << u;
+        float df = df_mixed<ANISO>(r2, K);
+        df = in ? df : 0.0f;
+        sx = fmaf(df, d.x, sx);
+        sy = fmaf(df, d.y, sy);
+        sz = fmaf(df, d.z, sz);
+      }
+      if (__any_sync(kFullMask, border != 0u)) {
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          if (!(border & (1u << u)) || !inside64(jj[u])) continue;
+          const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
+          const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+          const float df = df_mixed<ANISO>(r2, K);
+          sx = fmaf(df, d.x, sx);
+          sy = fmaf(df, d.y, sy);
+          sz = fmaf(df, d.z, sz);
+        }
+      }
+      acc32.x.add(sx);
+      acc32.y.add(sy);
+      acc32.z.add(sz);
+      // pairs that moved inside the near radius: two-float terms
+      if (__any_sync(kFullMask, near != 0u)) {
+        unsigned bff = 0u;
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          if (near & (1u << u)) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, true, bff, u);
+        if (__any_sync(kFullMask, bff != 0u)) {
+#pragma unroll
+          for (int u = 0; u < U; u++)
+            if ((bff & (1u << u)) && inside64(jj[u]))
+              pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 1, true, bff, u);
+        }
+      }
+    }
+  }
+  // FP32 sums (Kahan) join the two-float sums; FP32 terms are in pair units
+  // times the FP32 kick scale (fscale / 24 for the two-float kick)
+  float hx, lx, hy, ly, hz, lz, fx, gx, fy, gy, fz, gz;
+  acc.get(hx, lx, hy, ly, hz, lz);
+  acc32.get(fx, gx, fy, gy, fz, gz);
+  auto join = [](float& h, float& l, float f, float g) {
+    const float f24 = __fmul_rn(f, 0.041666668f), g24 = __fmul_rn(g, 0.041666668f);
+    const ff s = ff_two_sum(h, f24);
+    h = s.h;
+    l = __fadd_rn(l, __fadd_rn(s.l, g24));
+  };
+  join(hx, lx, fx, gx);
+  join(hy, ly, fy, gy);
+  join(hz, lz, fz, gz);
+  if (G > 1) {
+    group_reduce_comp<G>(hx, lx);
+    group_reduce_comp<G>(hy, ly);
+    group_reduce_comp<G>(hz, lz);
+  }
+  kick_group<SOA, G, true>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
+}
+
+// Orders every row near-first for k_gather_mixed_split: entries with FP32 r2
+// (coarse image) below K.near_build2 first, in list order, the others after
+// them in reverse list order; nn[i] receives the near count.  Rows keep
+// their starts (out has the layout of C).  One warp per row, rows in a
+// grid-stride loop.
+template <bool PBC, bool ANISO>
+__global__ void __launch_bounds__(128) k_partition_near(const Csr C, const int4* __restrict__ qfix,
+                                                        const MixedConsts K0,
+                                                        int32_t* __restrict__ out,
+                                                        int32_t* __restrict__ nn,
+                                                        const int32_t* guard) {
+  if (guard && *(volatile const int32_t*)guard == 0) return;
+  const MixedConsts K = PBC ? K0 : frame_consts(K0);
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < C.n; i += nwarps) {
+    const int cnt = __ldg(C.np + i);
+    const int64_t k0 = row_start(C, i);
+    const int4 xi = __ldg(qfix + i);
+    int nacc = 0, facc = 0;
+    for (int base = 0; base < cnt; base += 32) {
+      const int k = base + lane;
+      const bool ok = k < cnt;
+      int j = 0;
+      bool near = false;
+      if (ok) {
+        j = __ldg(C.list + k0 + k);
+        const float3 d = sep_mixed<ANISO>(xi, __ldg(qfix + j), K);
+        near = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x)) < K.near_build2;
+      }
+      const unsigned bn = __ballot_sync(kFullMask, near);
+      const unsigned bf = __ballot_sync(kFullMask, ok && !near);
+      if (near) out[k0 + nacc + __popc(bn & lt)] = j;
+      else if (ok) out[k0 + cnt - 1 - (facc + __popc(bf & lt))] = j;
+      nacc += __popc(bn);
+      facc += __popc(bf);
+    }
+    if (lane == 0) nn[i] = nacc;
+  }
 }
 
 // Batched mixed gather: as k_gather_mixed_u, with every constant that depends
@@ -1504,6 +1742,12 @@ MixedConsts make_mixed_consts(const ForceLaunch& L) {
   k.cl2_0 = (float)cl2u;
   k.band_base = (float)base;
   k.qerr = (float)q;
+  // FP32 terms of the near/far split: the FP32 band on the coarse image
+  const double band32 = cutoff_band(std::sqrt(cl2u), q_c, kBandFp32);
+  k.cl2s_lo = (float)(cl2u * (1.0 - band32));
+  k.cl2s_hi = (float)(cl2u * (1.0 + band32));
+  k.near2 = (float)(kFarCheck * kFarCheck / u2);
+  k.near_build2 = (float)(kFarSplit * kFarSplit / u2);
   split_float(L.aniso ? 1.0 : 1.0 / u2, k.k_hi, k.k_lo);
   // two-float terms: 24 moves from the pair term into the kick scale
   const double c = ff ? 24.0 : 1.0;
@@ -1571,5 +1815,6 @@ cudaError_t dispatch_bools(bool a, bool b, F&& f) {
 cudaError_t launch_mixed_fp32(const ForceLaunch& L, const MixedConsts& K, cudaStream_t s);
 cudaError_t launch_mixed_ff_gather(const ForceLaunch& L, const MixedConsts& K, cudaStream_t s);
 cudaError_t launch_mixed_ff_scatter(const ForceLaunch& L, const MixedConsts& K, cudaStream_t s);
+cudaError_t launch_mixed_ff_split(const ForceLaunch& L, const MixedConsts& K, cudaStream_t s);
 
 }  // namespace ljg

@@ -35,6 +35,8 @@ struct Csr {
   const int32_t* list;
   int64_t stride;
   int aligned4;  // every row starts on a 16-byte boundary and is readable to a multiple of 4
+  // near-first rows (k_partition_near): near entries of row i, or nullptr
+  const int32_t* nn;
 };
 
 __device__ __forceinline__ int64_t row_start(const Csr& c, int i) {
@@ -142,6 +144,12 @@ cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* 
 
 // Launchers (return cudaError_t of the launch)
 cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s);
+// Near-first copy of the rows of `in` (same row starts) into `out` for the
+// near/far split of two-float gathers (L's frame and cutoff), near counts
+// into nn; L's position image must be current.  `guard` (optional): nothing
+// happens while *guard == 0.
+cudaError_t launch_partition_near(const ForceLaunch& L, const Csr& in, int32_t* out, int32_t* nn,
+                                  const int32_t* guard, cudaStream_t s);
 cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s);
 cudaError_t launch_force_pairs(const Particles& part, int n, const int32_t* ip,
                                const int32_t* jp, int64_t npairs, const Periodic& box,

@@ -175,6 +175,10 @@ struct MdState {
   int maxrow = 0;
   DevBuf<int4> qfix, qref, cq, cq2;
   DevBuf<int32_t> flags, cell, count, cursor, order, order2, cnt, ptr, rows, list;
+  // near-first copy of the padded rows and its near counts (two-float kicks
+  // with the near/far split)
+  DevBuf<int32_t> rows2, nn;
+  bool split = false;
   DevBuf<int64_t> start, off;
   DevBuf<unsigned char> scan_tmp;
   DevBuf<double> energy;
@@ -207,7 +211,7 @@ namespace {
 // offsets, placement, per-cell ordering, warp-cooperative row build into the
 // padded rows.  The mixed gather reads the padded rows directly; the FP64
 // scatter sweeps rows flat, so its rows are compacted (scan + copy).
-cudaError_t md_rebuild(MdState& m, bool compact, cudaStream_t s) {
+cudaError_t md_rebuild(MdState& m, bool compact, const ForceLaunch& kick, cudaStream_t s) {
   const int32_t* g = m.flags.ptr + F_REBUILD;
   cudaError_t e;
   if ((e = launch_bin(m.build.q, m.n, m.grid, m.cell.ptr, m.count.ptr, s, g))) return e;
@@ -223,6 +227,10 @@ cudaError_t md_rebuild(MdState& m, bool compact, cudaStream_t s) {
   if ((e = launch_build_rows(m.build, m.build.want_half != 0, m.maxrow, m.rows.ptr, m.cnt.ptr,
                              m.flags.ptr + F_OVERFLOW, s, g)))
     return e;
+  if (m.split) {  // near-first rows from the positions of this build
+    const Csr rows{m.n, m.cap, m.cnt.ptr, nullptr, m.rows.ptr, (int64_t)m.maxrow, 1, nullptr};
+    if ((e = launch_partition_near(kick, rows, m.rows2.ptr, m.nn.ptr, g, s))) return e;
+  }
   if (compact) {
     if ((e = launch_scan_counts(m.cnt.ptr, m.n, m.off.ptr, m.scan_tmp.ptr, m.scan_tmp.cap, s, g)))
       return e;
@@ -255,7 +263,7 @@ cudaError_t md_step(MdState& m, const DriftArgs& d, const ForceLaunch& kick, cud
       d.rebuild_every, m.flags.ptr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  if ((e = md_rebuild(m, kick.method == LJ_METHOD_SCATTER_HALF, s))) return e;
+  if ((e = md_rebuild(m, kick.method == LJ_METHOD_SCATTER_HALF, kick, s))) return e;
   return launch_force(kick, s);
 }
 
@@ -328,6 +336,11 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   MD_CUDA(ctx, m.off.ensure((size_t)n + 1), "alloc");
   MD_CUDA(ctx, m.scan_tmp.ensure(scan_tmp_bytes(std::max(n, m.grid.ncells))), "alloc");
   MD_CUDA(ctx, m.rows.ensure((size_t)m.cap), "alloc");
+  m.split = prm->precision == LJ_PREC_MIXED && !prm->ff_all;
+  if (m.split) {
+    MD_CUDA(ctx, m.rows2.ensure((size_t)m.cap), "alloc");
+    MD_CUDA(ctx, m.nn.ensure((size_t)n), "alloc");
+  }
   // the compacted half list holds about half of the padded capacity
   const int64_t half_cap = std::min<int64_t>(m.cap, 0x7fffffffll);
   if (!mixed) MD_CUDA(ctx, m.list.ensure((size_t)half_cap), "alloc");
@@ -340,8 +353,9 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   K.part.p = p;
   // mixed: padded rows read in place (64-bit row starts i * maxrow); FP64:
   // compacted rows with int32 offsets
-  K.csr = mixed ? Csr{n, m.cap, m.cnt.ptr, nullptr, m.rows.ptr, (int64_t)m.maxrow, 1}
-                : Csr{n, m.cap, m.cnt.ptr, m.ptr.ptr, m.list.ptr, 0, 0};
+  K.csr = mixed ? Csr{n, m.cap, m.cnt.ptr, nullptr, m.split ? m.rows2.ptr : m.rows.ptr,
+                      (int64_t)m.maxrow, 1, m.split ? m.nn.ptr : nullptr}
+                : Csr{n, m.cap, m.cnt.ptr, m.ptr.ptr, m.list.ptr, 0, 0, nullptr};
   K.box.on = 1;
   for (int d = 0; d < 3; d++) {
     K.box.len[d] = prm->box[d];
@@ -405,7 +419,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   // ---- initial image and list ----------------------------------------------
   MD_CUDA(ctx, launch_fixed_image(K, s), "image");
   k_md_set<<<1, 32, 0, s>>>(m.flags.ptr, F_REBUILD, 1);
-  MD_CUDA(ctx, md_rebuild(m, !mixed, s), "initial build");
+  MD_CUDA(ctx, md_rebuild(m, !mixed, K, s), "initial build");
 
   int32_t nrec = 0;
   auto read_flags = [&](int32_t* f) -> int {

@@ -545,7 +545,7 @@ def test_vector_index_loads_kernel4(engine, name, layout, prec):
                              lanes=lanes, ctx=ctx, kernel=kernel, unroll=4)
             check_mixed(ol.rel_errors(got, ref), prec, kernel, lanes)
             outs[(kernel, lanes)] = got
-        same = 1e-8 if prec == "mixed" else 5e-6  # summation order only
+        same = 1e-7 if prec == "mixed" else 5e-6  # summation order only
         assert ol.rel_errors(outs[(4, 0)], outs[(2, 4)])["max_rel_rms"] <= same
 
 
@@ -566,6 +566,49 @@ def test_kernel4_measure_uses_the_uploaded_list(engine, fixture_rho05, prec):
         e = ol.rel_errors(p, ol.force_sorted_aos(f["q"], np.zeros_like(f["q"]), *half,
                                                  dt=0.001, box=None, calls=1))
         check_mixed(e, prec)
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+@pytest.mark.parametrize("kernel", [2, 4])
+def test_two_float_split_and_full_terms(engine, name, kernel):
+    """The two-float gather's near/far split (FP32 terms beyond 2.5 sigma,
+    the default) and two-float terms for every pair (ff_all) both meet the
+    per-particle bar; they differ only by the far terms' FP32 rounding."""
+    q, box, half = system(name)
+    ref = oracle_p(q, half, box, 1, 0.005)
+    with engine.Context(0) as ctx:
+        ctx.set_list_csr(dev(half[0]), dev(half[1]), dev(half[2]), kind="half")
+        out = {}
+        for ff_all in (False, True):
+            pd = dev(np.zeros_like(q))
+            ctx.force_aos(dev(q), pd, engine.make_opts(
+                dt=0.005, cl2=9.0, box=box, precision="mixed", method="gather", kernel=kernel,
+                unroll=4, ff_all=ff_all))
+            out[ff_all] = host(pd)
+            check_mixed(ol.rel_errors(out[ff_all], ref), "mixed", name, kernel, ff_all)
+        # every pair two-float: ~1e-9 of FP64
+        assert ol.rel_errors(out[True], ref)["max_rel"] <= 1e-7
+
+
+def test_split_order_from_other_positions_keeps_precision(engine):
+    """The near-first order is made from the positions of the first call;
+    later calls with particles moved by up to 0.45 sigma (past the 0.3 sigma
+    margin) still meet the per-particle bar: pairs that came closer than
+    2.2 sigma are evaluated in two-float terms wherever they sit."""
+    q, box = ol.init_fcc_periodic(6, 1.0, 0.05, seed=20240601)
+    rng = np.random.default_rng(8)
+    q2 = q.copy()
+    q2[:, :3] = np.mod(q2[:, :3] + rng.uniform(-0.26, 0.26, size=(q.shape[0], 3)), box)
+    half = ol.build_list(q, 3.9, box=box)  # covers every pair within 3.0 of q2
+    with engine.Context(0) as ctx:
+        ctx.set_list_csr(dev(half[0]), dev(half[1]), dev(half[2]), kind="half")
+        opts = engine.make_opts(dt=0.005, cl2=9.0, box=box, precision="mixed",
+                                method="gather")
+        for pos in (q, q2, q):
+            pd = dev(np.zeros_like(q))
+            ctx.force_aos(dev(pos), pd, opts)
+            ref = oracle_p(pos, half, box, 1, 0.005)
+            check_mixed(ol.rel_errors(host(pd), ref), "mixed", "moved")
 
 
 def test_launch_option_checks(engine, fixture_rho05):

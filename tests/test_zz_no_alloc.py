@@ -7,7 +7,8 @@ lj_force_mixed_noalloc_aos serves them with a static scratch array.  This
 file checks, on two calls in a row:
   * its result is bit for bit that of the regular mixed entry point
     (lj_force_aos, which allocates its scratch in the context) run with the
-    same launch shape (kernel 2, 4 lanes, 4 entries in flight, 128 threads);
+    same launch shape (kernel 2, 4 lanes, 4 entries in flight, 128 threads)
+    and every pair in two-float terms (ff_all);
   * both meet the mixed bar against the FP64 oracle (per particle
     max |dF_i| / |F_i| <= 1e-5);
   * after the first call on the device, further calls change neither the
@@ -53,7 +54,7 @@ def test_noalloc_matches_regular_entry_two_calls(engine, case):
     p_new = torch.zeros_like(qd)
     p_old = torch.zeros_like(qd)
     opts = engine.make_opts(dt=0.005, cl2=9.0, box=box, precision="mixed", method="gather",
-                            kernel=2, lanes=4, unroll=4, block=128)
+                            kernel=2, lanes=4, unroll=4, block=128, ff_all=True)
     with engine.Context(0) as ctx:
         ctx.set_list_csr(d_np, d_ptr, d_lst, kind="full")
         for call in range(2):
