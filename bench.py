@@ -1,26 +1,36 @@
 #!/usr/bin/env python
 """Benchmark of the Lennard-Jones neighbour-list force path on GB300.
 
-Workload (the reference's rho = 0.5 comparison case at 108,000 particles):
-FCC 30^3 cells x 4 = 108,000 particles, rho = 0.5, periodic cubic box
-L = (N / rho)^(1/3) = 60, jitter U[-0.05, 0.05) per coordinate from
-mt19937_64(20240601), cutoff 3.0 (CL2 = 9), search radius 3.3, i-sorted int32
-CSR half list (~37.6 partners per particle) built on the device, AoS double4
-and SoA positions, dt = 0.005.
+Default workload (md_8m): the large single system -- FCC 126^3 cells x 4 =
+8,001,504 particles, rho = 1, periodic cubic box L = (N / rho)^(1/3) =
+200.0, jitter U[-0.05, 0.05) per coordinate from mt19937_64(20240601),
+Maxwell-Boltzmann momenta at T* = 1, cutoff 3.0, skin 0.3 (list radius 3.3),
+velocity Verlet at dt = 0.005 with the neighbour list rebuilt on the device
+every 20 steps.  Mixed precision and plain FP64 run back to back from the
+same initial state, each in its own context.
 
-A step is one force call (p += F dt over the whole system).  L2 is flushed
-(512 MiB write) before every timed step; each step is timed with CUDA events
-on the engine's stream.  `value` is the best mixed-precision variant in
-G pair-interactions/s = P_half / t_call / 1e9 (P_half = i<j list pairs, the
-same count for gather and scatter); the FP64 path is reported beside it.
+A step is one MD step (drift, guarded rebuild, force kick).  W warm-up
+steps, then K steps timed with CUDA events on the engine's stream, bracketed
+by a barrier and a device synchronize.  `value` = P_half / t_step / 1e9 in
+G pair-interactions/s, P_half = i<j pairs within the list radius at the last
+build (the reference's count).  The working set (list rows 9.2 GB, positions
+and images 0.5 GB) is far larger than L2, so no flush is needed.  The force
+errors (per-particle max and RMS relative |dF| / |F|, and max |dF| / rms |F|)
+compare the mixed force of the final MD positions with the oracle's FP64
+force over the same list.
 
-e2e runs the reference's measure() through the C ABI (lj_measure_aos): host
-q, p and the CSR list uploaded from pinned memory, 100 force calls, p
-downloaded, every step.
+e2e: per step, the pinned host q and p copied to the device, lj_md_run over
+20 steps (one rebuild period, including its list build), q and p copied back.
 
 --impl reference times the reference's CPU force routine restated in C (the
 oracle; gather over the full list on every host core, project-written
-OpenMP -- the reference itself is single-threaded) on the same workload.
+OpenMP -- the reference itself is single-threaded) on the same 8M system, one
+sixteenth of the rows per step.
+
+Other workloads (--workload): rho0.5_108k / rho1_108k (one force call of the
+108,000-particle comparison cases, every variant), precision_1m (1,000 MD
+steps at 1,000,188 particles with force errors every 100 steps) and
+batch_512 (512 replicas in one batched MD loop).
 """
 from __future__ import annotations
 
@@ -45,15 +55,19 @@ METRIC = "G pair-interactions/s, mixed vs plain FP64, same GB300, force rel err 
 UNIT = "G pair-interactions/s"
 WORKLOAD = ("LJ force call, FCC 108,000 particles, rho=0.5, periodic L=60, rc=3.0, "
             "search 3.3, i-sorted int32 CSR, dt=0.005")
+NCELL_8M, REBUILD_8M, E2E_CHUNK = 126, 20, 20
+WORKLOAD_8M = ("LJ MD step, FCC 8,001,504 particles, rho=1, periodic L=200, MB momenta "
+               "T*=1, rc=3.0, skin 0.3, device list rebuild every 20 steps, velocity "
+               "Verlet dt=0.005; mixed and FP64 back to back")
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="time the 'auto' variants with the engine's default launch shapes "
@@ -63,14 +77,13 @@ def parse():
     ap.add_argument("--shape", action="append", default=[],
                     help="extra mixed AoS gather variant KERNEL,LANES,UNROLL (e.g. 3,4,2 for "
                          "the cell-tiled kernel), timed beside the default variants")
-    ap.add_argument("--workload", default="rho0.5_108k",
-                    choices=["rho0.5_108k", "rho1_108k", "precision_1m", "large_8m",
-                             "batch_512"],
-                    help="rho0.5_108k: the headline force benchmark; rho1_108k: the same at "
-                         "rho = 1; precision_1m: 1,000,188-particle mixed MD with force "
-                         "errors against FP64 every 100 steps; large_8m: 8,001,504-particle "
-                         "MD, mixed and FP64 back to back; batch_512: 512 replicas of "
-                         "uneven N in one mixed MD loop")
+    ap.add_argument("--workload", default="md_8m",
+                    choices=["md_8m", "rho0.5_108k", "rho1_108k", "precision_1m", "batch_512"],
+                    help="md_8m: 8,001,504-particle MD, mixed and FP64 back to back (the "
+                         "headline); rho0.5_108k / rho1_108k: one force call of the 108,000-"
+                         "particle cases, every variant; precision_1m: 1,000,188-particle "
+                         "mixed MD with force errors every 100 steps; batch_512: 512 "
+                         "replicas of uneven N in one mixed MD loop")
     return ap.parse_args()
 
 
@@ -311,11 +324,6 @@ def profiled_metric(name, metric):
     return None
 
 
-# FP64 add / FMA issue rate measured on this machine's GB300 (one op per lane):
-# 503 G/s, i.e. ~1.0 TFLOP/s counting an FMA as two
-FP64_PEAK_OPS = 503e9
-
-
 def pair_kernel_bytes(method, layout, P, N):
     """Compulsory bytes of the pair kernel alone: list indices, the 16-byte
     fixed-point image read once, number_of_partners + pointer, p read +
@@ -521,17 +529,16 @@ def run_ours(args, dist, density=DENSITY):
     fp_m, fp_l = best_fp64.split("/")[1], best_fp64.split("/")[2]
     if fp_m == "auto":
         fp_m = tuned["fp64"]["method"]
-    # FP64 arithmetic per pair inside the cutoff (scatter): 20 FP64 ops; the
-    # inside fraction of a search-radius list is (rc / rs)^3 for a uniform
-    # density
-    inside = (RC / RS) ** 3
-    dp_ops = P * inside * (20 if fp_m == "scatter" else 34)
+    # the FP64 pipe's busy fraction comes from the committed ncu capture of
+    # the FP64 scatter on this workload (a counter, not a model)
+    fp_prof = "force_fp64_scatter_108k_rho0.5.txt"
+    fp_pipe = (profiled_metric(fp_prof, "sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active")
+               if density == DENSITY and fp_m == "scatter" else None)
     fp64 = {"value": fp["gpairs"], "variant": best_fp64, "ms_per_call": fp["s_per_call"] * 1e3,
             "pair_kernel_ms": t_pair64_ms,
             "hbm_frac": algorithmic_bytes(fp_m, fp_l, P, N) / fp["s_per_call"] / 1e9 / hbm,
-            "fp64_ops_per_call": dp_ops,
-            "fp64_pipe_frac": dp_ops / (t_pair64_ms * 1e-3) / FP64_PEAK_OPS,
-            "fp64_peak_ops_per_s": FP64_PEAK_OPS,
+            "fp64_pipe_frac": fp_pipe / 100 if fp_pipe is not None else None,
+            "fp64_pipe_frac_source": f"profiles/{fp_prof}" if fp_pipe is not None else None,
             "mixed_over_fp64": head["gpairs"] / fp["gpairs"]}
 
     cpu = None
@@ -642,45 +649,196 @@ def run_precision(args, dist):
                     "engine's FP64 path on the same positions"}
 
 
-def run_large(args, dist):
-    """8,001,504 particles (FCC 126^3 x 4), rho = 1, rc 3.0, skin 0.3, MB
-    momenta at T* = 1, 500 steps at dt = 0.005 with a rebuild every 20 steps,
-    mixed then FP64 from the same initial state."""
+def per_particle_errors(test, ref):
+    """Relative force errors of `test` against `ref` (N x 3 arrays): the
+    per-particle max and RMS of |dF_i| / |F_i|, and max |dF_i| / rms |F|."""
+    d = np.linalg.norm(test - ref, axis=1)
+    r = np.linalg.norm(ref, axis=1)
+    per = d / np.where(r > 0, r, np.inf)
+    return {"max_rel": float(per.max()), "rms_rel": float(np.sqrt(np.mean(per * per))),
+            "max_rel_rms": float(d.max() / np.sqrt(np.mean(r * r)))}
+
+
+def run_md8m(args, dist):
+    """The large single system, mixed then FP64 from the same initial state
+    (see the module docstring)."""
     import torch
     import lj_gpu_gb300 as lj
     from lj_gpu_gb300 import _build
     _build.build()
     dev = torch.device("cuda", dist.local)
     torch.cuda.set_device(dev)
-    steps = 500 if args.steps >= 100 else args.steps
-    q, L = lj.init_fcc(126, 1.0, JITTER, SEED)
+    stream = torch.cuda.current_stream()
+    q, L = lj.init_fcc(NCELL_8M, 1.0, JITTER, SEED)
     N = q.shape[0]
-    p = lj.init_momenta(N, 1.0, SEED + 1)
-    hbm, _ = peaks()
-    out = {"metric": "MD ns/step and HBM GB/s, mixed vs FP64", "workload": "large_8m", "N": N,
-           "box": L, "steps": steps, "dt": DT, "rebuild_every": 20}
+    p0 = lj.init_momenta(N, 1.0, SEED + 1)
+    K, W = args.steps, args.warmup
+    hbm, peak_kind = peaks()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    runs, final_q = {}, {}
     for prec in ("mixed", "fp64"):
-        qd, pd = torch.from_numpy(q).to(dev), torch.from_numpy(p).to(dev)
-        ctx = lj.Context(dist.local, stream=torch.cuda.current_stream())
-        prm = lj.make_md_params(DT, RC, RS - RC, L, precision=prec, record_every=steps,
-                                rebuild_every=20)
+        qd, pd = torch.from_numpy(q).to(dev), torch.from_numpy(p0).to(dev)
+        ctx = lj.Context(dist.local, stream=stream)
+        prm = lj.make_md_params(DT, RC, RS - RC, L, precision=prec, rebuild_every=REBUILD_8M)
+        ctx.md_run(qd, pd, prm, W, max_records=0)  # warm-up: its own build + W steps
+        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        torch.cuda.synchronize()
+        dist.barrier()
         with ClockSampler(dist.local) as cs:
-            recs, st = ctx.md_run(qd, pd, prm, steps)
-        ctx.build_list(qd, RS, box=L, kinds=("half",))
+            ev[0].record(stream)
+            _, st = ctx.md_run(qd, pd, prm, K, max_records=0)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+        dist.barrier()
+        t_step = dist.max(ev[0].elapsed_time(ev[1]) / K / 1e3, dev)
+        # the list at the final positions: its pair count, and the pair
+        # kernel of a force call over it timed on the engine's stream (the MD
+        # step runs the same kernel over padded rows inside a graph)
+        ctx.build_list(qd, RS, box=L)
         _, P, _ = ctx.list_info("half")
-        ctx.close()
-        ms = st["ms_total"] / steps
-        step_bytes = md_step_bytes(P, N, 1 / 20, mixed=prec == "mixed")
-        out[prec] = {"ms_per_step": ms, "ns_per_step_per_particle": ms * 1e6 / N,
-                     "gpairs": P / (ms * 1e-3) / 1e9, "hbm_gbs": step_bytes / (ms * 1e-3) / 1e9,
-                     "hbm_frac": step_bytes / (ms * 1e-3) / 1e9 / hbm,
-                     "rebuilds": st["rebuilds"], "pairs_half": P,
-                     "energy_first_last": [recs[0][1] + recs[0][2], recs[-1][1] + recs[-1][2]],
-                     "clocks": cs.summary()}
-        del qd, pd
-        torch.cuda.empty_cache()
-    out["mixed_over_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
-    return out
+        opts = lj.make_opts(dt=DT, cl2=RC * RC, box=L, precision=prec,
+                            method="gather" if prec == "mixed" else "scatter")
+        pk = torch.zeros_like(qd)
+        for _ in range(3):
+            flush.add_(1.0)
+            ctx.force_aos(qd, pk, opts)
+        torch.cuda.synchronize()
+        ctx.set_timing(True)
+        for _ in range(10):
+            flush.add_(1.0)
+            ctx.force_aos(qd, pk, opts)
+        torch.cuda.synchronize()
+        tm = ctx.get_timing()
+        ctx.set_timing(False)
+        runs[prec] = {"t_step": t_step, "P": P, "stats": st, "clocks": cs.summary(),
+                      "pair_ms": tm[1] / tm[3], "image_ms": tm[0] / tm[3]}
+        if prec == "mixed":
+            final_q["mixed"] = qd
+            keep_ctx = ctx
+        else:
+            ctx.close()
+        del pd, pk
+    ctx = keep_ctx
+    qd = final_q["mixed"]
+    P = runs["mixed"]["P"]
+
+    # forces of the final mixed positions: mixed and FP64 engine paths, and
+    # the oracle's FP64 gather over the same (device-built) full list
+    def force_of(prec):
+        pz = torch.zeros_like(qd)
+        ctx.force_aos(qd, pz, lj.make_opts(dt=1.0, cl2=RC * RC, box=L, precision=prec,
+                                            method="gather" if prec == "mixed" else "scatter"))
+        torch.cuda.synchronize()
+        return pz[:, :3].cpu().numpy()
+    f_mixed, f_fp64 = force_of("mixed"), force_of("fp64")
+    errors = {"vs_engine_fp64": per_particle_errors(f_mixed, f_fp64)}
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_lib as ol
+        npp, ptr_, lst = ctx.get_list_csr("full")
+        qh = qd.cpu().numpy()
+        threads = ol.oracle().lj_or_max_threads()
+        po = np.zeros_like(qh)
+        t0 = time.perf_counter()
+        ol.force_gather_aos(qh, po, npp, ptr_, lst, cl2=RC * RC, dt=1.0, box=L, threads=threads)
+        t_cpu = time.perf_counter() - t0
+        errors["vs_oracle"] = per_particle_errors(f_mixed, po[:, :3])
+        errors["fp64_vs_oracle"] = per_particle_errors(f_fp64, po[:, :3])
+        cpu = {"value": P / t_cpu / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+               "cpu": cpu_model(), "nproc": os.cpu_count(), "seconds": t_cpu,
+               "sample": "one full-list force call of the 8,001,504-particle system at the "
+                         "final mixed MD positions (OpenMP gather over every host core, "
+                         "project-written parallelisation); value counts its P_half pairs"}
+        del npp, ptr_, lst
+    err = errors.get("vs_oracle", errors["vs_engine_fp64"])
+
+    # e2e: pinned host state in, lj_md_run over one rebuild period, state out
+    e2e = None
+    if args.e2e_steps > 0:
+        hq = torch.from_numpy(q).pin_memory()
+        hp = torch.from_numpy(p0).pin_memory()
+        oq, op = torch.empty_like(hq).pin_memory(), torch.empty_like(hp).pin_memory()
+        prm = lj.make_md_params(DT, RC, RS - RC, L, precision="mixed", rebuild_every=REBUILD_8M)
+        qe, pe = torch.empty_like(qd), torch.empty_like(qd)
+
+        def e2e_step():
+            qe.copy_(hq, non_blocking=True)
+            pe.copy_(hp, non_blocking=True)
+            ctx.md_run(qe, pe, prm, E2E_CHUNK, max_records=0)
+            oq.copy_(qe, non_blocking=True)
+            op.copy_(pe, non_blocking=True)
+            torch.cuda.synchronize()
+        e2e_step()  # warm-up
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        t_e = dist.max((time.perf_counter() - t0) / args.e2e_steps, dev)
+        nbytes = hq.numel() * 8 + hp.numel() * 8
+        e2e = {"value": dist.world * P * E2E_CHUNK / t_e / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": int(nbytes), "d2h_bytes_per_step": int(nbytes),
+               "ms_per_step": t_e * 1e3,
+               "step": f"pinned host q, p -> device, lj_md_run of {E2E_CHUNK} MD steps (its "
+                       "list build included), q, p -> host; host wall clock",
+               "md_steps_per_step": E2E_CHUNK}
+    ctx.close()
+
+    mx, fp = runs["mixed"], runs["fp64"]
+    alg = pair_kernel_bytes("gather", "aos", P, N)
+    prof = "force_mixed_gather_md_1m.txt"
+    tr1m = profiled_traffic(prof)
+    # the 1M capture's DRAM bytes scaled to this launch by the list entries
+    # (traffic grows with the entries; the image and p terms scale with N alike)
+    traffic = tr1m * (P / 75_400_000) if tr1m else None
+    roofline = {"bound": "hbm", "achieved": alg / (mx["pair_ms"] * 1e-3) / 1e9, "peak": hbm,
+                "unit": "GB/s", "frac": alg / (mx["pair_ms"] * 1e-3) / 1e9 / hbm,
+                "traffic": traffic,
+                "traffic_source": (f"profiles/{prof}, scaled by list entries from the 1,000,188-"
+                                   "particle capture") if traffic else None,
+                "peak_kind": peak_kind,
+                "kernel": "k_gather_mixed_u (two-float split gather, 4 lanes per row, 4 entries "
+                          "in flight), timed in force calls at the final MD positions",
+                "algorithmic_bytes_per_launch": alg, "kernel_ms": mx["pair_ms"],
+                "position_image_ms": mx["image_ms"],
+                "md_step_bytes": md_step_bytes(P, N, 1 / REBUILD_8M),
+                "md_step_frac": md_step_bytes(P, N, 1 / REBUILD_8M) / mx["t_step"] / 1e9 / hbm}
+    iss = profiled_metric(prof, "smsp__issue_active.avg.pct_of_peak_sustained_active")
+    if iss is not None:
+        roofline["issue_active_frac"] = iss / 100
+    fp_prof = "force_fp64_scatter_md_1m.txt"
+    fp_pipe = profiled_metric(fp_prof, "sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active")
+    fp64 = {"value": dist.world * fp["P"] / fp["t_step"] / 1e9, "ms_per_step": fp["t_step"] * 1e3,
+            "pairs_half": fp["P"], "pair_kernel_ms": fp["pair_ms"],
+            "kernel": "k_scatter_fp64_c (compacted half-list scatter)",
+            "md_step_hbm_frac": md_step_bytes(fp["P"], N, 1 / REBUILD_8M, mixed=False)
+            / fp["t_step"] / 1e9 / hbm,
+            "fp64_pipe_frac": fp_pipe / 100 if fp_pipe is not None else None,
+            "fp64_pipe_frac_source": f"profiles/{fp_prof}" if fp_pipe is not None else None,
+            "rebuilds": fp["stats"]["rebuilds"], "gpu_launches": fp["stats"]["launches"],
+            "clocks": fp["clocks"]}
+    line = {
+        "metric": METRIC, "value": dist.world * P / mx["t_step"] / 1e9, "unit": UNIT,
+        "n_gpus": dist.world, "steps": K, "warmup": W, "ms_per_step": mx["t_step"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 two-float pair math, f64 q/p", "data": "synthetic",
+        "config": {"workload": WORKLOAD_8M, "N": N, "box": L, "pairs_half": P,
+                   "step": "one MD step (drift, guarded rebuild, force kick)",
+                   "rebuild_every": REBUILD_8M, "rebuilds": mx["stats"]["rebuilds"],
+                   "l2": "working set (list rows ~9 GB) far larger than L2; no flush",
+                   "parallelism": f"replicas x{dist.world}"},
+        "force_error": dict(err, reference="oracle FP64 gather" if "vs_oracle" in errors
+                            else "engine FP64 path", positions="final mixed MD state"),
+        "force_errors": errors,
+        "fp64": fp64,
+        "mixed_over_fp64": {"md_step": fp["t_step"] / mx["t_step"],
+                            "pair_kernel": fp["pair_ms"] / mx["pair_ms"]},
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+        "clocks": mx["clocks"], "gpu_launches": mx["stats"]["launches"],
+        "gpu_launches_note": "kernels of the timed mixed lj_md_run (graph nodes counted by "
+                             "the engine)",
+    }
+    return line
 
 
 def run_batch(args, dist):
@@ -790,30 +948,54 @@ def run_reference(args, dist):
         return None
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_lib as ol
-    q, L = ol.init_fcc_periodic(NCELL, DENSITY, JITTER, SEED)
-    full = ol.build_list(q, RS, box=L, full=True)
-    half = ol.build_list(q, RS, box=L)
-    P = len(half[2])
     threads = ol.oracle().lj_or_max_threads()
-    p = np.zeros_like(q)
-    for _ in range(args.warmup):
-        ol.force_gather_aos(q, p, *full, cl2=RC * RC, dt=DT, box=L, threads=threads)
-    t0 = time.perf_counter()
-    ol.force_gather_aos(q, p, *full, cl2=RC * RC, dt=DT, box=L, calls=args.steps,
-                        threads=threads)
-    t = time.perf_counter() - t0
+    if args.workload == "md_8m":
+        # the 8,001,504-particle system; a step is the force call over one
+        # sixteenth of its rows (a fixed slice, its list built once)
+        q, L = ol.init_fcc_periodic(NCELL_8M, 1.0, JITTER, SEED)
+        n = q.shape[0]
+        row1 = n // 16
+        npp, ptr_, lst = ol.build_rows(q, RS, 0, row1, box=L, full=True)
+        P = int(npp.sum()) // 2  # the slice's share of the half-list pairs
+        p = np.zeros_like(q)
+        for _ in range(args.warmup):
+            ol.force_gather_rows_aos(q, p, 0, npp, ptr_, lst, cl2=RC * RC, dt=DT, box=L,
+                                     threads=threads)
+        t0 = time.perf_counter()
+        ol.force_gather_rows_aos(q, p, 0, npp, ptr_, lst, cl2=RC * RC, dt=DT, box=L,
+                                 calls=args.steps, threads=threads)
+        t = time.perf_counter() - t0
+        workload, sample = WORKLOAD_8M, (
+            f"every step is the force call over rows 0..{row1 - 1} (1/16) of the "
+            "8,001,504-particle system, full-list gather (C restatement of the reference "
+            "routine, project-written OpenMP); value counts that slice's P_half share")
+        config = {"workload": workload, "N": n, "rows_per_step": row1, "pairs_half": P,
+                  "step": "force call over 1/16 of the rows", "parallelism": "host cores"}
+    else:
+        q, L = ol.init_fcc_periodic(NCELL, DENSITY, JITTER, SEED)
+        full = ol.build_list(q, RS, box=L, full=True)
+        half = ol.build_list(q, RS, box=L)
+        P = len(half[2])
+        p = np.zeros_like(q)
+        for _ in range(args.warmup):
+            ol.force_gather_aos(q, p, *full, cl2=RC * RC, dt=DT, box=L, threads=threads)
+        t0 = time.perf_counter()
+        ol.force_gather_aos(q, p, *full, cl2=RC * RC, dt=DT, box=L, calls=args.steps,
+                            threads=threads)
+        t = time.perf_counter() - t0
+        workload, sample = WORKLOAD, ("every step is one full force call of the workload "
+                                      "(C restatement of the reference routine, OpenMP "
+                                      "gather)")
+        config = {"workload": workload, "N": q.shape[0], "pairs_half": P,
+                  "step": "one force call", "parallelism": "host cores"}
     v = P * args.steps / t / 1e9
     return {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic",
-        "config": {"workload": WORKLOAD, "N": q.shape[0], "pairs_half": P,
-                   "step": "one force call", "parallelism": "host cores"},
+        "data": "synthetic", "config": config,
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "cpu": cpu_model(), "nproc": os.cpu_count(),
-                         "sample": "every step is one full force call of the workload "
-                                   "(C restatement of the reference routine, OpenMP gather)"},
+                         "cpu": cpu_model(), "nproc": os.cpu_count(), "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -825,10 +1007,10 @@ def main():
         line = run_reference(args, dist)
     else:
         dist = Dist("nccl")
-        if args.workload == "precision_1m":
+        if args.workload == "md_8m":
+            line = run_md8m(args, dist)
+        elif args.workload == "precision_1m":
             line = run_precision(args, dist)
-        elif args.workload == "large_8m":
-            line = run_large(args, dist)
         elif args.workload == "batch_512":
             line = run_batch(args, dist)
         else:

@@ -297,6 +297,7 @@ typedef struct lj_md_stats {
   int64_t rebuilds;       /* list builds after the initial one */
   double ms_total;        /* device time of the whole run */
   int64_t list_capacity;  /* entries reserved for the list */
+  int64_t launches;       /* kernels launched by the run (-1: not counted) */
 } lj_md_stats;
 
 /* q, p: AoS device arrays (modified in place; p must hold the initial

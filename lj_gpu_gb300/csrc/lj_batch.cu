@@ -508,6 +508,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     stats->rebuilds = f[B_COUNT] - 1;  // the initial build is counted by the finish kernel
     stats->ms_total = ms;
     stats->list_capacity = (int64_t)n_total * b.maxrow;
+    stats->launches = -1;
   }
   if (n_records) *n_records = nrec;
   return LJ_OK;

@@ -56,10 +56,10 @@ struct DevList {
   int64_t aentries = 0;
   bool avalid = false;
   Csr acsr() const { return Csr{n, entries, np.ptr, aptr.ptr, alist.ptr, 0, 1}; }
-  // near-first copies of list and alist (k_partition_near, made from the
-  // positions of the first two-float gather after the list changed) with
-  // their near counts; reset whenever the list changes
-  DevBuf<int32_t> slist, snn, salist, sann;
+  // copies of list and alist with rows ordered near | in range | beyond
+  // (k_partition_near, from the positions of the first two-float gather
+  // after the list changed); reset whenever the list changes
+  DevBuf<int32_t> slist, salist;
   bool svalid = false, savalid = false;
 };
 

@@ -26,7 +26,7 @@ cudaError_t launch_mixed_ff_gather(const ForceLaunch& L, const MixedConsts& K, c
       });
     });
   }
-  if (L.csr.nn) return launch_mixed_ff_split(L, K, s);  // near-first rows
+  if (L.split) return launch_mixed_ff_split(L, K, s);  // ordered rows
   auto go = [&](auto u) -> cudaError_t {
     constexpr int U = decltype(u)::value;
     return dispatch_lanes(L.lanes, [&](auto g) {

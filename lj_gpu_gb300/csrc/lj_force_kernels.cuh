@@ -677,13 +677,18 @@ __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const C
 // U terms of one step are summed in FP32 and the step sum enters the Kahan
 // accumulator, so compensation costs 12/U operations per pair.  FF: every
 // term is a two-float pair term (lj_ff.cuh) entering the compensated sums on
-// its own.
+// its own.  SPLIT (with FF, over rows ordered by k_partition_near): a warp
+// step whose pairs are all farther than K.near2 (2.2 sigma) takes FP32 terms
+// instead, and one whose pairs all lie beyond the cutoff band takes none; the
+// decision uses the step's own r2, so the order of the rows sets the speed,
+// never the precision.
 // Accepts padded rows (C.ptr == nullptr, row i at i * C.stride).  VEC
 // (U == 4, rows on 16-byte boundaries and readable to a multiple of 4): lane
 // l of a row takes the 4 consecutive entries base + 4 l .. + 3 with one
 // 16-byte load, which quarters the index-load instructions and the L1
 // wavefronts they cost (a 32-lane scalar index load touches one line per row).
-template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC = false, bool FF = false>
+template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC = false, bool FF = false,
+          bool SPLIT = false>
 __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const Csr C,
                                                         const int4* __restrict__ qfix,
                                                         const MixedConsts K0) {
@@ -745,15 +750,65 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
     load_idx(base + G * U, jn);
     unsigned border = 0u;
     if constexpr (FF) {
-#pragma unroll
-      for (int u = 0; u < U; u++) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, ok[u], border, u);
-      if (__any_sync(kFullMask, border != 0u)) {
+      bool two_float = true;
+      if constexpr (SPLIT) {
+        // the warp step's own r2 (FP32, coarse image) picks its arithmetic:
+        // two-float terms if any pair is closer than K.near2, else FP32
+        // terms if any is inside the cutoff band, else none
+        bool nr = false, inr = false;
 #pragma unroll
         for (int u = 0; u < U; u++) {
-          if (!(border & (1u << u))) continue;
-          const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, jj[u]), K.f64);
-          if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
-          pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 1, true, border, u);
+          const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
+          const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+          nr |= ok[u] && r2 < K.near2;
+          inr |= ok[u] && r2 <= K.cl2s_hi;
+        }
+        two_float = __any_sync(kFullMask, nr);
+        if (!two_float && __any_sync(kFullMask, inr)) {
+          float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+          for (int u = 0; u < U; u++) {
+            const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
+            const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+            const bool in = ok[u] && r2 <= K.cl2s_lo;
+            if (ok[u] && r2 > K.cl2s_lo && r2 <= K.cl2s_hi) border |= 1u << u;
+            float df = df_mixed<ANISO>(r2, K);
+            df = in ? df : 0.0f;
+            sx = fmaf(df, d.x, sx);
+            sy = fmaf(df, d.y, sy);
+            sz = fmaf(df, d.z, sz);
+          }
+          if (__any_sync(kFullMask, border != 0u)) {
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+              if (!(border & (1u << u))) continue;
+              const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, jj[u]), K.f64);
+              if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
+              const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
+              const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+              const float df = df_mixed<ANISO>(r2, K);
+              sx = fmaf(df, d.x, sx);
+              sy = fmaf(df, d.y, sy);
+              sz = fmaf(df, d.z, sz);
+            }
+          }
+          // FP32 terms carry the 24 of df; the two-float sums and kick do not
+          acc.x.add_parts(__fmul_rn(sx, 0.041666668f), 0.f);
+          acc.y.add_parts(__fmul_rn(sy, 0.041666668f), 0.f);
+          acc.z.add_parts(__fmul_rn(sz, 0.041666668f), 0.f);
+        }
+      }
+      if (two_float) {
+#pragma unroll
+        for (int u = 0; u < U; u++) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, ok[u], border, u);
+        if (__any_sync(kFullMask, border != 0u)) {
+#pragma unroll
+          for (int u = 0; u < U; u++) {
+            if (!(border & (1u << u))) continue;
+            const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, jj[u]), K.f64);
+            if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
+            pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 1, true, border, u);
+          }
         }
       }
     } else {
@@ -799,196 +854,15 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
   kick_group<SOA, G, FF>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
 }
 
-// Two-float gather over a near-first list (kernel 2 with the near/far split,
-// rows ordered by k_partition_near, C.nn[i] near entries first).  The near
-// segment [0, nn) runs the two-float pair terms of k_gather_mixed_u; the far
-// segment [nn, cnt) runs FP32 pair terms from the coarse image (the FP32
-// kernels' arithmetic, with their cutoff band), summed apart in compensated
-// FP32.  A far entry closer than K.near2 -- a pair that moved in since the
-// ordering -- is evaluated in two-float arithmetic all the same, so the
-// ordering only decides the speed, never the precision.  VEC as in
-// k_gather_mixed_u: the far segment starts at nn rounded down to a multiple
-// of 4 with the entries before nn masked.
-template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC>
-__global__ void __launch_bounds__(256) k_gather_mixed_split(const Particles P, const Csr C,
-                                                            const int4* __restrict__ qfix,
-                                                            const MixedConsts K0) {
-  static_assert(!VEC || U == 4, "vector index loads take 4 entries per lane");
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = t / G;
-  const int lane = t & (G - 1);
-  // launched as a programmatic dependent of the image pass
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  const MixedConsts K = PBC ? K0 : frame_consts(K0);
-  const bool valid = i < C.n;
-  int cnt = 0, nn = 0;
-  int64_t k0 = 0;
-  int4 xi = make_int4(0, 0, 0, 0);
-  if (valid) {
-    cnt = __ldg(C.np + i);
-    nn = __ldg(C.nn + i);
-    k0 = row_start(C, i);
-    xi = __ldg(qfix + i);
-  }
-  int li[3];
-  image_lo(xi.w, li[0], li[1], li[2]);
-  RowSums<true> acc;    // two-float terms
-  RowSums<false> acc32;  // FP32 terms of the far segment
-  acc.init();
-  acc32.init();
-  // entry `base` + (lane, u) of a segment starting at entry `from`
-  auto entry = [&](int base, int u) { return VEC ? base + 4 * lane + u : base + lane + u * G; };
-  auto load_idx = [&](int from, int lim, int base, int* jn) {
-    if (VEC) {
-      int4 v = make_int4(0, 0, 0, 0);
-      if (from + entry(base, 0) < lim)
-        v = __ldg(reinterpret_cast<const int4*>(C.list + k0 + from + entry(base, 0)));
-      jn[0] = v.x;
-      jn[1] = v.y;
-      jn[2] = v.z;
-      jn[3] = v.w;
-    } else {
-#pragma unroll
-      for (int u = 0; u < U; u++)
-        jn[u] = from + entry(base, u) < lim ? __ldg(C.list + k0 + from + entry(base, u)) : 0;
-    }
-  };
-  // FP64 re-decision of a pair in the cutoff band (either term type)
-  auto inside64 = [&](int j) {
-    const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, j), K.f64);
-    return !beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits);
-  };
-  // ---- near segment [0, nn): two-float terms
-  {
-    int cmax = nn;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-      cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
-    int jn[U];
-    load_idx(0, nn, 0, jn);
-    for (int base = 0; base < cmax; base += G * U) {
-      int jj[U];
-      bool ok[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        ok[u] = entry(base, u) < nn;
-        jj[u] = ok[u] ? jn[u] : 0;
-      }
-      int4 xj[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
-      load_idx(0, nn, base + G * U, jn);
-      unsigned border = 0u;
-#pragma unroll
-      for (int u = 0; u < U; u++) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, ok[u], border, u);
-      if (__any_sync(kFullMask, border != 0u)) {
-#pragma unroll
-        for (int u = 0; u < U; u++)
-          if ((border & (1u << u)) && inside64(jj[u]))
-            pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 1, true, border, u);
-      }
-    }
-  }
-  // ---- far segment [nn, cnt): FP32 terms
-  {
-    const int from = VEC ? (nn & ~3) : nn;
-    int cmax = cnt - from;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-      cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
-    int jn[U];
-    load_idx(from, cnt, 0, jn);
-    for (int base = 0; base < cmax; base += G * U) {
-      int jj[U];
-      bool ok[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const int e = from + entry(base, u);
-        ok[u] = e >= nn && e < cnt;
-        jj[u] = ok[u] ? jn[u] : 0;
-      }
-      int4 xj[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
-      load_idx(from, cnt, base + G * U, jn);
-      float sx = 0.f, sy = 0.f, sz = 0.f;
-      unsigned border = 0u, near = 0u;
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
-        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-        const bool close = ok[u] && r2 < K.near2;
-        if (close) near |= 1u << u;
-        const bool in = ok[u] && !close && r2 <= K.cl2s_lo;
-        if (ok[u] && !close && r2 > K.cl2s_lo && r2 <= K.cl2s_hi) border |= 1u << u;
-        float df = df_mixed<ANISO>(r2, K);
-        df = in ? df : 0.0f;
-        sx = fmaf(df, d.x, sx);
-        sy = fmaf(df, d.y, sy);
-        sz = fmaf(df, d.z, sz);
-      }
-      if (__any_sync(kFullMask, border != 0u)) {
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-          if (!(border & (1u << u)) || !inside64(jj[u])) continue;
-          const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
-          const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-          const float df = df_mixed<ANISO>(r2, K);
-          sx = fmaf(df, d.x, sx);
-          sy = fmaf(df, d.y, sy);
-          sz = fmaf(df, d.z, sz);
-        }
-      }
-      acc32.x.add(sx);
-      acc32.y.add(sy);
-      acc32.z.add(sz);
-      // pairs that moved inside the near radius: two-float terms
-      if (__any_sync(kFullMask, near != 0u)) {
-        unsigned bff = 0u;
-#pragma unroll
-        for (int u = 0; u < U; u++)
-          if (near & (1u << u)) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, true, bff, u);
-        if (__any_sync(kFullMask, bff != 0u)) {
-#pragma unroll
-          for (int u = 0; u < U; u++)
-            if ((bff & (1u << u)) && inside64(jj[u]))
-              pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 1, true, bff, u);
-        }
-      }
-    }
-  }
-  // FP32 sums (Kahan) join the two-float sums; FP32 terms are in pair units
-  // times the FP32 kick scale (fscale / 24 for the two-float kick)
-  float hx, lx, hy, ly, hz, lz, fx, gx, fy, gy, fz, gz;
-  acc.get(hx, lx, hy, ly, hz, lz);
-  acc32.get(fx, gx, fy, gy, fz, gz);
-  auto join = [](float& h, float& l, float f, float g) {
-    const float f24 = __fmul_rn(f, 0.041666668f), g24 = __fmul_rn(g, 0.041666668f);
-    const ff s = ff_two_sum(h, f24);
-    h = s.h;
-    l = __fadd_rn(l, __fadd_rn(s.l, g24));
-  };
-  join(hx, lx, fx, gx);
-  join(hy, ly, fy, gy);
-  join(hz, lz, fz, gz);
-  if (G > 1) {
-    group_reduce_comp<G>(hx, lx);
-    group_reduce_comp<G>(hy, ly);
-    group_reduce_comp<G>(hz, lz);
-  }
-  kick_group<SOA, G, true>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
-}
-
-// Orders every row near-first for k_gather_mixed_split: entries with FP32 r2
-// (coarse image) below K.near_build2 first, in list order, the others after
-// them in reverse list order; nn[i] receives the near count.  Rows keep
-// their starts (out has the layout of C).  One warp per row, rows in a
-// grid-stride loop.
+// Orders every row for the split two-float gather: entries with FP32 r2
+// (coarse image) below K.near_build2 first, then those up to the upper edge
+// of the FP32 cutoff band, then the ones beyond; list order within each
+// group.  Rows keep their starts (out has the layout of C).  One warp per
+// row (two passes: count, place), rows in a grid-stride loop.
 template <bool PBC, bool ANISO>
 __global__ void __launch_bounds__(128) k_partition_near(const Csr C, const int4* __restrict__ qfix,
                                                         const MixedConsts K0,
                                                         int32_t* __restrict__ out,
-                                                        int32_t* __restrict__ nn,
                                                         const int32_t* guard) {
   if (guard && *(volatile const int32_t*)guard == 0) return;
   const MixedConsts K = PBC ? K0 : frame_consts(K0);
@@ -999,25 +873,34 @@ __global__ void __launch_bounds__(128) k_partition_near(const Csr C, const int4*
     const int cnt = __ldg(C.np + i);
     const int64_t k0 = row_start(C, i);
     const int4 xi = __ldg(qfix + i);
-    int nacc = 0, facc = 0;
+    // group of entry k: 0 near, 1 in range, 2 beyond the cutoff
+    auto group = [&](int k, int& j) {
+      j = __ldg(C.list + k0 + k);
+      const float3 d = sep_mixed<ANISO>(xi, __ldg(qfix + j), K);
+      const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+      return r2 < K.near_build2 ? 0 : (r2 <= K.cl2s_hi ? 1 : 2);
+    };
+    int n0 = 0, n1 = 0;
     for (int base = 0; base < cnt; base += 32) {
-      const int k = base + lane;
-      const bool ok = k < cnt;
-      int j = 0;
-      bool near = false;
-      if (ok) {
-        j = __ldg(C.list + k0 + k);
-        const float3 d = sep_mixed<ANISO>(xi, __ldg(qfix + j), K);
-        near = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x)) < K.near_build2;
-      }
-      const unsigned bn = __ballot_sync(kFullMask, near);
-      const unsigned bf = __ballot_sync(kFullMask, ok && !near);
-      if (near) out[k0 + nacc + __popc(bn & lt)] = j;
-      else if (ok) out[k0 + cnt - 1 - (facc + __popc(bf & lt))] = j;
-      nacc += __popc(bn);
-      facc += __popc(bf);
+      int j, g = 3;
+      if (base + lane < cnt) g = group(base + lane, j);
+      n0 += __popc(__ballot_sync(kFullMask, g == 0));
+      n1 += __popc(__ballot_sync(kFullMask, g == 1));
     }
-    if (lane == 0) nn[i] = nacc;
+    int c0 = 0, c1 = n0, c2 = n0 + n1;
+    for (int base = 0; base < cnt; base += 32) {
+      int j = 0, g = 3;
+      if (base + lane < cnt) g = group(base + lane, j);
+      const unsigned b0 = __ballot_sync(kFullMask, g == 0);
+      const unsigned b1 = __ballot_sync(kFullMask, g == 1);
+      const unsigned b2 = __ballot_sync(kFullMask, g == 2);
+      if (g == 0) out[k0 + c0 + __popc(b0 & lt)] = j;
+      if (g == 1) out[k0 + c1 + __popc(b1 & lt)] = j;
+      if (g == 2) out[k0 + c2 + __popc(b2 & lt)] = j;
+      c0 += __popc(b0);
+      c1 += __popc(b1);
+      c2 += __popc(b2);
+    }
   }
 }
 

@@ -1,6 +1,6 @@
-// lj_force_split.cu -- launch of the two-float gather with the near/far
-// split (LJ_PREC_MIXED, kernels 2 and 4 over near-first rows): two-float
-// terms for the near segment of every row, FP32 terms for the far segment.
+// lj_force_split.cu -- launch of the split two-float gather (LJ_PREC_MIXED,
+// kernels 2 and 4 over rows ordered near | in range | beyond): each warp step
+// takes two-float, FP32 or no pair terms by its own r2.
 #include "lj_force_kernels.cuh"
 
 namespace ljg {
@@ -18,16 +18,20 @@ cudaError_t launch_mixed_ff_split(const ForceLaunch& L, const MixedConsts& K, cu
         const int4* qf = L.qfix;
         if (U == 4 && L.csr.aligned4) {
           if (L.aniso)
-            return launch_dependent(k_gather_mixed_split<G, 4, P.value, S.value, true, true>,
-                                    blocks, block, s, L.part, L.csr, qf, K);
-          return launch_dependent(k_gather_mixed_split<G, 4, P.value, S.value, false, true>,
-                                  blocks, block, s, L.part, L.csr, qf, K);
+            return launch_dependent(
+                k_gather_mixed_u<G, 4, P.value, S.value, true, true, true, true>, blocks, block,
+                s, L.part, L.csr, qf, K);
+          return launch_dependent(
+              k_gather_mixed_u<G, 4, P.value, S.value, false, true, true, true>, blocks, block, s,
+              L.part, L.csr, qf, K);
         }
         if (L.aniso)
-          return launch_dependent(k_gather_mixed_split<G, U, P.value, S.value, true, false>,
-                                  blocks, block, s, L.part, L.csr, qf, K);
-        return launch_dependent(k_gather_mixed_split<G, U, P.value, S.value, false, false>,
-                                blocks, block, s, L.part, L.csr, qf, K);
+          return launch_dependent(
+              k_gather_mixed_u<G, U, P.value, S.value, true, false, true, true>, blocks, block, s,
+              L.part, L.csr, qf, K);
+        return launch_dependent(
+            k_gather_mixed_u<G, U, P.value, S.value, false, false, true, true>, blocks, block, s,
+            L.part, L.csr, qf, K);
       });
     });
   };

@@ -35,8 +35,6 @@ struct Csr {
   const int32_t* list;
   int64_t stride;
   int aligned4;  // every row starts on a 16-byte boundary and is readable to a multiple of 4
-  // near-first rows (k_partition_near): near entries of row i, or nullptr
-  const int32_t* nn;
 };
 
 __device__ __forceinline__ int64_t row_start(const Csr& c, int i) {
@@ -81,6 +79,9 @@ struct ForceLaunch {
   int block;       // threads per block
   int kernel;      // 1: simple strided, 2: unrolled (mixed) / compacted (FP64)
   int unroll;      // entries in flight per lane (kernel 2, mixed)
+  // two-float gathers: rows ordered near | in range | beyond (k_partition_near);
+  // each warp step then picks two-float, FP32 or no pair terms by its own r2
+  int split;
   // mixed precision only
   int4* qfix;      // n entries, written by the fixed-image pass
   float* fscratch; // 4 n floats, one float4 per particle (scatter-half mixed only)
@@ -144,11 +145,11 @@ cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* 
 
 // Launchers (return cudaError_t of the launch)
 cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s);
-// Near-first copy of the rows of `in` (same row starts) into `out` for the
-// near/far split of two-float gathers (L's frame and cutoff), near counts
-// into nn; L's position image must be current.  `guard` (optional): nothing
+// Copy of the rows of `in` (same row starts) into `out` ordered near | in
+// range | beyond the cutoff for the split two-float gather (L's frame and
+// cutoff); L's position image must be current.  `guard` (optional): nothing
 // happens while *guard == 0.
-cudaError_t launch_partition_near(const ForceLaunch& L, const Csr& in, int32_t* out, int32_t* nn,
+cudaError_t launch_partition_near(const ForceLaunch& L, const Csr& in, int32_t* out,
                                   const int32_t* guard, cudaStream_t s);
 cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s);
 cudaError_t launch_force_pairs(const Particles& part, int n, const int32_t* ip,

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "lj_ctx.h"
 #include "lj_nlist.h"
@@ -175,9 +176,9 @@ struct MdState {
   int maxrow = 0;
   DevBuf<int4> qfix, qref, cq, cq2;
   DevBuf<int32_t> flags, cell, count, cursor, order, order2, cnt, ptr, rows, list;
-  // near-first copy of the padded rows and its near counts (two-float kicks
-  // with the near/far split)
-  DevBuf<int32_t> rows2, nn;
+  // copy of the padded rows ordered near | in range | beyond (split
+  // two-float kicks)
+  DevBuf<int32_t> rows2;
   bool split = false;
   DevBuf<int64_t> start, off;
   DevBuf<unsigned char> scan_tmp;
@@ -227,9 +228,9 @@ cudaError_t md_rebuild(MdState& m, bool compact, const ForceLaunch& kick, cudaSt
   if ((e = launch_build_rows(m.build, m.build.want_half != 0, m.maxrow, m.rows.ptr, m.cnt.ptr,
                              m.flags.ptr + F_OVERFLOW, s, g)))
     return e;
-  if (m.split) {  // near-first rows from the positions of this build
-    const Csr rows{m.n, m.cap, m.cnt.ptr, nullptr, m.rows.ptr, (int64_t)m.maxrow, 1, nullptr};
-    if ((e = launch_partition_near(kick, rows, m.rows2.ptr, m.nn.ptr, g, s))) return e;
+  if (m.split) {  // rows ordered from the positions of this build
+    const Csr rows{m.n, m.cap, m.cnt.ptr, nullptr, m.rows.ptr, (int64_t)m.maxrow, 1};
+    if ((e = launch_partition_near(kick, rows, m.rows2.ptr, g, s))) return e;
   }
   if (compact) {
     if ((e = launch_scan_counts(m.cnt.ptr, m.n, m.off.ptr, m.scan_tmp.ptr, m.scan_tmp.cap, s, g)))
@@ -265,6 +266,20 @@ cudaError_t md_step(MdState& m, const DriftArgs& d, const ForceLaunch& kick, cud
   if (e != cudaSuccess) return e;
   if ((e = md_rebuild(m, kick.method == LJ_METHOD_SCATTER_HALF, kick, s))) return e;
   return launch_force(kick, s);
+}
+
+// Kernel nodes of a captured graph: the kernels one replay launches.
+int64_t graph_kernels(cudaGraph_t g) {
+  size_t n = 0;
+  if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return 0;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return 0;
+  int64_t k = 0;
+  for (size_t a = 0; a < n; a++) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[a], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+  }
+  return k;
 }
 
 }  // namespace
@@ -339,7 +354,6 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   m.split = prm->precision == LJ_PREC_MIXED && !prm->ff_all;
   if (m.split) {
     MD_CUDA(ctx, m.rows2.ensure((size_t)m.cap), "alloc");
-    MD_CUDA(ctx, m.nn.ensure((size_t)n), "alloc");
   }
   // the compacted half list holds about half of the padded capacity
   const int64_t half_cap = std::min<int64_t>(m.cap, 0x7fffffffll);
@@ -354,8 +368,9 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   // mixed: padded rows read in place (64-bit row starts i * maxrow); FP64:
   // compacted rows with int32 offsets
   K.csr = mixed ? Csr{n, m.cap, m.cnt.ptr, nullptr, m.split ? m.rows2.ptr : m.rows.ptr,
-                      (int64_t)m.maxrow, 1, m.split ? m.nn.ptr : nullptr}
-                : Csr{n, m.cap, m.cnt.ptr, m.ptr.ptr, m.list.ptr, 0, 0, nullptr};
+                      (int64_t)m.maxrow, 1}
+                : Csr{n, m.cap, m.cnt.ptr, m.ptr.ptr, m.list.ptr, 0, 0};
+  K.split = m.split ? 1 : 0;
   K.box.on = 1;
   for (int d = 0; d < 3; d++) {
     K.box.len[d] = prm->box[d];
@@ -416,10 +431,30 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   } evg{t0, t1};
   MD_CUDA(ctx, cudaEventRecord(t0, s), "event");
 
-  // ---- initial image and list ----------------------------------------------
-  MD_CUDA(ctx, launch_fixed_image(K, s), "image");
-  k_md_set<<<1, 32, 0, s>>>(m.flags.ptr, F_REBUILD, 1);
-  MD_CUDA(ctx, md_rebuild(m, !mixed, K, s), "initial build");
+  // ---- initial image and list (one captured graph, so that its kernels are
+  // counted) -------------------------------------------------------------------
+  int64_t launches = 0;
+  {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    MD_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
+    cudaError_t ce = launch_fixed_image(K, s);
+    if (ce == cudaSuccess) {
+      k_md_set<<<1, 32, 0, s>>>(m.flags.ptr, F_REBUILD, 1);
+      ce = md_rebuild(m, !mixed, K, s);
+    }
+    cudaError_t ee = cudaStreamEndCapture(s, &g);
+    if (ce == cudaSuccess && ee == cudaSuccess) {
+      launches += graph_kernels(g);
+      ce = cudaGraphInstantiate(&ge, g, 0);
+      if (ce == cudaSuccess) ce = cudaGraphLaunch(ge, s);
+      if (ge) cudaGraphExecDestroy(ge);
+    }
+    if (g) cudaGraphDestroy(g);
+    if (ce != cudaSuccess || ee != cudaSuccess)
+      return lj_fail(ctx, LJ_ERR_CUDA, "initial build: %s",
+                     cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+  }
 
   int32_t nrec = 0;
   auto read_flags = [&](int32_t* f) -> int {
@@ -445,6 +480,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
           q, m.qfix.ptr, c, K.box.len[0], K.box.len[1], K.box.len[2], 0.f, 0.f, 0.f, 0.f, K.cl2,
           m.energy.ptr + 1);
     k_md_kinetic<<<std::min(grid1(n, 256), 1024), 256, 0, s>>>(p, n, m.energy.ptr);
+    launches += 2;
     double e[2];
     MD_CUDA(ctx, cudaGetLastError(), "energy");
     MD_CUDA(ctx, cudaMemcpyAsync(e, m.energy.ptr, sizeof e, cudaMemcpyDeviceToHost, s), "energy");
@@ -465,6 +501,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
 
   // ---- graph of `graph_steps` plain steps ----------------------------------
   const int gsteps = prm->graph_steps > 0 ? prm->graph_steps : 20;
+  int64_t step_kernels = -1;  // kernels of one step (from the captured graph)
   if (m.graph) {
     cudaGraphExecDestroy(m.graph);
     m.graph = nullptr;
@@ -480,6 +517,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
       return lj_fail(ctx, LJ_ERR_CUDA, "graph capture: %s",
                      cudaGetErrorString(ce != cudaSuccess ? ce : ee));
     }
+    step_kernels = graph_kernels(g) / gsteps;
     ce = cudaGraphInstantiate(&m.graph, g, 0);
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) return lj_fail(ctx, LJ_ERR_CUDA, "graph instantiate");
@@ -489,6 +527,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   // ---- integrate -------------------------------------------------------------
   const int every = prm->record_every > 0 ? prm->record_every : nsteps;
   if (nsteps > 0) MD_CUDA(ctx, launch_force(Khalf, s), "kick");  // p(1/2)
+  int64_t kicks = nsteps > 0 ? 1 : 0;  // each launch_force of the MD path is one kernel
   int64_t step = 0;
   while (step < nsteps) {
     int64_t stop = std::min<int64_t>(nsteps, (step / every + 1) * every);
@@ -505,7 +544,10 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
                      "a neighbour row exceeded its capacity of %d entries", m.maxrow);
     if (stop % every == 0 || stop == nsteps)
       if ((rc = record(stop))) return rc;
-    if (stop < nsteps) MD_CUDA(ctx, launch_force(Khalf, s), "kick");
+    if (stop < nsteps) {
+      MD_CUDA(ctx, launch_force(Khalf, s), "kick");
+      kicks++;
+    }
     step = stop;
   }
   MD_CUDA(ctx, cudaEventRecord(t1, s), "event");
@@ -517,6 +559,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     stats->rebuilds = f[F_COUNT] - 1;  // the initial build goes through the same finish
     stats->ms_total = ms;
     stats->list_capacity = m.cap;
+    stats->launches = step_kernels < 0 ? -1 : launches + kicks + nsteps * step_kernels;
   }
   if (n_records) *n_records = nrec;
   if (!ctx->stream) MD_CUDA(ctx, cudaStreamSynchronize(s), "sync");

@@ -223,7 +223,16 @@ static int cmp_i32(const void* a, const void* b) {
 int64_t lj_or_build_list_cells(const double* q4, int n, double sl2, const double* box,
                                int full, int32_t* np, int32_t* ptr, int32_t* list,
                                int64_t cap) {
-  if (n <= 0) return 0;
+  return lj_or_build_rows_cells(q4, n, sl2, box, full, 0, n, np, ptr, list, cap);
+}
+
+/* Rows [row0, row1) of the cell-grid list (np and ptr indexed by i - row0,
+ * ptr relative to list): the rows lj_or_build_list_cells gives for them. */
+int64_t lj_or_build_rows_cells(const double* q4, int n, double sl2, const double* box,
+                               int full, int row0, int row1, int32_t* np, int32_t* ptr,
+                               int32_t* list, int64_t cap) {
+  if (n <= 0 || row0 >= row1) return 0;
+  if (row0 < 0 || row1 > n) return -1;
   const double rs = sqrt(sl2);
   double lo[3], ext[3];
   int nc[3];
@@ -274,7 +283,7 @@ int64_t lj_or_build_list_cells(const double* q4, int n, double sl2, const double
   }
   int64_t pos = 0;
   int overflow = 0;
-  for (int i = 0; i < n && !overflow; i++) {
+  for (int i = row0; i < row1 && !overflow; i++) {
     const int ci = cell_of[i];
     const int cx = ci % nc[0], cy = (ci / nc[0]) % nc[1], cz = ci / (nc[0] * nc[1]);
     int cnt = 0;
@@ -304,8 +313,8 @@ int64_t lj_or_build_list_cells(const double* q4, int n, double sl2, const double
       overflow = 1;
       break;
     }
-    ptr[i] = (int32_t)pos;
-    np[i] = cnt;
+    ptr[i - row0] = (int32_t)pos;
+    np[i - row0] = cnt;
     memcpy(list + pos, row, sizeof(int32_t) * (size_t)cnt);
     pos += cnt;
   }
@@ -442,16 +451,23 @@ int lj_or_max_threads(void) {
 void lj_or_force_gather_aos(const double* q4, double* p4, int n, const int32_t* np,
                             const int32_t* ptr, const int32_t* list, double cl2, double dt,
                             const double* box, int nthreads) {
+  lj_or_force_gather_rows_aos(q4, p4, 0, n, np, ptr, list, cl2, dt, box, nthreads);
+}
+
+/* The gather for rows [row0, row1) only (np, ptr indexed by i - row0). */
+void lj_or_force_gather_rows_aos(const double* q4, double* p4, int row0, int row1,
+                                 const int32_t* np, const int32_t* ptr, const int32_t* list,
+                                 double cl2, double dt, const double* box, int nthreads) {
 #ifdef _OPENMP
   const int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
 #else
   (void)nthreads;
 #endif
-  for (int i = 0; i < n; i++) {
+  for (int i = row0; i < row1; i++) {
     const double qx = q4[4 * i + 0], qy = q4[4 * i + 1], qz = q4[4 * i + 2];
-    const int cnt = np[i];
-    const int kp = ptr[i];
+    const int cnt = np[i - row0];
+    const int kp = ptr[i - row0];
     double pfx = 0, pfy = 0, pfz = 0;
     for (int k = 0; k < cnt; k++) {
       const int j = list[kp + k];

@@ -59,6 +59,10 @@ int64_t lj_or_build_half_brute(const double* q4, int n, double sl2, const double
 int64_t lj_or_build_list_cells(const double* q4, int n, double sl2, const double* box,
                                int full, int32_t* np, int32_t* ptr, int32_t* list,
                                int64_t cap);
+/* rows [row0, row1) of the same list; np, ptr indexed by i - row0 */
+int64_t lj_or_build_rows_cells(const double* q4, int n, double sl2, const double* box, int full,
+                               int row0, int row1, int32_t* np, int32_t* ptr, int32_t* list,
+                               int64_t cap);
 /* (i, j) pair array in makepair order from a CSR half list. */
 void lj_or_csr_to_pairs(int n, const int32_t* np, const int32_t* ptr, const int32_t* list,
                         int32_t* ip, int32_t* jp);
@@ -82,6 +86,10 @@ void lj_or_force_sorted_soa(const double* qx, const double* qy, const double* qz
 void lj_or_force_gather_aos(const double* q4, double* p4, int n, const int32_t* np,
                             const int32_t* ptr, const int32_t* list, double cl2, double dt,
                             const double* box, int nthreads);
+/* the gather over rows [row0, row1); np, ptr indexed by i - row0 */
+void lj_or_force_gather_rows_aos(const double* q4, double* p4, int row0, int row1,
+                                 const int32_t* np, const int32_t* ptr, const int32_t* list,
+                                 double cl2, double dt, const double* box, int nthreads);
 int  lj_or_max_threads(void);
 
 /* ---- energies and integration (project extension: the reference has none) ---- */

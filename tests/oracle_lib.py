@@ -53,6 +53,10 @@ def oracle() -> C.CDLL:
                                               C.c_double, _V]),
             "lj_or_force_sorted_soa": (None, [_dp, _dp, _dp, _dp, _dp, _dp, C.c_int, _ip, _ip,
                                               _ip, C.c_double, C.c_double, _V]),
+            "lj_or_build_rows_cells": (C.c_int64, [_dp, C.c_int, C.c_double, _V, C.c_int,
+                                                   C.c_int, C.c_int, _ip, _ip, _ip, C.c_int64]),
+            "lj_or_force_gather_rows_aos": (None, [_dp, _dp, C.c_int, C.c_int, _ip, _ip, _ip,
+                                                   C.c_double, C.c_double, _V, C.c_int]),
             "lj_or_force_gather_aos": (None, [_dp, _dp, C.c_int, _ip, _ip, _ip, C.c_double,
                                               C.c_double, _V, C.c_int]),
             "lj_or_max_threads": (C.c_int, []),
@@ -109,6 +113,32 @@ def build_list(q, search, box=None, full=False, cap=None):
     if e < 0:
         raise RuntimeError("oracle list overflow")
     return npp, ptr, lst[:e].copy()
+
+
+def build_rows(q, search, row0, row1, box=None, full=False, cap=None):
+    """Rows [row0, row1) of build_list's list (npp, ptr indexed by i - row0)."""
+    n = q.shape[0]
+    m = row1 - row0
+    cap = cap or max(16, int(m * 200))
+    npp = np.zeros(m, np.int32)
+    ptr = np.zeros(m, np.int32)
+    lst = np.zeros(cap, np.int32)
+    b, bp = _box(box)
+    e = oracle().lj_or_build_rows_cells(np.ascontiguousarray(q), n, search * search, bp,
+                                        1 if full else 0, row0, row1, npp, ptr, lst, cap)
+    if e < 0:
+        raise RuntimeError("oracle list overflow")
+    return npp, ptr, lst[:e].copy()
+
+
+def force_gather_rows_aos(q, p, row0, npp, ptr, lst, cl2=9.0, dt=0.001, box=None, calls=1,
+                          threads=1):
+    """The gather over rows [row0, row0 + len(npp)) of a build_rows list."""
+    b, bp = _box(box)
+    for _ in range(calls):
+        oracle().lj_or_force_gather_rows_aos(q, p, row0, row0 + len(npp), npp, ptr, lst, cl2,
+                                             dt, bp, threads)
+    return p
 
 
 def build_half_brute(q, search, box=None):

@@ -25,8 +25,8 @@ def _json_lines(out):
 
 def test_reference_arm_one_rank():
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
-                        "--steps", "2", "--warmup", "1"], capture_output=True, text=True,
-                       timeout=300, cwd=ROOT)
+                        "--workload", "rho0.5_108k", "--steps", "2", "--warmup", "1"],
+                       capture_output=True, text=True, timeout=300, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = _json_lines(r.stdout)
     assert len(lines) == 1
@@ -37,11 +37,26 @@ def test_reference_arm_one_rank():
     assert d["config"]["pairs_half"] == 4212000  # 108,000 particles, rho 0.5, search 3.3
 
 
+def test_reference_arm_large_system_samples_a_sixteenth():
+    """The default workload's reference arm: the 8,001,504-particle system,
+    each step the gather over its first 500,094 rows."""
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                        "--steps", "2", "--warmup", "0"], capture_output=True, text=True,
+                       timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = _json_lines(r.stdout)[0]
+    assert d["config"]["N"] == 8001504 and d["config"]["rows_per_step"] == 500094
+    # the rows' full-list entries / 2: about 75 half pairs per particle at rho 1
+    assert 70 * 500094 < d["config"]["pairs_half"] < 80 * 500094
+    assert d["value"] > 0 and d["e2e"]["value"] == d["value"]
+
+
 def test_reference_arm_two_ranks_prints_one_line():
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "2", "--warmup", "1"]
+           "--impl", "reference", "--workload", "rho0.5_108k", "--gpus", "2", "--steps", "2",
+           "--warmup", "1"]
     env = dict(os.environ, OMP_NUM_THREADS="2")
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
     assert r.returncode == 0, r.stderr[-3000:]

@@ -125,6 +125,23 @@ def test_periodic_forces_newton_third_law():
     assert ol.rel_errors(g, p)["max_rel"] <= 1e-12
 
 
+def test_row_range_list_and_gather_equal_the_full_ones():
+    """build_rows / force_gather_rows_aos (the CPU timing sample of the large
+    system) give the rows and forces of the whole-system list and gather."""
+    q, L = ol.init_fcc_periodic(5, 1.0, 0.05, seed=3)
+    fnp, fptr, flst = ol.build_list(q, 3.3, box=L, full=True)
+    g = ol.force_gather_aos(q, np.zeros_like(q), fnp, fptr, flst, dt=0.005, box=L)
+    for r0, r1 in ((0, 37), (123, 500), (0, q.shape[0])):
+        npp, ptr, lst = ol.build_rows(q, 3.3, r0, r1, box=L, full=True)
+        assert np.array_equal(npp, fnp[r0:r1])
+        assert np.array_equal(lst, flst[fptr[r0]:fptr[r0] + len(lst)])
+        assert np.array_equal(ptr, fptr[r0:r1] - fptr[r0])
+        p = ol.force_gather_rows_aos(q, np.zeros_like(q), r0, npp, ptr, lst, dt=0.005, box=L,
+                                     threads=2)
+        assert np.array_equal(p[r0:r1], g[r0:r1])
+        assert not p[:r0].any() and not p[r1:].any()
+
+
 @pytest.mark.skipif(not ol.ref_available(), reason="reference cpu_ref not built here (x86 only)")
 def test_oracle_bitwise_vs_compiled_reference_random_input():
     """Random positions (not the lattice) through the reference's makepair /
