@@ -298,6 +298,10 @@ typedef struct lj_md_stats {
   double ms_total;        /* device time of the whole run */
   int64_t list_capacity;  /* entries reserved for the list */
   int64_t launches;       /* kernels launched by the run (-1: not counted) */
+  int32_t loop_graph;     /* 1: the steps between records ran as one launch of a
+                             persistent graph (a WHILE node counted down on the
+                             device); 0: as back-to-back chunk graphs */
+  int32_t reserved;
 } lj_md_stats;
 
 /* q, p: AoS device arrays (modified in place; p must hold the initial

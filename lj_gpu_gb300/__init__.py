@@ -91,7 +91,8 @@ class MdRecord(C.Structure):
 
 class MdStats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("rebuilds", C.c_int64), ("ms_total", C.c_double),
-                ("list_capacity", C.c_int64), ("launches", C.c_int64)]
+                ("list_capacity", C.c_int64), ("launches", C.c_int64),
+                ("loop_graph", C.c_int32), ("reserved", C.c_int32)]
 
 
 def make_md_params(dt, rc, skin, box, precision="mixed", record_every=0, graph_steps=0,
@@ -361,7 +362,8 @@ class Context:
         self._check(s, "md_run")
         return ([(recs[k].step, recs[k].kinetic, recs[k].potential) for k in range(nrec.value)],
                 {"steps": st.steps, "rebuilds": st.rebuilds, "ms_total": st.ms_total,
-                 "list_capacity": st.list_capacity, "launches": st.launches})
+                 "list_capacity": st.list_capacity, "launches": st.launches,
+                 "loop_graph": st.loop_graph})
 
     def batch_run(self, q, p, offsets, boxes, params: MdParams, nsteps, max_records=16):
         """Replica batch (see lj_batch_run).  offsets: n_replicas + 1 ints, boxes:

@@ -19,7 +19,7 @@
 namespace ljg {
 namespace {
 
-enum { B_REBUILD = 0, B_OVERFLOW = 2, B_COUNT = 3, B_STEP = 5, B_WORDS = 8 };
+enum { B_REBUILD = 0, B_OVERFLOW = 2, B_COUNT = 3, B_STEP = 5, B_LOOP = 6, B_WORDS = 8 };
 
 __global__ void __launch_bounds__(256) k_batch_drift(double* __restrict__ q,
                                                      const double* __restrict__ p, int n,
@@ -283,7 +283,11 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     // two-float terms the float comparison plus the fine quantum
     const double bc = cutoff_band(std::sqrt(cl2u), kCoarseQuantumErr, kBandFp32);
     const double bf = cutoff_band(std::sqrt(cl2u), kCoarseQuantumErr / 1024.0, kBandFF);
-    const double bs = cutoff_band(std::sqrt(sl2u), kCoarseQuantumErr, kBandFp32);
+    // the list build's separations also carry the rounding of positions
+    // relative to the cell origin (two cell widths, 8 W 2^-24)
+    const double wmax = 4294967296.0 / std::min(I.nc[0], std::min(I.nc[1], I.nc[2]));
+    const double bs = cutoff_band(std::sqrt(sl2u), kCoarseQuantumErr + 8.0 * wmax * 0x1p-24,
+                                  kBandFp32);
     I.cl2u_lo = (float)(cl2u * (1 - bc));
     I.cl2u_hi = (float)(cl2u * (1 + bc));
     I.cl2f_lo = (float)(cl2u * (1 - bf));
@@ -456,6 +460,8 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
   if ((rc = record(0))) return rc;
   B_CUDA(ctx, cudaEventRecord(t0, s), "event");
 
+  // the steps between records: one launch of the persistent loop graph, or
+  // (no conditional node) chunk graphs launched back to back
   const int gsteps = prm->graph_steps > 0 ? prm->graph_steps : 20;
   cudaGraphExec_t graph = nullptr;
   struct GraphGuard {
@@ -464,7 +470,16 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
       if (*g) cudaGraphExecDestroy(*g);
     }
   } gg{&graph};
-  if (gsteps > 1) {
+  LoopGraph loop;
+  if (gsteps > 1 && loop.build(s, b.flags.ptr + B_LOOP, b.flags.ptr + B_OVERFLOW,
+                               [&](cudaStream_t) {
+                                 cudaError_t ce = cudaSuccess;
+                                 for (int k = 0; k < gsteps && ce == cudaSuccess; k++)
+                                   ce = step(prm->dt);
+                                 return ce;
+                               }) == cudaSuccess) {
+    // the loop runs the chunks
+  } else if (gsteps > 1) {
     cudaGraph_t g = nullptr;
     B_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
     cudaError_t ce = cudaSuccess;
@@ -485,6 +500,10 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
   while (done < nsteps) {
     const int64_t stop = std::min<int64_t>(nsteps, (done / every + 1) * every);
     int64_t plain = stop - done - 1;
+    if (loop.exec && plain >= gsteps) {
+      B_CUDA(ctx, loop.launch((int32_t)(plain / gsteps), s), "loop launch");
+      plain %= gsteps;
+    }
     while (graph && plain >= gsteps) {
       B_CUDA(ctx, cudaGraphLaunch(graph, s), "graph launch");
       plain -= gsteps;
@@ -509,6 +528,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     stats->ms_total = ms;
     stats->list_capacity = (int64_t)n_total * b.maxrow;
     stats->launches = -1;
+    stats->loop_graph = loop.exec ? 1 : 0;
   }
   if (n_records) *n_records = nrec;
   return LJ_OK;

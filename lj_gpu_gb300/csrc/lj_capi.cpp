@@ -422,23 +422,36 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
       return LJ_OK;
     }
     LJ_CUDA(ctx, launch_fixed_image(L, ctx->stream), "fixed image");
-    // two-float gathers (kernels 2 and 4) run the split gather over a copy
-    // of the full list ordered near | in range | beyond from these positions
-    // the first time; later positions change its speed, not its precision
+    // two-float gathers (kernels 2 and 4) run the segment gather over a
+    // near-first copy of the full list, ordered from these positions the
+    // first time; later positions change its speed, not its precision
     if (o->precision == LJ_PREC_MIXED && method == LJ_METHOD_GATHER_FULL && L.kernel == 2 &&
         !o->ff_all) {
       DevList& f = ctx->full;
       const bool al = L.csr.aligned4 != 0;
       bool& ok = al ? f.savalid : f.svalid;
       DevBuf<int32_t>& buf = al ? f.salist : f.slist;
+      DevBuf<int32_t>& nn = al ? f.sann : f.snn;
       if (!ok) {
         LJ_CUDA(ctx, buf.ensure((size_t)std::max<int64_t>(al ? f.aentries : f.entries, 4)),
                 "alloc");
-        LJ_CUDA(ctx, launch_partition_near(L, L.csr, buf.ptr, nullptr, ctx->stream),
-                "ordered rows");
+        LJ_CUDA(ctx, nn.ensure((size_t)n), "alloc");
+        LJ_CUDA(ctx, launch_partition_near(L, L.csr, buf.ptr, nn.ptr, nullptr, ctx->stream),
+                "near-first rows");
         ok = true;
       }
+      if (!ctx->closef_zeroed) {
+        LJ_CUDA(ctx, ctx->closef.ensure(2), "alloc");
+        LJ_CUDA(ctx, cudaMemsetAsync(ctx->closef.ptr, 0, 2 * sizeof(int32_t), ctx->stream),
+                "memset");
+        ctx->closef_zeroed = true;
+      }
+      L.close_flag = ctx->closef.ptr;
+      // near part [0, nn), far part [nn, np) of every row
       L.csr.list = buf.ptr;
+      L.far = L.csr;
+      L.far.first = nn.ptr;
+      L.csr.np = nn.ptr;
       L.split = 1;
     }
   }

@@ -56,10 +56,10 @@ struct DevList {
   int64_t aentries = 0;
   bool avalid = false;
   Csr acsr() const { return Csr{n, entries, np.ptr, aptr.ptr, alist.ptr, 0, 1}; }
-  // copies of list and alist with rows ordered near | in range | beyond
-  // (k_partition_near, from the positions of the first two-float gather
-  // after the list changed); reset whenever the list changes
-  DevBuf<int32_t> slist, salist;
+  // near-first copies of list and alist (k_partition_near, from the
+  // positions of the first two-float gather after the list changed) with
+  // their near counts; reset whenever the list changes
+  DevBuf<int32_t> slist, snn, salist, sann;
   bool svalid = false, savalid = false;
 };
 
@@ -91,6 +91,9 @@ struct lj_ctx {
   // open-box frame words (kOpenFrameWords), armed once by k_open_frame_init
   ljg::DevBuf<long long> oframe;
   bool oframe_armed = false;
+  // the segment gather's close-entry flag (two words, zeroed once)
+  ljg::DevBuf<int32_t> closef;
+  bool closef_zeroed = false;
   ljg::DevBuf<int32_t> err2;
   ljg::DevBuf<int32_t> tmp_i32a, tmp_i32b;
   ljg::DevBuf<int64_t> tmp_off;

@@ -156,17 +156,17 @@ cudaError_t launch_fixed_image_sorted(const ForceLaunch& L, const int32_t* order
   return cudaGetLastError();
 }
 
-cudaError_t launch_partition_near(const ForceLaunch& L, const Csr& in, int32_t* out,
+cudaError_t launch_partition_near(const ForceLaunch& L, const Csr& in, int32_t* out, int32_t* nn,
                                   const int32_t* guard, cudaStream_t s) {
   if (in.n == 0) return cudaSuccess;
   const MixedConsts K = make_mixed_consts(L);
   // one warp per row, capped near a few resident waves (grid-stride rows)
   const int blocks = (int)std::min<long long>(((long long)in.n * 32 + 127) / 128, 152 * 16);
   if (L.box.on) {
-    if (L.aniso) k_partition_near<true, true><<<blocks, 128, 0, s>>>(in, L.qfix, K, out, guard);
-    else k_partition_near<true, false><<<blocks, 128, 0, s>>>(in, L.qfix, K, out, guard);
+    if (L.aniso) k_partition_near<true, true><<<blocks, 128, 0, s>>>(in, L.qfix, K, out, nn, guard);
+    else k_partition_near<true, false><<<blocks, 128, 0, s>>>(in, L.qfix, K, out, nn, guard);
   } else {
-    k_partition_near<false, false><<<blocks, 128, 0, s>>>(in, L.qfix, K, out, guard);
+    k_partition_near<false, false><<<blocks, 128, 0, s>>>(in, L.qfix, K, out, nn, guard);
   }
   return cudaGetLastError();
 }

@@ -677,18 +677,13 @@ __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const C
 // U terms of one step are summed in FP32 and the step sum enters the Kahan
 // accumulator, so compensation costs 12/U operations per pair.  FF: every
 // term is a two-float pair term (lj_ff.cuh) entering the compensated sums on
-// its own.  SPLIT (with FF, over rows ordered by k_partition_near): a warp
-// step whose pairs are all farther than K.near2 (2.2 sigma) takes FP32 terms
-// instead, and one whose pairs all lie beyond the cutoff band takes none; the
-// decision uses the step's own r2, so the order of the rows sets the speed,
-// never the precision.
+// its own.
 // Accepts padded rows (C.ptr == nullptr, row i at i * C.stride).  VEC
 // (U == 4, rows on 16-byte boundaries and readable to a multiple of 4): lane
 // l of a row takes the 4 consecutive entries base + 4 l .. + 3 with one
 // 16-byte load, which quarters the index-load instructions and the L1
 // wavefronts they cost (a 32-lane scalar index load touches one line per row).
-template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC = false, bool FF = false,
-          bool SPLIT = false>
+template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC = false, bool FF = false>
 __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const Csr C,
                                                         const int4* __restrict__ qfix,
                                                         const MixedConsts K0) {
@@ -750,65 +745,15 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
     load_idx(base + G * U, jn);
     unsigned border = 0u;
     if constexpr (FF) {
-      bool two_float = true;
-      if constexpr (SPLIT) {
-        // the warp step's own r2 (FP32, coarse image) picks its arithmetic:
-        // two-float terms if any pair is closer than K.near2, else FP32
-        // terms if any is inside the cutoff band, else none
-        bool nr = false, inr = false;
+#pragma unroll
+      for (int u = 0; u < U; u++) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, ok[u], border, u);
+      if (__any_sync(kFullMask, border != 0u)) {
 #pragma unroll
         for (int u = 0; u < U; u++) {
-          const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
-          const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-          nr |= ok[u] && r2 < K.near2;
-          inr |= ok[u] && r2 <= K.cl2s_hi;
-        }
-        two_float = __any_sync(kFullMask, nr);
-        if (!two_float && __any_sync(kFullMask, inr)) {
-          float sx = 0.f, sy = 0.f, sz = 0.f;
-#pragma unroll
-          for (int u = 0; u < U; u++) {
-            const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
-            const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-            const bool in = ok[u] && r2 <= K.cl2s_lo;
-            if (ok[u] && r2 > K.cl2s_lo && r2 <= K.cl2s_hi) border |= 1u << u;
-            float df = df_mixed<ANISO>(r2, K);
-            df = in ? df : 0.0f;
-            sx = fmaf(df, d.x, sx);
-            sy = fmaf(df, d.y, sy);
-            sz = fmaf(df, d.z, sz);
-          }
-          if (__any_sync(kFullMask, border != 0u)) {
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-              if (!(border & (1u << u))) continue;
-              const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, jj[u]), K.f64);
-              if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
-              const float3 d = sep_mixed<ANISO>(xi, xj[u], K);
-              const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-              const float df = df_mixed<ANISO>(r2, K);
-              sx = fmaf(df, d.x, sx);
-              sy = fmaf(df, d.y, sy);
-              sz = fmaf(df, d.z, sz);
-            }
-          }
-          // FP32 terms carry the 24 of df; the two-float sums and kick do not
-          acc.x.add_parts(__fmul_rn(sx, 0.041666668f), 0.f);
-          acc.y.add_parts(__fmul_rn(sy, 0.041666668f), 0.f);
-          acc.z.add_parts(__fmul_rn(sz, 0.041666668f), 0.f);
-        }
-      }
-      if (two_float) {
-#pragma unroll
-        for (int u = 0; u < U; u++) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, ok[u], border, u);
-        if (__any_sync(kFullMask, border != 0u)) {
-#pragma unroll
-          for (int u = 0; u < U; u++) {
-            if (!(border & (1u << u))) continue;
-            const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, jj[u]), K.f64);
-            if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
-            pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 1, true, border, u);
-          }
+          if (!(border & (1u << u))) continue;
+          const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, jj[u]), K.f64);
+          if (beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits)) continue;
+          pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 1, true, border, u);
         }
       }
     } else {
@@ -854,15 +799,16 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
   kick_group<SOA, G, FF>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
 }
 
-// Orders every row for the split two-float gather: entries with FP32 r2
-// (coarse image) below K.near_build2 first, then those up to the upper edge
-// of the FP32 cutoff band, then the ones beyond; list order within each
-// group.  Rows keep their starts (out has the layout of C).  One warp per
-// row (two passes: count, place), rows in a grid-stride loop.
+// Orders every row near-first for the segment gather: the entries with FP32
+// r2 (coarse image) below K.near_build2 first, in list order, the others
+// after them in reverse list order; nn[i] receives the near count.  Rows
+// keep their starts (out has the layout of C).  One warp per row, rows in a
+// grid-stride loop.
 template <bool PBC, bool ANISO>
 __global__ void __launch_bounds__(128) k_partition_near(const Csr C, const int4* __restrict__ qfix,
                                                         const MixedConsts K0,
                                                         int32_t* __restrict__ out,
+                                                        int32_t* __restrict__ nn,
                                                         const int32_t* guard) {
   if (guard && *(volatile const int32_t*)guard == 0) return;
   const MixedConsts K = PBC ? K0 : frame_consts(K0);
@@ -873,33 +819,244 @@ __global__ void __launch_bounds__(128) k_partition_near(const Csr C, const int4*
     const int cnt = __ldg(C.np + i);
     const int64_t k0 = row_start(C, i);
     const int4 xi = __ldg(qfix + i);
-    // group of entry k: 0 near, 1 in range, 2 beyond the cutoff
-    auto group = [&](int k, int& j) {
-      j = __ldg(C.list + k0 + k);
-      const float3 d = sep_mixed<ANISO>(xi, __ldg(qfix + j), K);
-      const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-      return r2 < K.near_build2 ? 0 : (r2 <= K.cl2s_hi ? 1 : 2);
-    };
-    int n0 = 0, n1 = 0;
+    int nacc = 0, facc = 0;
     for (int base = 0; base < cnt; base += 32) {
-      int j, g = 3;
-      if (base + lane < cnt) g = group(base + lane, j);
-      n0 += __popc(__ballot_sync(kFullMask, g == 0));
-      n1 += __popc(__ballot_sync(kFullMask, g == 1));
+      const int k = base + lane;
+      const bool ok = k < cnt;
+      int j = 0;
+      bool near = false;
+      if (ok) {
+        j = __ldg(C.list + k0 + k);
+        const float3 d = sep_mixed<ANISO>(xi, __ldg(qfix + j), K);
+        near = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x)) < K.near_build2;
+      }
+      const unsigned bn = __ballot_sync(kFullMask, near);
+      const unsigned bf = __ballot_sync(kFullMask, ok && !near);
+      if (near) out[k0 + nacc + __popc(bn & lt)] = j;
+      else if (ok) out[k0 + cnt - 1 - (facc + __popc(bf & lt))] = j;
+      nacc += __popc(bn);
+      facc += __popc(bf);
     }
-    int c0 = 0, c1 = n0, c2 = n0 + n1;
-    for (int base = 0; base < cnt; base += 32) {
-      int j = 0, g = 3;
-      if (base + lane < cnt) g = group(base + lane, j);
-      const unsigned b0 = __ballot_sync(kFullMask, g == 0);
-      const unsigned b1 = __ballot_sync(kFullMask, g == 1);
-      const unsigned b2 = __ballot_sync(kFullMask, g == 2);
-      if (g == 0) out[k0 + c0 + __popc(b0 & lt)] = j;
-      if (g == 1) out[k0 + c1 + __popc(b1 & lt)] = j;
-      if (g == 2) out[k0 + c2 + __popc(b2 & lt)] = j;
-      c0 += __popc(b0);
-      c1 += __popc(b1);
-      c2 += __popc(b2);
+    if (lane == 0) nn[i] = nacc;
+  }
+}
+
+// Walks entries [first, np) of row i of C (first = C.first[i], or 0) in
+// steps of G * U entries per row group, U per lane, the indices loaded one
+// step ahead, calling body(xj, jj, ok) per step.  VEC: 16-byte index loads
+// of 4 consecutive entries per lane (rows start on 16-byte boundaries and
+// are readable to a multiple of 4); the walk starts at `first` rounded down
+// to a multiple of 4 with the entries before it masked.
+template <int G, int U, bool VEC, class Body>
+__device__ __forceinline__ void walk_row(const Csr& C, int i, bool valid, int lane,
+                                         const int4* __restrict__ qfix, Body&& body) {
+  static_assert(!VEC || U == 4, "vector index loads take 4 entries per lane");
+  int end = 0, first = 0, from = 0;
+  int64_t k0 = 0;
+  if (valid) {
+    end = __ldg(C.np + i);
+    first = C.first ? __ldg(C.first + i) : 0;
+    from = VEC ? (first & ~3) : first;
+    k0 = row_start(C, i) + from;
+  }
+  int cmax = end - from;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) cmax = max(cmax, __shfl_xor_sync(kFullMask, cmax, off));
+  const int lim = end - from, skip = first - from;
+  auto entry = [&](int base, int u) { return VEC ? base + 4 * lane + u : base + lane + u * G; };
+  auto load_idx = [&](int base, int* jn) {
+    if (VEC) {
+      int4 v = make_int4(0, 0, 0, 0);
+      if (entry(base, 0) < lim) v = __ldg(reinterpret_cast<const int4*>(C.list + k0 + entry(base, 0)));
+      jn[0] = v.x;
+      jn[1] = v.y;
+      jn[2] = v.z;
+      jn[3] = v.w;
+    } else {
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        jn[u] = entry(base, u) < lim ? __ldg(C.list + k0 + entry(base, u)) : 0;
+    }
+  };
+  int jn[U];
+  load_idx(0, jn);
+  for (int base = 0; base < cmax; base += G * U) {
+    int jj[U];
+    bool ok[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int e = entry(base, u);
+      ok[u] = e < lim && (!VEC || e >= skip);
+      jj[u] = ok[u] ? jn[u] : 0;
+    }
+    int4 xj[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) xj[u] = __ldg(qfix + jj[u]);
+    load_idx(base + G * U, jn);
+    body(xj, jj, ok);
+  }
+}
+
+// Segment gather (LJ_PREC_MIXED over rows in two parts): C holds every row's
+// near part, F its far part (k_partition_near's order, or the split rows of
+// the MD build).  The far part runs first in FP32 terms from the coarse image
+// (the FP32 kernels' arithmetic and cutoff band) into compensated FP32 sums,
+// which then seed the two-float sums of the near part's two-float terms.  A
+// far entry closer than K.near2 (2.2 sigma) -- a pair that moved in since
+// the rows were split -- is skipped there and raises close_flag[0], and
+// k_seg_close_terms then adds its two-float term, so the split decides the
+// speed, never the precision.
+template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC>
+__global__ void __launch_bounds__(256, 3) k_gather_mixed_seg(const Particles P, const Csr C,
+                                                          const Csr F,
+                                                          const int4* __restrict__ qfix,
+                                                          const MixedConsts K0,
+                                                          int32_t* close_flag) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / G;
+  const int lane = t & (G - 1);
+  // launched as a programmatic dependent of the image pass
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const MixedConsts K = PBC ? K0 : frame_consts(K0);
+  const bool valid = i < C.n;
+  const int4 xi = valid ? __ldg(qfix + i) : make_int4(0, 0, 0, 0);
+  int li[3];
+  image_lo(xi.w, li[0], li[1], li[2]);
+  // FP64 cutoff decision of a pair in the band
+  auto inside64 = [&](int j) {
+    const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, j), K.f64);
+    return !beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits);
+  };
+  // ---- far part: FP32 terms
+  bool missed = false;
+  RowSums<true> acc;
+  {
+    RowSums<false> acc32;
+    acc32.init();
+    walk_row<G, U, VEC>(F, i, valid, lane, qfix, [&](const int4* xj, const int* jj, const bool* ok) {
+      float3 d[U];
+      float r2[U];
+      bool any = false;
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        d[u] = sep_mixed<ANISO>(xi, xj[u], K);
+        r2[u] = fmaf(d[u].z, d[u].z, fmaf(d[u].y, d[u].y, d[u].x * d[u].x));
+        if (ok[u] && r2[u] < K.near2) missed = true;
+        any |= ok[u] && r2[u] <= K.cl2s_hi;
+      }
+      if (!__any_sync(kFullMask, any)) return;  // the whole step beyond the cutoff
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      unsigned border = 0u;
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const bool use = ok[u] && !(r2[u] < K.near2);
+        const bool in = use && r2[u] <= K.cl2s_lo;
+        if (use && r2[u] > K.cl2s_lo && r2[u] <= K.cl2s_hi) border |= 1u << u;
+        float df = df_mixed<ANISO>(r2[u], K);
+        df = in ? df : 0.0f;
+        sx = fmaf(df, d[u].x, sx);
+        sy = fmaf(df, d[u].y, sy);
+        sz = fmaf(df, d[u].z, sz);
+      }
+      if (__any_sync(kFullMask, border != 0u)) {
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          if (!(border & (1u << u)) || !inside64(jj[u])) continue;
+          const float df = df_mixed<ANISO>(r2[u], K);
+          sx = fmaf(df, d[u].x, sx);
+          sy = fmaf(df, d[u].y, sy);
+          sz = fmaf(df, d[u].z, sz);
+        }
+      }
+      acc32.x.add(sx);
+      acc32.y.add(sy);
+      acc32.z.add(sz);
+    });
+    // FP32 terms carry the 24 of df; the two-float sums and kick do not
+    float h[6];
+    acc32.get(h[0], h[1], h[2], h[3], h[4], h[5]);
+    const float r24 = 0.041666668f;
+    acc.x.hi = __fmul_rn(h[0], r24);
+    acc.x.lo = __fmul_rn(h[1], r24);
+    acc.y.hi = __fmul_rn(h[2], r24);
+    acc.y.lo = __fmul_rn(h[3], r24);
+    acc.z.hi = __fmul_rn(h[4], r24);
+    acc.z.lo = __fmul_rn(h[5], r24);
+  }
+  // rare: far entries that moved inside K.near2 since the split are left to
+  // k_seg_close_terms (its own kernel, so that its registers do not add to
+  // this one's)
+  if (__any_sync(kFullMask, missed) && (threadIdx.x & 31) == 0) atomicExch(close_flag, 1);
+  // ---- near part: two-float terms
+  walk_row<G, U, VEC>(C, i, valid, lane, qfix, [&](const int4* xj, const int* jj, const bool* ok) {
+    unsigned border = 0u;
+#pragma unroll
+    for (int u = 0; u < U; u++) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, ok[u], border, u);
+    if (__any_sync(kFullMask, border != 0u)) {
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if ((border & (1u << u)) && inside64(jj[u]))
+          pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 1, true, border, u);
+    }
+  });
+  float hx, lx, hy, ly, hz, lz;
+  acc.get(hx, lx, hy, ly, hz, lz);
+  if (G > 1) {
+    group_reduce_comp<G>(hx, lx);
+    group_reduce_comp<G>(hy, ly);
+    group_reduce_comp<G>(hz, lz);
+  }
+  kick_group<SOA, G, true>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
+}
+
+// The two-float terms of the far-part entries closer than K.near2 (FP32 r2,
+// the far walk's own test) of every row, kicked into p, when
+// k_gather_mixed_seg raised flag[0]; otherwise every block returns at once.
+// Rows in a grid-stride loop, G lanes per row, one entry per lane and step.
+// The last block to finish clears flag[0] and its counter flag[1].
+template <int G, bool PBC, bool SOA, bool ANISO>
+__global__ void __launch_bounds__(256) k_seg_close_terms(const Particles P, const Csr F,
+                                                         const int4* __restrict__ qfix,
+                                                         const MixedConsts K0, int32_t* flag) {
+  if (*(volatile int32_t*)flag == 0) return;
+  const MixedConsts K = PBC ? K0 : frame_consts(K0);
+  const int lane = threadIdx.x & (G - 1);
+  const int groups = (gridDim.x * blockDim.x) / G;
+  const int rows = (F.n + groups - 1) / groups * groups;  // whole warps take every pass
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) / G; i < rows; i += groups) {
+    const bool valid = i < F.n;
+    const int4 xi = valid ? __ldg(qfix + i) : make_int4(0, 0, 0, 0);
+    int li[3];
+    image_lo(xi.w, li[0], li[1], li[2]);
+    RowSums<true> acc;
+    acc.init();
+    walk_row<G, 1, false>(F, i, valid, lane, qfix, [&](const int4* xj, const int* jj,
+                                                       const bool* ok) {
+      const float3 d = sep_mixed<ANISO>(xi, xj[0], K);
+      const bool close = ok[0] && fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x)) < K.near2;
+      unsigned border = 0u;
+      pair_term_ff<ANISO>(xi, li, xj[0], K, acc, 0, close, border, 0);
+      if (border) {
+        const double3 d64 = sep_fp64<PBC>(load_q<SOA>(P, i), load_q<SOA>(P, jj[0]), K.f64);
+        if (!beyond_cutoff(r2_fp64(d64), K.f64.cl2_bits))
+          pair_term_ff<ANISO>(xi, li, xj[0], K, acc, 1, true, border, 0);
+      }
+    });
+    float hx, lx, hy, ly, hz, lz;
+    acc.get(hx, lx, hy, ly, hz, lz);
+    if (G > 1) {
+      group_reduce_comp<G>(hx, lx);
+      group_reduce_comp<G>(hy, ly);
+      group_reduce_comp<G>(hz, lz);
+    }
+    kick_group<SOA, G, true>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, K.fscale, K.fexp);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(flag + 1, 1) == (int)gridDim.x - 1) {
+      flag[0] = 0;
+      flag[1] = 0;
     }
   }
 }

@@ -1,6 +1,6 @@
-// lj_force_split.cu -- launch of the split two-float gather (LJ_PREC_MIXED,
-// kernels 2 and 4 over rows ordered near | in range | beyond): each warp step
-// takes two-float, FP32 or no pair terms by its own r2.
+// lj_force_split.cu -- launch of the segment gather (LJ_PREC_MIXED, kernels
+// 2 and 4 over rows in a near and a far part): two-float terms for the near
+// part, FP32 terms for the far part (k_gather_mixed_seg).
 #include "lj_force_kernels.cuh"
 
 namespace ljg {
@@ -10,36 +10,38 @@ cudaError_t launch_mixed_ff_split(const ForceLaunch& L, const MixedConsts& K, cu
   const int block = L.block;
   const int blocks = (int)(((long long)n * L.lanes + block - 1) / block);
   const bool pbc = L.box.on != 0, soa = L.part.soa != 0;
-  auto go = [&](auto u) -> cudaError_t {
+  const bool vec = L.unroll == 4 && L.csr.aligned4 && L.far.aligned4;
+  auto go = [&](auto u, auto v) -> cudaError_t {
     constexpr int U = decltype(u)::value;
+    constexpr bool V = decltype(v)::value;
     return dispatch_lanes(L.lanes, [&](auto g) {
       return dispatch_bools(pbc, soa, [&](auto P, auto S) {
         constexpr int G = decltype(g)::value;
-        const int4* qf = L.qfix;
-        if (U == 4 && L.csr.aligned4) {
-          if (L.aniso)
-            return launch_dependent(
-                k_gather_mixed_u<G, 4, P.value, S.value, true, true, true, true>, blocks, block,
-                s, L.part, L.csr, qf, K);
-          return launch_dependent(
-              k_gather_mixed_u<G, 4, P.value, S.value, false, true, true, true>, blocks, block, s,
-              L.part, L.csr, qf, K);
-        }
+        cudaError_t e;
         if (L.aniso)
-          return launch_dependent(
-              k_gather_mixed_u<G, U, P.value, S.value, true, false, true, true>, blocks, block, s,
-              L.part, L.csr, qf, K);
-        return launch_dependent(
-            k_gather_mixed_u<G, U, P.value, S.value, false, false, true, true>, blocks, block, s,
-            L.part, L.csr, qf, K);
+          e = launch_dependent(k_gather_mixed_seg<G, U, P.value, S.value, true, V>, blocks,
+                               block, s, L.part, L.csr, L.far, L.qfix, K, L.close_flag);
+        else
+          e = launch_dependent(k_gather_mixed_seg<G, U, P.value, S.value, false, V>, blocks,
+                               block, s, L.part, L.csr, L.far, L.qfix, K, L.close_flag);
+        if (e != cudaSuccess) return e;
+        // far entries that came inside 2.2 sigma (a no-op unless the flag is up)
+        const int cb = (int)std::min<long long>(((long long)n * G + 255) / 256, 152 * 4);
+        if (L.aniso)
+          k_seg_close_terms<G, P.value, S.value, true>
+              <<<cb, 256, 0, s>>>(L.part, L.far, L.qfix, K, L.close_flag);
+        else
+          k_seg_close_terms<G, P.value, S.value, false>
+              <<<cb, 256, 0, s>>>(L.part, L.far, L.qfix, K, L.close_flag);
+        return cudaGetLastError();
       });
     });
   };
-  switch (L.unroll) {
-    case 2: return go(std::integral_constant<int, 2>{});
-    case 4: return go(std::integral_constant<int, 4>{});
-    default: return cudaErrorInvalidValue;
-  }
+  using T = std::true_type;
+  using N = std::false_type;
+  if (vec) return go(std::integral_constant<int, 4>{}, T{});
+  if (L.unroll == 4) return go(std::integral_constant<int, 4>{}, N{});
+  return go(std::integral_constant<int, 2>{}, N{});
 }
 
 }  // namespace ljg

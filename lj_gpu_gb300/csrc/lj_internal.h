@@ -3,11 +3,30 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <cuda_runtime.h>
 
 #include "lj_common.cuh"
 
 namespace ljg {
+
+// The persistent step loop of the MD and batch runs (lj_graph.cu): a graph
+// whose one node is a WHILE node over `chunk` (captured once), run `chunks`
+// times per launch from a device counter, or fewer if *stop_word turns
+// nonzero.
+struct LoopGraph {
+  cudaGraphExec_t exec = nullptr;
+  int32_t* counter = nullptr;
+  int64_t kernels_per_chunk = 0;  // kernels one pass of the body launches
+  LoopGraph() = default;
+  LoopGraph(const LoopGraph&) = delete;
+  LoopGraph& operator=(const LoopGraph&) = delete;
+  ~LoopGraph() { reset(); }
+  void reset();
+  cudaError_t build(cudaStream_t s, int32_t* counter_word, const int32_t* stop_word,
+                    const std::function<cudaError_t(cudaStream_t)>& chunk);
+  cudaError_t launch(int32_t chunks, cudaStream_t s);
+};
 
 // Where q / p live and how they are laid out.
 struct Particles {
@@ -35,6 +54,9 @@ struct Csr {
   const int32_t* list;
   int64_t stride;
   int aligned4;  // every row starts on a 16-byte boundary and is readable to a multiple of 4
+  // optional: row i's entries start at first[i] (the far part of a
+  // near-first row); its entries are then [first[i], np[i])
+  const int32_t* first;
 };
 
 __device__ __forceinline__ int64_t row_start(const Csr& c, int i) {
@@ -79,9 +101,13 @@ struct ForceLaunch {
   int block;       // threads per block
   int kernel;      // 1: simple strided, 2: unrolled (mixed) / compacted (FP64)
   int unroll;      // entries in flight per lane (kernel 2, mixed)
-  // two-float gathers: rows ordered near | in range | beyond (k_partition_near);
-  // each warp step then picks two-float, FP32 or no pair terms by its own r2
+  // two-float gathers over rows in two parts: csr holds the near part of
+  // every row (two-float terms), far the rest (FP32 terms); see
+  // k_gather_mixed_seg
   int split;
+  Csr far;
+  // two device words, zero between calls (k_seg_close_terms clears them)
+  int32_t* close_flag;
   // mixed precision only
   int4* qfix;      // n entries, written by the fixed-image pass
   float* fscratch; // 4 n floats, one float4 per particle (scatter-half mixed only)
@@ -145,11 +171,10 @@ cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* 
 
 // Launchers (return cudaError_t of the launch)
 cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s);
-// Copy of the rows of `in` (same row starts) into `out` ordered near | in
-// range | beyond the cutoff for the split two-float gather (L's frame and
-// cutoff); L's position image must be current.  `guard` (optional): nothing
-// happens while *guard == 0.
-cudaError_t launch_partition_near(const ForceLaunch& L, const Csr& in, int32_t* out,
+// Near-first copy of the rows of `in` (same row starts) into `out` for the
+// segment gather (L's frame), near counts into nn; L's position image must
+// be current.  `guard` (optional): nothing happens while *guard == 0.
+cudaError_t launch_partition_near(const ForceLaunch& L, const Csr& in, int32_t* out, int32_t* nn,
                                   const int32_t* guard, cudaStream_t s);
 cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s);
 cudaError_t launch_force_pairs(const Particles& part, int n, const int32_t* ip,

@@ -15,8 +15,11 @@
 //   kick    the mixed gather (or FP64 compacted scatter) with dt
 // Half kicks of consecutive steps are merged into one full kick; they are
 // split only where synchronous momenta are needed (energy records and the
-// end), so a run of S steps costs S + 1 + records force calls.  Steps between
-// records run as CUDA graph launches of `graph_steps` captured steps.
+// end), so a run of S steps costs S + 1 + records force calls.  The steps
+// between two records run as one launch of a persistent graph (LoopGraph: a
+// WHILE node over `graph_steps` captured steps, counted down on the device),
+// or, where a conditional node cannot be built, as back-to-back launches of
+// a graph of `graph_steps` steps.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -35,7 +38,9 @@ enum {
   F_COUNT = 3,    // rebuilds done
   F_MAXROW = 4,   // longest row of the last build
   F_STEP = 5,     // steps taken (drives rebuild_every)
-  F_WORDS = 8
+  F_CLOSE = 6,    // two words for k_seg_close_terms
+  F_LOOP = 8,     // chunks left in the persistent loop
+  F_WORDS = 10
 };
 
 __global__ void __launch_bounds__(256) k_md_drift(double* __restrict__ q,
@@ -173,12 +178,14 @@ struct MdState {
   CellGrid grid{};
   ForceLaunch kick_full{}, kick_half{};
   BuildArgs build{};
-  int maxrow = 0;
+  int maxrow = 0;          // capacity of the rows in use (full, half or near part)
+  int maxrow_full = 0, maxrow_near = 0, maxrow_far = 0;
   DevBuf<int4> qfix, qref, cq, cq2;
   DevBuf<int32_t> flags, cell, count, cursor, order, order2, cnt, ptr, rows, list;
-  // copy of the padded rows ordered near | in range | beyond (split
-  // two-float kicks)
-  DevBuf<int32_t> rows2;
+  // split two-float kicks: rows / cnt hold every row's near part, rows2 /
+  // cnt2 the far part (launch_build_rows_split)
+  DevBuf<int32_t> rows2, cnt2;
+  int64_t cap2 = 0;
   bool split = false;
   DevBuf<int64_t> start, off;
   DevBuf<unsigned char> scan_tmp;
@@ -186,6 +193,7 @@ struct MdState {
   cudaStream_t own_stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
+  LoopGraph loop;
   ~MdState() {
     if (graph) cudaGraphExecDestroy(graph);
     if (own_stream) cudaStreamDestroy(own_stream);
@@ -225,13 +233,13 @@ cudaError_t md_rebuild(MdState& m, bool compact, const ForceLaunch& kick, cudaSt
   if ((e = launch_sort_cells(m.start.ptr, m.grid.ncells, m.order.ptr, m.cq.ptr, m.order2.ptr,
                              m.cq2.ptr, s, g)))
     return e;
-  if ((e = launch_build_rows(m.build, m.build.want_half != 0, m.maxrow, m.rows.ptr, m.cnt.ptr,
-                             m.flags.ptr + F_OVERFLOW, s, g)))
-    return e;
-  if (m.split) {  // rows ordered from the positions of this build
-    const Csr rows{m.n, m.cap, m.cnt.ptr, nullptr, m.rows.ptr, (int64_t)m.maxrow, 1};
-    if ((e = launch_partition_near(kick, rows, m.rows2.ptr, g, s))) return e;
-  }
+  if (m.split)
+    e = launch_build_rows_split(m.build, m.maxrow, m.rows.ptr, m.cnt.ptr, m.maxrow_far,
+                                m.rows2.ptr, m.cnt2.ptr, m.flags.ptr + F_OVERFLOW, s, g);
+  else
+    e = launch_build_rows(m.build, m.build.want_half != 0, m.maxrow, m.rows.ptr, m.cnt.ptr,
+                          m.flags.ptr + F_OVERFLOW, s, g);
+  if (e) return e;
   if (compact) {
     if ((e = launch_scan_counts(m.cnt.ptr, m.n, m.off.ptr, m.scan_tmp.ptr, m.scan_tmp.cap, s, g)))
       return e;
@@ -323,8 +331,21 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   m.n = n;
   const double vol = prm->box[0] * prm->box[1] * prm->box[2];
   const double per = 4.18879 * rs * rs * rs * (n / vol);  // full-list partners / particle
-  // padded row length: the mean full row plus room for density fluctuations
-  m.maxrow = std::max(m.maxrow, ((int)std::ceil(per * 1.5) + 32 + 31) / 32 * 32);
+  // two-float kicks split every row into a near and a far part at the build
+  m.split = prm->precision == LJ_PREC_MIXED && !prm->ff_all;
+  // padded row lengths: the mean row plus room for density fluctuations
+  auto padded = [](double mean) { return ((int)std::ceil(mean * 1.5) + 32 + 31) / 32 * 32; };
+  if (m.split) {
+    const double rn = std::min(kFarSplit, rs);
+    const double per_near = 4.18879 * rn * rn * rn * (n / vol);
+    m.maxrow_near = std::max(m.maxrow_near, padded(per_near));
+    m.maxrow_far = std::max(m.maxrow_far, padded(per - per_near));
+    m.maxrow = m.maxrow_near;
+    m.cap2 = (int64_t)n * m.maxrow_far;
+  } else {
+    m.maxrow_full = std::max(m.maxrow_full, padded(per));
+    m.maxrow = m.maxrow_full;
+  }
   m.cap = (int64_t)n * m.maxrow;
   if (!mixed && per * 0.5 * n * 1.3 > 0x7fffffff)
     return lj_fail(ctx, LJ_ERR_UNSUPPORTED, "compacted half list would exceed 2^31 entries");
@@ -351,9 +372,9 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   MD_CUDA(ctx, m.off.ensure((size_t)n + 1), "alloc");
   MD_CUDA(ctx, m.scan_tmp.ensure(scan_tmp_bytes(std::max(n, m.grid.ncells))), "alloc");
   MD_CUDA(ctx, m.rows.ensure((size_t)m.cap), "alloc");
-  m.split = prm->precision == LJ_PREC_MIXED && !prm->ff_all;
   if (m.split) {
-    MD_CUDA(ctx, m.rows2.ensure((size_t)m.cap), "alloc");
+    MD_CUDA(ctx, m.rows2.ensure((size_t)m.cap2), "alloc");
+    MD_CUDA(ctx, m.cnt2.ensure(n), "alloc");
   }
   // the compacted half list holds about half of the padded capacity
   const int64_t half_cap = std::min<int64_t>(m.cap, 0x7fffffffll);
@@ -367,10 +388,11 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   K.part.p = p;
   // mixed: padded rows read in place (64-bit row starts i * maxrow); FP64:
   // compacted rows with int32 offsets
-  K.csr = mixed ? Csr{n, m.cap, m.cnt.ptr, nullptr, m.split ? m.rows2.ptr : m.rows.ptr,
-                      (int64_t)m.maxrow, 1}
+  K.csr = mixed ? Csr{n, m.cap, m.cnt.ptr, nullptr, m.rows.ptr, (int64_t)m.maxrow, 1}
                 : Csr{n, m.cap, m.cnt.ptr, m.ptr.ptr, m.list.ptr, 0, 0};
   K.split = m.split ? 1 : 0;
+  if (m.split) K.far = Csr{n, m.cap2, m.cnt2.ptr, nullptr, m.rows2.ptr, (int64_t)m.maxrow_far, 1};
+  K.close_flag = m.flags.ptr + F_CLOSE;
   K.box.on = 1;
   for (int d = 0; d < 3; d++) {
     K.box.len[d] = prm->box[d];
@@ -405,6 +427,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   b.cq = m.cq2.ptr;
   b.cell = m.cell.ptr;
   b.superset = 1;  // the force kernels and energies apply the cutoff
+  b.near = kFarSplit;
   b.want_half = mixed ? 0 : 1;
   b.want_full = mixed ? 1 : 0;
 
@@ -470,17 +493,21 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     const double cl2u = K.cl2 / u2;
     const float khi = (float)(1.0 / u2), klo = (float)(1.0 / u2 - (double)khi);
     const double band = cutoff_band(std::sqrt(cl2u), kCoarseQuantumErr, kBandFp32);
-    const Csr c = K.csr;
-    if (mixed && !K.aniso)
-      k_md_potential<false><<<grid1(n, 256), 256, 0, s>>>(
-          q, m.qfix.ptr, c, K.box.len[0], K.box.len[1], K.box.len[2], khi, klo,
-          (float)(cl2u * (1 - band)), (float)(cl2u * (1 + band)), K.cl2, m.energy.ptr + 1);
-    else
-      k_md_potential<true><<<grid1(n, 256), 256, 0, s>>>(
-          q, m.qfix.ptr, c, K.box.len[0], K.box.len[1], K.box.len[2], 0.f, 0.f, 0.f, 0.f, K.cl2,
-          m.energy.ptr + 1);
+    // split rows: the near and the far part of every row in turn
+    for (int part = 0; part < (K.split ? 2 : 1); part++) {
+      const Csr c = part ? K.far : K.csr;
+      if (mixed && !K.aniso)
+        k_md_potential<false><<<grid1(n, 256), 256, 0, s>>>(
+            q, m.qfix.ptr, c, K.box.len[0], K.box.len[1], K.box.len[2], khi, klo,
+            (float)(cl2u * (1 - band)), (float)(cl2u * (1 + band)), K.cl2, m.energy.ptr + 1);
+      else
+        k_md_potential<true><<<grid1(n, 256), 256, 0, s>>>(
+            q, m.qfix.ptr, c, K.box.len[0], K.box.len[1], K.box.len[2], 0.f, 0.f, 0.f, 0.f,
+            K.cl2, m.energy.ptr + 1);
+      launches++;
+    }
     k_md_kinetic<<<std::min(grid1(n, 256), 1024), 256, 0, s>>>(p, n, m.energy.ptr);
-    launches += 2;
+    launches++;
     double e[2];
     MD_CUDA(ctx, cudaGetLastError(), "energy");
     MD_CUDA(ctx, cudaMemcpyAsync(e, m.energy.ptr, sizeof e, cudaMemcpyDeviceToHost, s), "energy");
@@ -499,14 +526,25 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     return lj_fail(ctx, LJ_ERR_LIST_OVERFLOW, "a neighbour row exceeds %d entries", m.maxrow);
   if ((rc = record(0))) return rc;
 
-  // ---- graph of `graph_steps` plain steps ----------------------------------
+  // ---- the persistent loop over chunks of `graph_steps` plain steps --------
   const int gsteps = prm->graph_steps > 0 ? prm->graph_steps : 20;
   int64_t step_kernels = -1;  // kernels of one step (from the captured graph)
   if (m.graph) {
     cudaGraphExecDestroy(m.graph);
     m.graph = nullptr;
   }
-  if (gsteps > 1) {
+  m.loop.reset();
+  if (gsteps > 1 &&
+      m.loop.build(s, m.flags.ptr + F_LOOP, m.flags.ptr + F_OVERFLOW,
+                   [&](cudaStream_t cs) {
+                     cudaError_t ce = cudaSuccess;
+                     for (int k = 0; k < gsteps && ce == cudaSuccess; k++)
+                       ce = md_step(m, D, Kfull, cs);
+                     return ce;
+                   }) == cudaSuccess) {
+    step_kernels = m.loop.kernels_per_chunk / gsteps;
+    m.graph_steps = gsteps;
+  } else if (gsteps > 1) {  // no conditional node: chunk graphs launched back to back
     cudaGraph_t g = nullptr;
     MD_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
     cudaError_t ce = cudaSuccess;
@@ -532,6 +570,12 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   while (step < nsteps) {
     int64_t stop = std::min<int64_t>(nsteps, (step / every + 1) * every);
     int64_t plain = stop - step - 1;
+    const int64_t chunks = m.graph_steps > 0 ? plain / m.graph_steps : 0;
+    if (chunks > 0 && m.loop.exec) {
+      MD_CUDA(ctx, m.loop.launch((int32_t)chunks, s), "loop launch");
+      plain -= chunks * m.graph_steps;
+      launches += 1 + chunks;  // the count write and each pass's loop kernel
+    }
     while (m.graph && plain >= m.graph_steps) {
       MD_CUDA(ctx, cudaGraphLaunch(m.graph, s), "graph launch");
       plain -= m.graph_steps;
@@ -560,6 +604,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     stats->ms_total = ms;
     stats->list_capacity = m.cap;
     stats->launches = step_kernels < 0 ? -1 : launches + kicks + nsteps * step_kernels;
+    stats->loop_graph = m.loop.exec ? 1 : 0;
   }
   if (n_records) *n_records = nrec;
   if (!ctx->stream) MD_CUDA(ctx, cudaStreamSynchronize(s), "sync");

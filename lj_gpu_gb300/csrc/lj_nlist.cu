@@ -75,6 +75,7 @@ __global__ void k_place(const int32_t* __restrict__ cell, int n, const int64_t* 
 
 struct BuildConsts {
   float sl2_lo, sl2_hi;  // certainly inside / possibly inside, fixed units^2
+  float near2;           // ROWS_SPLIT: near part below this FP32 r2
   float u_hi[3], u_lo[3];
   int aniso;
   int periodic;
@@ -125,43 +126,61 @@ __global__ void k_sort_cells(const int64_t* __restrict__ start, int ncells,
 // Warp-cooperative neighbour build into padded rows.  One warp per cell:
 // the candidates of the 27-cell walk are flattened into one sequence (walk
 // order, then slot order inside each cell) and the lanes hold 32 consecutive
-// candidates, loaded with coalesced reads.  Up to 32 of the cell's own
+// candidates, loaded with coalesced reads.  Up to 64 of the cell's own
 // particles are staged in shared memory; the warp tests all 32 candidates
-// against one of them per step and keeps the step's ballot in that
-// particle's lane.  After a chunk of candidates every lane appends its hits,
-// in candidate order, to its particle's row, so rows come out in walk order
-// (deterministic after k_sort_cells).  Membership is decided in FP32 from the
-// exact fixed-point separation; a step with a candidate near the search
-// sphere re-decides those in FP64 with the reference's expression.  Rows
-// longer than maxrow are truncated and raise *overflow.
+// against one of them per step and keeps the step's ballot for that
+// particle.  After a chunk of candidates every lane appends its particles'
+// hits, in candidate order, to their rows, so rows come out in walk order
+// (deterministic after k_sort_cells).
+//
+// Membership is decided in FP32 on positions relative to the cell's first
+// particle: every staged particle and candidate is converted once per chunk
+// from the exact int32 fixed-point image, so a test costs three subtractions
+// and three multiply-adds.  The conversion error is part of the band of the
+// search sphere (make_build_consts); a candidate inside the band is
+// re-decided in FP64 with the reference's expression (EXACT), or kept (the
+// superset lists of the MD and batch loops, whose users apply the cutoff).
+// Rows longer than their capacity are truncated and raise *overflow.
 constexpr int kBuildBlock = 128;
 constexpr int kBuildWarps = kBuildBlock / 32;
+constexpr int kStage = 64;  // cell particles staged per candidate walk
 
-enum RowMode { ROWS_FULL = 0, ROWS_HALF = 1, ROWS_LOCAL = 2 };
+// ROWS_SPLIT: full rows in two parts, the candidates with FP32 r2 below
+// BuildConsts::near2 into rows / cnt and the others into rows2 / cnt2.
+enum RowMode { ROWS_FULL = 0, ROWS_HALF = 1, ROWS_LOCAL = 2, ROWS_SPLIT = 3 };
 
 struct BuildStage {
-  int4 xi[32];       // fixed-point position, particle index in w
-  unsigned bal[32];  // hits of staged particle t among the chunk's candidates
-  int js[32];        // the chunk's candidates (particle index)
-  int loc[32];       // and their 16-bit local indices (ROWS_LOCAL)
-  int nb_start[32];  // first slot of each walk cell
-  int nb_pref[32];   // candidates before it in the flattened walk
+  float4 xr[kStage];      // position relative to the cell origin, particle index bits in w
+  int4 xi[kStage];        // fixed-point image, particle index in w
+  unsigned bal[kStage];   // hits of staged particle t among the chunk's candidates
+  unsigned nbal[kStage];  // ROWS_SPLIT: the near ones among them
+  int js[32];             // the chunk's candidates (particle index)
+  int loc[32];            // and their 16-bit local indices (ROWS_LOCAL)
+  int nb_start[32];       // first slot of each walk cell
+  int nb_pref[32];        // candidates before it in the flattened walk
 };
 
-// Row of the particle in slot a + t: particle-indexed (i * maxrow) for
-// ROWS_FULL / ROWS_HALF, slot-indexed 16-bit local indices (walk position
-// << maxc_shift | slot in that cell) for ROWS_LOCAL.  EXACT: the reference's
-// membership (FP64 re-decision near the sphere); otherwise every candidate
-// with FP32 r2 < sl2_hi, a superset by at most the relative band.
+struct RowOut {
+  int32_t* rows;     // particle-indexed rows (i * maxrow), or
+  uint16_t* lrows;   // slot-indexed 16-bit local rows (ROWS_LOCAL)
+  int32_t* cnt;
+  int maxrow;
+  int maxc_shift;    // ROWS_LOCAL: walk position << maxc_shift | slot
+  int32_t* rows2;    // ROWS_SPLIT: far part (i * maxrow2), cnt2 entries
+  int32_t* cnt2;
+  int maxrow2;
+  int32_t* overflow;
+};
+
+// Rows of the particles in cell c (see above).  EXACT: the reference's
+// membership (FP64 re-decision in the band); otherwise every candidate with
+// FP32 r2 < sl2_hi, a superset by at most the band.
 template <int MODE, bool ANISO, bool EXACT>
 __device__ __forceinline__ void build_cell_rows(int c, int cell_base, const CellGrid& g,
                                                 const int64_t* __restrict__ start,
                                                 const int32_t* __restrict__ order,
                                                 const int4* __restrict__ cq, const double* q,
-                                                const BuildConsts& k, int maxrow, int maxc_shift,
-                                                int32_t* __restrict__ rows,
-                                                uint16_t* __restrict__ lrows,
-                                                int32_t* __restrict__ cnt, int32_t* overflow,
+                                                const BuildConsts& k, const RowOut& out,
                                                 BuildStage& ws, int lane) {
   int nnb;
   const int c2 = neighbour_cell_at(c, g, lane, &nnb);
@@ -185,19 +204,66 @@ __device__ __forceinline__ void build_cell_rows(int c, int cell_base, const Cell
     ws.nb_start[lane] = st;
     ws.nb_pref[lane] = incl - n2;
   }
-  const float sl2 = EXACT ? k.sl2_lo : k.sl2_hi;
   const int s0 = (int)start[cell_base + c], s1 = (int)start[cell_base + c + 1];
-  for (int a = s0; a < s1; a += 32) {
-    const int ni = min(32, s1 - a);
-    int my_i = -1;
-    if (lane < ni) {
-      int4 x = cq[a + lane];
-      my_i = order[a + lane];
-      x.w = my_i;
-      ws.xi[lane] = x;
-    }
+  if (s1 <= s0) {
     __syncwarp();
-    int len = 0;
+    return;
+  }
+  // Separations: on periodic grids of fewer than five cells along an axis a
+  // candidate may lie more than half a box from the cell origin, so those
+  // take the minimum image of every pair from the int32 image (DIRECT);
+  // elsewhere positions relative to the cell's first particle are exact
+  // differences and are converted to FP32 once.
+  const bool direct = g.periodic && min(g.nc[0], min(g.nc[1], g.nc[2])) <= 4;
+  const int4 o = cq[s0];
+  auto rel = [&](const int4& x) {
+    float dx = (float)wrap_sub(x.x, o.x), dy = (float)wrap_sub(x.y, o.y),
+          dz = (float)wrap_sub(x.z, o.z);
+    if (ANISO) {
+      dx = fmaf(dx, k.u_hi[0], dx * k.u_lo[0]);
+      dy = fmaf(dy, k.u_hi[1], dy * k.u_lo[1]);
+      dz = fmaf(dz, k.u_hi[2], dz * k.u_lo[2]);
+    }
+    return make_float3(dx, dy, dz);
+  };
+  // FP32 r2 of staged particle t and this lane's candidate (image xj or
+  // relative position cr)
+  auto pair_r2 = [&](auto direct_tag, int t, const int4& xj, const float3& cr) {
+    float dx, dy, dz;
+    if (decltype(direct_tag)::value) {
+      const int4 x = ws.xi[t];
+      dx = (float)wrap_sub(x.x, xj.x);
+      dy = (float)wrap_sub(x.y, xj.y);
+      dz = (float)wrap_sub(x.z, xj.z);
+      if (ANISO) {
+        dx = fmaf(dx, k.u_hi[0], dx * k.u_lo[0]);
+        dy = fmaf(dy, k.u_hi[1], dy * k.u_lo[1]);
+        dz = fmaf(dz, k.u_hi[2], dz * k.u_lo[2]);
+      }
+    } else {
+      const float4 x = ws.xr[t];
+      dx = x.x - cr.x;
+      dy = x.y - cr.y;
+      dz = x.z - cr.z;
+    }
+    return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+  };
+  const float inf = __int_as_float(0x7f800000);
+  for (int a = s0; a < s1; a += kStage) {
+    const int ni = min(kStage, s1 - a);
+    // staged particles t = lane and lane + 32 belong to this lane
+    auto stage = [&](int t) {
+      if (t >= ni) return -1;
+      const int i = order[a + t];
+      const int4 x = cq[a + t];
+      const float3 r = rel(x);
+      ws.xr[t] = make_float4(r.x, r.y, r.z, __int_as_float(i));
+      ws.xi[t] = make_int4(x.x, x.y, x.z, i);
+      return i;
+    };
+    const int i0 = stage(lane), i1 = stage(lane + 32);
+    __syncwarp();
+    int len0 = 0, len1 = 0, far0 = 0, far1 = 0;
     for (int base = 0; base < total; base += 32) {
       const int gi = base + lane;
       const bool act = gi < total;
@@ -208,56 +274,84 @@ __device__ __forceinline__ void build_cell_rows(int c, int cell_base, const Cell
       const int r = gi - ws.nb_pref[nb];
       int j = -1;
       int4 xj = make_int4(0, 0, 0, 0);
+      float3 cr = make_float3(inf, inf, inf);  // an absent candidate is never a hit
       if (act) {
         j = order[ws.nb_start[nb] + r];
         xj = cq[ws.nb_start[nb] + r];
+        cr = rel(xj);
       }
       ws.js[lane] = j;
-      if (MODE == ROWS_LOCAL) ws.loc[lane] = (nb << maxc_shift) + r;
+      if (MODE == ROWS_LOCAL) ws.loc[lane] = (nb << out.maxc_shift) + r;
+      // every staged particle against this chunk's candidates
+      auto tests = [&](auto direct_tag) {
+        bool band = false;  // a hit of this candidate lies in the band (EXACT)
 #pragma unroll 4
-      for (int t = 0; t < ni; t++) {
-        const int4 x = ws.xi[t];
-        float dx = (float)wrap_sub(x.x, xj.x), dy = (float)wrap_sub(x.y, xj.y),
-              dz = (float)wrap_sub(x.z, xj.z);
-        if (ANISO) {
-          dx = fmaf(dx, k.u_hi[0], dx * k.u_lo[0]);
-          dy = fmaf(dy, k.u_hi[1], dy * k.u_lo[1]);
-          dz = fmaf(dz, k.u_hi[2], dz * k.u_lo[2]);
+        for (int t = 0; t < ni; t++) {
+          float r2 = pair_r2(direct_tag, t, xj, cr);
+          if (decltype(direct_tag)::value && !act) r2 = inf;
+          const bool hit = (MODE != ROWS_HALF || j > ws.xi[t].w) && r2 < k.sl2_hi;
+          const unsigned bal = __ballot_sync(kFullMask, hit);
+          if (EXACT) band |= hit && !(r2 < k.sl2_lo);
+          if (MODE == ROWS_SPLIT) {
+            const unsigned nbal = __ballot_sync(kFullMask, r2 < k.near2);
+            if (lane == 0) ws.nbal[t] = nbal;
+          }
+          if (lane == 0) ws.bal[t] = bal;
         }
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        const bool keep = MODE != ROWS_HALF || j > x.w;
-        unsigned bal = __ballot_sync(kFullMask, keep && r2 < sl2);
-        if (EXACT) {
-          const bool maybe = keep && r2 < k.sl2_hi;
-          if (__ballot_sync(kFullMask, maybe) != bal)
-            bal |= __ballot_sync(kFullMask,
-                                 act && maybe && !(r2 < sl2) && within_fp64(q, x.w, j, k));
+        __syncwarp();
+        if (EXACT && __any_sync(kFullMask, band)) {
+          // rare: this lane's hits in the band, re-decided in FP64
+          if (band) {
+            for (int t = 0; t < ni; t++) {
+              const float r2 = pair_r2(direct_tag, t, xj, cr);
+              const int i = ws.xi[t].w;
+              const bool hit = (MODE != ROWS_HALF || j > i) && r2 < k.sl2_hi;
+              if (hit && !(r2 < k.sl2_lo) && !within_fp64(q, i, j, k))
+                atomicAnd(&ws.bal[t], ~(1u << lane));
+            }
+          }
+          __syncwarp();
         }
-        if (lane == 0) ws.bal[t] = bal;
-      }
-      __syncwarp();
-      unsigned mine = lane < ni ? ws.bal[lane] : 0u;
-      mine &= __ballot_sync(kFullMask, act);
-      if (MODE != ROWS_HALF) {  // a particle is its own candidate once
-        const int d = self_pref + (a - s0) + lane - base;
-        if (d >= 0 && d < 32) mine &= ~(1u << d);
-      }
-      const size_t rb = (size_t)(MODE == ROWS_LOCAL ? a + lane : max(my_i, 0)) * (size_t)maxrow;
-      while (mine) {
-        const int b = __ffs(mine) - 1;
-        mine &= mine - 1u;
-        if (len < maxrow) {
-          if (MODE == ROWS_LOCAL) lrows[rb + len] = (uint16_t)ws.loc[b];
-          else rows[rb + len] = ws.js[b];
+      };
+      if (direct) tests(std::true_type{});
+      else tests(std::false_type{});
+      // this chunk's hits of staged particle t (particle i) onto its rows
+      auto append = [&](int t, int i, int& len, int& len2) {
+        unsigned mine = ws.bal[t];
+        if (MODE != ROWS_HALF) {  // a particle is its own candidate once
+          const int d = self_pref + (a - s0) + t - base;
+          if (d >= 0 && d < 32) mine &= ~(1u << d);
         }
-        len++;
-      }
+        const unsigned nearm = MODE == ROWS_SPLIT ? ws.nbal[t] : 0u;
+        const size_t rb = (size_t)(MODE == ROWS_LOCAL ? a + t : i) * (size_t)out.maxrow;
+        const size_t rb2 = MODE == ROWS_SPLIT ? (size_t)i * (size_t)out.maxrow2 : 0;
+        while (mine) {
+          const int b = __ffs(mine) - 1;
+          mine &= mine - 1u;
+          if (MODE == ROWS_SPLIT && !((nearm >> b) & 1u)) {
+            if (len2 < out.maxrow2) out.rows2[rb2 + len2] = ws.js[b];
+            len2++;
+            continue;
+          }
+          if (len < out.maxrow) {
+            if (MODE == ROWS_LOCAL) out.lrows[rb + len] = (uint16_t)ws.loc[b];
+            else out.rows[rb + len] = ws.js[b];
+          }
+          len++;
+        }
+      };
+      if (lane < ni) append(lane, i0, len0, far0);
+      if (lane + 32 < ni) append(lane + 32, i1, len1, far1);
       __syncwarp();
     }
-    if (lane < ni) {
-      cnt[MODE == ROWS_LOCAL ? a + lane : my_i] = min(len, maxrow);
-      if (len > maxrow) atomicMax(overflow, 1);
-    }
+    auto finish = [&](int t, int i, int len, int len2) {
+      out.cnt[MODE == ROWS_LOCAL ? a + t : i] = min(len, out.maxrow);
+      if (MODE == ROWS_SPLIT) out.cnt2[i] = min(len2, out.maxrow2);
+      if (len > out.maxrow || (MODE == ROWS_SPLIT && len2 > out.maxrow2))
+        atomicMax(out.overflow, 1);
+    };
+    if (lane < ni) finish(lane, i0, len0, far0);
+    if (lane + 32 < ni) finish(lane + 32, i1, len1, far1);
     __syncwarp();
   }
   __syncwarp();
@@ -266,17 +360,15 @@ __device__ __forceinline__ void build_cell_rows(int c, int cell_base, const Cell
 template <int MODE, bool ANISO, bool EXACT>
 __global__ void __launch_bounds__(kBuildBlock) k_build_rows(
     const double* __restrict__ q, CellGrid g, const int64_t* __restrict__ start,
-    const int32_t* __restrict__ order, const int4* __restrict__ cq, BuildConsts k, int maxrow,
-    int maxc_shift, int32_t* __restrict__ rows, uint16_t* __restrict__ lrows,
-    int32_t* __restrict__ cnt, int32_t* __restrict__ overflow, const int32_t* guard) {
+    const int32_t* __restrict__ order, const int4* __restrict__ cq, BuildConsts k, RowOut out,
+    const int32_t* guard) {
   if (off_guard(guard)) return;
   __shared__ BuildStage stage[kBuildWarps];
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < g.ncells; c += nwarps)
-    build_cell_rows<MODE, ANISO, EXACT>(c, 0, g, start, order, cq, q, k, maxrow, maxc_shift,
-                                        rows, lrows, cnt, overflow, stage[threadIdx.x >> 5],
-                                        lane);
+    build_cell_rows<MODE, ANISO, EXACT>(c, 0, g, start, order, cq, q, k, out,
+                                        stage[threadIdx.x >> 5], lane);
 }
 
 // Batched binning: every replica has its own grid starting at cell_base.
@@ -323,9 +415,13 @@ __global__ void __launch_bounds__(kBuildBlock) k_build_rows_batch(
       k.half_bits[d] = R.half_bits[d];
     }
     k.sl2 = sl2;
+    RowOut out{};
+    out.rows = rows;
+    out.cnt = cnt;
+    out.maxrow = maxrow;
+    out.overflow = overflow;
     build_cell_rows<ROWS_FULL, false, false>(c - R.cell_base, R.cell_base, g, start, order, cq,
-                                             q, k, maxrow, 0, rows, nullptr, cnt, overflow,
-                                             stage[threadIdx.x >> 5], lane);
+                                             q, k, out, stage[threadIdx.x >> 5], lane);
   }
 }
 
@@ -416,12 +512,19 @@ BuildConsts make_build_consts(const BuildArgs& a) {
   BuildConsts k{};
   const double u2 = a.aniso ? 1.0 : a.unit[0] * a.unit[0];
   const double sl2u = a.search * a.search / u2;
-  // FP32 r2 from the coarse image: arithmetic band plus the coarse quantum
+  // FP32 r2 from the coarse image: arithmetic band plus the separation
+  // error, which is the coarse quantum plus the rounding of the positions
+  // relative to the cell origin (each within two cell widths W of it: at
+  // most 6 W 2^-24 on a separation, 8 W with the anisotropic scaling)
   const double umax = std::max(a.unit[0], std::max(a.unit[1], a.unit[2]));
-  const double band = cutoff_band(std::sqrt(sl2u), kCoarseQuantumErr * (a.aniso ? umax : 1.0),
-                                  kBandFp32);
+  double wmax = 0.0;  // widest cell, in the units of sl2u
+  for (int d = 0; d < 3; d++)
+    wmax = std::max(wmax, (1.0 / a.grid.inv_w[d]) / (a.aniso ? 1.0 : a.unit[d]));
+  const double qerr = kCoarseQuantumErr * (a.aniso ? umax : 1.0) + 8.0 * wmax * 0x1p-24;
+  const double band = cutoff_band(std::sqrt(sl2u), qerr, kBandFp32);
   k.sl2_lo = (float)(sl2u * (1.0 - band));
   k.sl2_hi = (float)(sl2u * (1.0 + band));
+  k.near2 = (float)(a.near * a.near / u2);
   for (int d = 0; d < 3; d++) {
     k.u_hi[d] = (float)a.unit[d];
     k.u_lo[d] = (float)(a.unit[d] - (double)k.u_hi[d]);
@@ -452,10 +555,14 @@ cudaError_t launch_build_rows(const BuildArgs& a, bool half, int maxrow, int32_t
   if (a.n == 0) return cudaSuccess;
   const BuildConsts k = make_build_consts(a);
   const int blocks = grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, kResidentBlocks);
+  RowOut out{};
+  out.rows = rows;
+  out.cnt = cnt;
+  out.maxrow = maxrow;
+  out.overflow = overflow;
   auto go = [&](auto mode, auto aniso, auto exact) {
     k_build_rows<decltype(mode)::value, decltype(aniso)::value, decltype(exact)::value>
-        <<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, maxrow, 0, rows,
-                                        nullptr, cnt, overflow, guard);
+        <<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, out, guard);
     return cudaGetLastError();
   };
   using H = std::integral_constant<int, ROWS_HALF>;
@@ -476,10 +583,38 @@ cudaError_t launch_build_rows_local(const BuildArgs& a, int maxrow, int maxc_shi
   if (a.n == 0) return cudaSuccess;
   const BuildConsts k = make_build_consts(a);
   const int blocks = grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, kResidentBlocks);
+  RowOut out{};
+  out.lrows = rows;
+  out.cnt = cnt;
+  out.maxrow = maxrow;
+  out.maxc_shift = maxc_shift;
+  out.overflow = overflow;
   // the cell-tiled kernel applies the cutoff itself; isotropic frames only
   k_build_rows<ROWS_LOCAL, false, false><<<blocks, kBuildBlock, 0, s>>>(
-      a.q, a.grid, a.start, a.order, a.cq, k, maxrow, maxc_shift, nullptr, rows, cnt, overflow,
-      nullptr);
+      a.q, a.grid, a.start, a.order, a.cq, k, out, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_rows_split(const BuildArgs& a, int maxrow, int32_t* rows, int32_t* cnt,
+                                    int maxrow2, int32_t* rows2, int32_t* cnt2,
+                                    int32_t* overflow, cudaStream_t s, const int32_t* guard) {
+  if (a.n == 0) return cudaSuccess;
+  const BuildConsts k = make_build_consts(a);
+  const int blocks = grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, kResidentBlocks);
+  RowOut out{};
+  out.rows = rows;
+  out.cnt = cnt;
+  out.maxrow = maxrow;
+  out.rows2 = rows2;
+  out.cnt2 = cnt2;
+  out.maxrow2 = maxrow2;
+  out.overflow = overflow;
+  if (a.aniso)
+    k_build_rows<ROWS_SPLIT, true, false>
+        <<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, out, guard);
+  else
+    k_build_rows<ROWS_SPLIT, false, false>
+        <<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, out, guard);
   return cudaGetLastError();
 }
 

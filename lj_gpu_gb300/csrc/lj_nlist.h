@@ -34,6 +34,8 @@ struct BuildArgs {
   // 1: a superset that may add pairs within the FP32 band outside the
   //    sphere (Verlet lists whose users apply the cutoff themselves)
   int superset;
+  // launch_build_rows_split: candidates closer than this go to the near rows
+  double near;
 };
 
 double key_to_double(unsigned long long k);
@@ -54,6 +56,13 @@ cudaError_t launch_sort_cells(const int64_t* start, int ncells, const int32_t* o
 cudaError_t launch_build_rows(const BuildArgs& a, bool half, int maxrow, int32_t* rows,
                               int32_t* cnt, int32_t* overflow, cudaStream_t s,
                               const int32_t* guard = nullptr);
+// Full superset rows in two parts: candidates with FP32 r2 below near^2
+// (BuildArgs::near) into rows / cnt (row i at i * maxrow), the others into
+// rows2 / cnt2 (i * maxrow2), each in walk order.
+cudaError_t launch_build_rows_split(const BuildArgs& a, int maxrow, int32_t* rows, int32_t* cnt,
+                                    int maxrow2, int32_t* rows2, int32_t* cnt2,
+                                    int32_t* overflow, cudaStream_t s,
+                                    const int32_t* guard = nullptr);
 // Local-index rows for the cell-tiled gather (full rows, slot-indexed).
 cudaError_t launch_build_rows_local(const BuildArgs& a, int maxrow, int maxc_shift,
                                     uint16_t* rows, int32_t* cnt, int32_t* overflow,

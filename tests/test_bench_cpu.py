@@ -117,3 +117,27 @@ def test_bench_helpers():
         {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}])
     assert merged["samples"] == 8 and merged["sm_min_mhz"] == 1950
     assert merged["reasons"] == ["sw_power_cap"] and merged["sm_mhz"] == 2060
+
+
+def test_ncu_summary_extractor():
+    """The summary extractor behind profiles/: a long-form metrics capture
+    and a launch list, as ncu writes them with --csv."""
+    sys.path.insert(0, str(ROOT))
+    from lj_gpu_gb300 import ncu_summary as ns
+    head = '"ID","Process ID","Process Name","Host Name","Kernel Name","Context","Stream",' \
+           '"Block Size","Grid Size","Device","CC","Section Name","Metric Name","Metric Unit",' \
+           '"Metric Value"'
+    def row(i, kern, metric, unit, value):
+        return f'"{i}","1","python","h","{kern}","1","7","(256, 1, 1)","(10, 1, 1)","0",' \
+               f'"10.3","Command line profiler metrics","{metric}","{unit}","{value}"'
+    text = "\n".join(["==PROF== Connected", head,
+                      row(0, "k_a(int)", "dram__bytes_read.sum", "Mbyte", "1.5"),
+                      row(0, "k_a(int)", "dram__bytes_write.sum", "Kbyte", "2"),
+                      row(0, "k_a(int)", "gpu__time_duration.sum", "us", "10"),
+                      row(1, "k_b(int)", "gpu__time_duration.sum", "ms", "0.03"),
+                      row(2, "k_a(int)", "gpu__time_duration.sum", "ns", "10000")])
+    s = ns.summarise_raw(text, kernel="k_a")
+    assert "traffic_bytes_per_launch: 1502000" in s and "k_b" not in s
+    t = ns.summarise_launches(text)
+    assert "| `k_a` | 2 | 0.020 | 10.0 | 40.0 % |" in t
+    assert "| `k_b` | 1 | 0.030 | 30.0 | 60.0 % |" in t
