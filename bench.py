@@ -56,9 +56,18 @@ UNIT = "G pair-interactions/s"
 WORKLOAD = ("LJ force call, FCC 108,000 particles, rho=0.5, periodic L=60, rc=3.0, "
             "search 3.3, i-sorted int32 CSR, dt=0.005")
 NCELL_8M, REBUILD_8M, E2E_CHUNK = 126, 20, 20
-WORKLOAD_8M = ("LJ MD step, FCC 8,001,504 particles, rho=1, periodic L=200, MB momenta "
-               "T*=1, rc=3.0, skin 0.3, device list rebuild every 20 steps, velocity "
-               "Verlet dt=0.005; mixed and FP64 back to back")
+NCELL_MD = {"md_8m": 126, "md_1m": 63}
+PAIRS_HALF_1M = 74_033_514  # half-list pairs of the md_1m capture under profiles/
+
+
+def md_workload(ncell):
+    n = 4 * ncell ** 3
+    return (f"LJ MD step, FCC {n:,} particles, rho=1, periodic L={n ** (1 / 3):.0f}, MB "
+            "momenta T*=1, rc=3.0, skin 0.3, device list rebuild every 20 steps, velocity "
+            "Verlet dt=0.005; mixed and FP64 back to back")
+
+
+WORKLOAD_8M = md_workload(NCELL_8M)
 
 
 def parse():
@@ -69,6 +78,10 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--chunk-graphs", action="store_true",
+                    help="MD workloads: launch the captured step chunks from the host "
+                         "instead of the persistent WHILE-node graph, so that a profiler "
+                         "can capture the step's kernels one by one")
     ap.add_argument("--no-autotune", action="store_true",
                     help="time the 'auto' variants with the engine's default launch shapes "
                          "(what the tuner picks on this workload) instead of tuning first; "
@@ -78,10 +91,12 @@ def parse():
                     help="extra mixed AoS gather variant KERNEL,LANES,UNROLL (e.g. 3,4,2 for "
                          "the cell-tiled kernel), timed beside the default variants")
     ap.add_argument("--workload", default="md_8m",
-                    choices=["md_8m", "rho0.5_108k", "rho1_108k", "precision_1m", "batch_512"],
+                    choices=["md_8m", "md_1m", "rho1_1m", "rho0.5_108k", "rho1_108k", "precision_1m", "batch_512"],
                     help="md_8m: 8,001,504-particle MD, mixed and FP64 back to back (the "
                          "headline); rho0.5_108k / rho1_108k: one force call of the 108,000-"
-                         "particle cases, every variant; precision_1m: 1,000,188-particle "
+                         "particle cases, every variant; md_1m: md_8m's step at 1,000,188 "
+                         "particles (the size the kernel profiles are captured on); rho1_1m: "
+                         "every force variant at 1,000,188 particles, rho = 1; precision_1m: 1,000,188-particle "
                          "mixed MD with force errors every 100 steps; batch_512: 512 "
                          "replicas of uneven N in one mixed MD loop")
     return ap.parse_args()
@@ -342,7 +357,7 @@ def algorithmic_bytes(method, layout, P, N):
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
-def run_ours(args, dist, density=DENSITY):
+def run_ours(args, dist, density=DENSITY, ncell=NCELL):
     import torch
     import lj_gpu_gb300 as lj
     from lj_gpu_gb300 import _build
@@ -351,7 +366,7 @@ def run_ours(args, dist, density=DENSITY):
     dev = torch.device("cuda", dist.local)
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
-    q, L = lj.init_fcc(NCELL, density, JITTER, SEED)
+    q, L = lj.init_fcc(ncell, density, JITTER, SEED)
     N = q.shape[0]
     qd = torch.from_numpy(q).to(dev)
     qs = [torch.from_numpy(np.ascontiguousarray(q[:, d])).to(dev) for d in range(3)]
@@ -616,7 +631,8 @@ def run_precision(args, dist):
     qd, pd = torch.from_numpy(q).to(dev), torch.from_numpy(p).to(dev)
     errors = [dict(step=0, **force_errors(torch, lj, L, qd))]
     ctx = lj.Context(dist.local, stream=torch.cuda.current_stream())
-    prm = lj.make_md_params(DT, RC, RS - RC, L, precision="mixed", record_every=100)
+    prm = lj.make_md_params(DT, RC, RS - RC, L, precision="mixed", record_every=100,
+                            chunk_graphs=args.chunk_graphs)
     records, ms, rebuilds, clock_samples = [], 0.0, 0, []
     for seg in range(10):
         with ClockSampler(dist.local) as cs:
@@ -669,7 +685,8 @@ def run_md8m(args, dist):
     dev = torch.device("cuda", dist.local)
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
-    q, L = lj.init_fcc(NCELL_8M, 1.0, JITTER, SEED)
+    ncell = NCELL_MD[args.workload]
+    q, L = lj.init_fcc(ncell, 1.0, JITTER, SEED)
     N = q.shape[0]
     p0 = lj.init_momenta(N, 1.0, SEED + 1)
     K, W = args.steps, args.warmup
@@ -679,7 +696,8 @@ def run_md8m(args, dist):
     for prec in ("mixed", "fp64"):
         qd, pd = torch.from_numpy(q).to(dev), torch.from_numpy(p0).to(dev)
         ctx = lj.Context(dist.local, stream=stream)
-        prm = lj.make_md_params(DT, RC, RS - RC, L, precision=prec, rebuild_every=REBUILD_8M)
+        prm = lj.make_md_params(DT, RC, RS - RC, L, precision=prec, rebuild_every=REBUILD_8M,
+                                chunk_graphs=args.chunk_graphs)
         ctx.md_run(qd, pd, prm, W, max_records=0)  # warm-up: its own build + W steps
         ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         torch.cuda.synchronize()
@@ -747,7 +765,7 @@ def run_md8m(args, dist):
         errors["fp64_vs_oracle"] = per_particle_errors(f_fp64, po[:, :3])
         cpu = {"value": P / t_cpu / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
                "cpu": cpu_model(), "nproc": os.cpu_count(), "seconds": t_cpu,
-               "sample": "one full-list force call of the 8,001,504-particle system at the "
+               "sample": f"one full-list force call of the {N:,}-particle system at the "
                          "final mixed MD positions (OpenMP gather over every host core, "
                          "project-written parallelisation); value counts its P_half pairs"}
         del npp, ptr_, lst
@@ -786,19 +804,20 @@ def run_md8m(args, dist):
 
     mx, fp = runs["mixed"], runs["fp64"]
     alg = pair_kernel_bytes("gather", "aos", P, N)
-    prof = "force_mixed_gather_md_1m.txt"
+    prof = "force_mixed_seg_gather_md_1m.txt"
     tr1m = profiled_traffic(prof)
     # the 1M capture's DRAM bytes scaled to this launch by the list entries
     # (traffic grows with the entries; the image and p terms scale with N alike)
-    traffic = tr1m * (P / 75_400_000) if tr1m else None
+    traffic = tr1m * (P / PAIRS_HALF_1M) if tr1m else None
     roofline = {"bound": "hbm", "achieved": alg / (mx["pair_ms"] * 1e-3) / 1e9, "peak": hbm,
                 "unit": "GB/s", "frac": alg / (mx["pair_ms"] * 1e-3) / 1e9 / hbm,
                 "traffic": traffic,
                 "traffic_source": (f"profiles/{prof}, scaled by list entries from the 1,000,188-"
                                    "particle capture") if traffic else None,
                 "peak_kind": peak_kind,
-                "kernel": "k_gather_mixed_u (two-float split gather, 4 lanes per row, 4 entries "
-                          "in flight), timed in force calls at the final MD positions",
+                "kernel": "k_gather_mixed_seg (FP32 far part, two-float near part; 4 lanes per "
+                          "row, 4 entries in flight), timed in force calls at the final MD "
+                          "positions",
                 "algorithmic_bytes_per_launch": alg, "kernel_ms": mx["pair_ms"],
                 "position_image_ms": mx["image_ms"],
                 "md_step_bytes": md_step_bytes(P, N, 1 / REBUILD_8M),
@@ -822,7 +841,7 @@ def run_md8m(args, dist):
         "n_gpus": dist.world, "steps": K, "warmup": W, "ms_per_step": mx["t_step"] * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 two-float pair math, f64 q/p", "data": "synthetic",
-        "config": {"workload": WORKLOAD_8M, "N": N, "box": L, "pairs_half": P,
+        "config": {"workload": md_workload(ncell), "N": N, "box": L, "pairs_half": P,
                    "step": "one MD step (drift, guarded rebuild, force kick)",
                    "rebuild_every": REBUILD_8M, "rebuilds": mx["stats"]["rebuilds"],
                    "l2": "working set (list rows ~9 GB) far larger than L2; no flush",
@@ -867,7 +886,8 @@ def run_batch(args, dist):
         specs.append((nc, rho))
     q, p = np.concatenate(qs), np.concatenate(ps)
     qd, pd = torch.from_numpy(q).to(dev), torch.from_numpy(p).to(dev)
-    prm = lj.make_md_params(DT, 2.5, 0.3, 1.0, precision="mixed", record_every=steps)
+    prm = lj.make_md_params(DT, 2.5, 0.3, 1.0, precision="mixed", record_every=steps,
+                            chunk_graphs=args.chunk_graphs)
     ctx = lj.Context(dist.local, stream=torch.cuda.current_stream())
     with ClockSampler(dist.local) as cs:
         en, st, shapes = ctx.batch_run(qd, pd, np.array(offs, np.int32), np.array(boxes), prm,
@@ -1007,12 +1027,14 @@ def main():
         line = run_reference(args, dist)
     else:
         dist = Dist("nccl")
-        if args.workload == "md_8m":
+        if args.workload in NCELL_MD:
             line = run_md8m(args, dist)
         elif args.workload == "precision_1m":
             line = run_precision(args, dist)
         elif args.workload == "batch_512":
             line = run_batch(args, dist)
+        elif args.workload == "rho1_1m":
+            line = run_ours(args, dist, 1.0, ncell=63)
         else:
             line = run_ours(args, dist, 1.0 if args.workload == "rho1_108k" else DENSITY)
     if dist.rank == 0 and line is not None:

@@ -62,6 +62,9 @@ enum {
 enum { LJ_PREC_FP64 = 0, LJ_PREC_MIXED = 1, LJ_PREC_MIXED_FP32 = 2 };
 enum { LJ_LIST_HALF = 0, LJ_LIST_FULL = 1 };
 enum { LJ_WHERE_HOST = 0, LJ_WHERE_DEVICE = 1 };
+/* Particle layouts (the entry point called): lj_force_aos, lj_force_soa,
+ * lj_force_z (the reference's force_sorted / force_soa / force_sorted_z). */
+enum { LJ_LAYOUT_AOS = 0, LJ_LAYOUT_SOA = 1, LJ_LAYOUT_Z = 2 };
 enum {
   LJ_METHOD_AUTO = 0,         /* engine choice (tuned per precision)          */
   LJ_METHOD_GATHER_FULL = 1,  /* full list, each row writes only its own p_i  */
@@ -81,9 +84,14 @@ typedef struct lj_force_opts {
   int32_t kernel;     /* kernel generation: 0 = default, 1 = simple strided,
                          2 = unrolled / compacted, 3 = cell-tiled (mixed
                          gather on a list from lj_list_build), 4 = unrolled
-                         with 16-byte index loads (mixed gather, unroll 4);
-                         3 and 4 fall back to 2 when their list form is
-                         missing (see lj_force.cu)                          */
+                         with 16-byte index loads (mixed gather, unroll 4),
+                         5 = gather over the transposed ("ELL") copy of the
+                         full list, entry k of row i at [i + k n], one lane
+                         per row (the reference's force_kernel_memopt2 /
+                         _unrolling2 layout, cuda/kernel.cuh:102-134,
+                         547-620; mixed: every pair in the precision's own
+                         terms, unroll 2 or 4); 3 and 4 fall back to 2 when
+                         their list form is missing (see lj_force.cu)       */
   int32_t unroll;     /* entries per lane in flight (kernel 2), 0 = default   */
   int32_t ff_all;     /* LJ_PREC_MIXED gathers (kernels 2 and 4): 0 = pairs
                          beyond 2.5 sigma of the first call's positions in
@@ -225,9 +233,14 @@ int lj_force_pairs_fp64_aos(const double* q, double* p, int32_t n, double dt, do
  * library); larger n returns LJ_ERR_INVALID_ARGUMENT.  Every call shares that
  * array, so calls that overlap on the GPU race: order them.  The first call on
  * a device looks up the array's device address; make it before any stream
- * capture.  Open boundaries (box == NULL) synchronise the stream once per
- * call to read the coordinate extent.  Same arithmetic as lj_force_aos with
- * LJ_PREC_MIXED and LJ_METHOD_GATHER_FULL. */
+ * capture.  Open boundaries (box == NULL) choose the fixed-point frame on the
+ * device (no host round trip).  The list is used as given and not validated
+ * (as in lj_force_pairs_fp64_aos): every index must lie in [0, n), or the
+ * kernel reads positions past the caller's arrays and past the scratch
+ * image.  Same arithmetic and launch shape as lj_force_aos with
+ * LJ_PREC_MIXED, LJ_METHOD_GATHER_FULL, kernel 2, 4 lanes per row, 4 entries
+ * in flight, 128 threads per block and ff_all = 1 (every pair in two-float
+ * terms): the two give identical bits. */
 #define LJ_NOALLOC_MAX_PARTICLES 1048576
 int lj_force_mixed_noalloc_aos(const double* q, double* p, int32_t n, double dt, double cl2,
                                const int32_t* sorted_list, const int32_t* number_of_partners,
@@ -283,7 +296,11 @@ typedef struct lj_md_params {
   int32_t ff_all;         /* LJ_PREC_MIXED: 0 = pairs beyond 2.5 sigma at the
                              last rebuild in FP32 terms (the default), 1 =
                              every pair in two-float terms */
-  int32_t reserved[3];
+  int32_t chunk_graphs;   /* 0: the steps between records run as one launch of a
+                             persistent graph (a WHILE node); 1: as chunk graphs
+                             launched back to back from the host, whose kernels
+                             profilers can capture one by one */
+  int32_t reserved[2];
 } lj_md_params;
 
 typedef struct lj_md_record {
@@ -340,6 +357,31 @@ int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total, int32_t n_r
  * (cuda/force_cuda.cu:45,378-383). */
 int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts* opts,
                     int32_t reps, lj_force_opts* best, double* ms_best);
+
+/* The tuner over launch shapes, list layouts and particle layouts, with a
+ * persistent cache.  Every launch shape is timed on AoS positions (kernel 5
+ * is the transposed-list layout); the three fastest are timed again on each
+ * other particle layout asked for in `layouts` (bit 1 << LJ_LAYOUT_*, 0 =
+ * AoS only), from copies of q the tuner makes.  The key of the problem
+ * (`key`): GPU name and SM count, class of n (log2), class of the mean full
+ * row length (the density at a given cutoff: round(2 log2(mean))), precision,
+ * boundary kind, the requested method and the layout set.  With a cache file
+ * (`cache_path`, NULL = none) a key found there returns its entry without
+ * timing anything (from_cache = 1); otherwise the winner is appended to the
+ * file.  The winner is remembered in the context for calls of its layout
+ * that leave method = AUTO and every launch field 0, as lj_autotune_aos. */
+typedef struct lj_tune_result {
+  lj_force_opts best;   /* *opts with the winner's method and launch fields */
+  int32_t layout;       /* LJ_LAYOUT_* of the winner                        */
+  int32_t from_cache;   /* 1: read from the cache file, nothing was timed   */
+  int32_t timed;        /* (shape, layout) candidates timed                 */
+  int32_t reserved;
+  double ms;            /* the winner's time per call (from the cache when
+                           from_cache)                                       */
+  char key[160];        /* the problem's cache key (NUL-terminated)          */
+} lj_tune_result;
+int lj_autotune(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts* opts,
+                int32_t reps, int32_t layouts, const char* cache_path, lj_tune_result* out);
 
 /* ---- host-buffer call (the reference's measure(), force_cuda.cu:319-342) - */
 /* Uploads q and p from host memory, runs `calls` force calls on the installed

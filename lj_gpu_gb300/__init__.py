@@ -77,11 +77,22 @@ def make_opts(dt=0.001, cl2=9.0, box=None, precision="fp64", method="auto", lane
     return o
 
 
+LJ_LAYOUT_AOS, LJ_LAYOUT_SOA, LJ_LAYOUT_Z = 0, 1, 2
+LAYOUTS = {"aos": LJ_LAYOUT_AOS, "soa": LJ_LAYOUT_SOA, "z": LJ_LAYOUT_Z}
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("best", ForceOpts), ("layout", C.c_int32), ("from_cache", C.c_int32),
+                ("timed", C.c_int32), ("reserved", C.c_int32), ("ms", C.c_double),
+                ("key", C.c_char * 160)]
+
+
 class MdParams(C.Structure):
     _fields_ = [
         ("dt", C.c_double), ("rc", C.c_double), ("skin", C.c_double), ("box", C.c_double * 3),
         ("precision", C.c_int32), ("record_every", C.c_int32), ("graph_steps", C.c_int32),
-        ("rebuild_every", C.c_int32), ("ff_all", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("rebuild_every", C.c_int32), ("ff_all", C.c_int32), ("chunk_graphs", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -96,7 +107,7 @@ class MdStats(C.Structure):
 
 
 def make_md_params(dt, rc, skin, box, precision="mixed", record_every=0, graph_steps=0,
-                   rebuild_every=0, ff_all=False):
+                   rebuild_every=0, ff_all=False, chunk_graphs=False):
     m = MdParams()
     m.dt, m.rc, m.skin = float(dt), float(rc), float(skin)
     b = [float(box)] * 3 if isinstance(box, (int, float)) else [float(v) for v in box]
@@ -105,6 +116,7 @@ def make_md_params(dt, rc, skin, box, precision="mixed", record_every=0, graph_s
     m.record_every, m.graph_steps = int(record_every), int(graph_steps)
     m.rebuild_every = int(rebuild_every)
     m.ff_all = 1 if ff_all else 0
+    m.chunk_graphs = 1 if chunk_graphs else 0
     return m
 
 
@@ -157,6 +169,8 @@ _SIGNATURES = {
                                   C.POINTER(C.c_int64)]),
     "lj_autotune_aos": (C.c_int, [_P, _P, C.c_int32, C.POINTER(ForceOpts), C.c_int32,
                                   C.POINTER(ForceOpts), C.POINTER(C.c_double)]),
+    "lj_autotune": (C.c_int, [_P, _P, C.c_int32, C.POINTER(ForceOpts), C.c_int32, C.c_int32,
+                              C.c_char_p, C.POINTER(TuneResult)]),
     "lj_md_run": (C.c_int, [_P, _P, _P, C.c_int32, C.POINTER(MdParams), C.c_int32,
                             C.POINTER(MdRecord), C.c_int32, C.POINTER(C.c_int32),
                             C.POINTER(MdStats)]),
@@ -349,6 +363,22 @@ class Context:
         self._check(lib().lj_autotune_aos(self._h, ptr(q), q.shape[0], C.byref(opts), reps,
                                           C.byref(best), C.byref(ms)), "autotune")
         return best, ms.value
+
+    def autotune_layouts(self, q, opts: ForceOpts, reps=5, layouts=("aos",), cache=None):
+        """lj_autotune: launch shapes, the transposed list (kernel 5) and the
+        particle layouts named in `layouts`, with an optional cache file.
+        Returns a dict: opts, layout (name), ms, from_cache, timed, key."""
+        _check_contig(q)
+        mask = 0
+        for name in layouts:
+            mask |= 1 << LAYOUTS[name]
+        r = TuneResult()
+        path = None if cache is None else str(cache).encode()
+        self._check(lib().lj_autotune(self._h, ptr(q), q.shape[0], C.byref(opts), reps, mask,
+                                      path, C.byref(r)), "autotune")
+        names = {v: k for k, v in LAYOUTS.items()}
+        return {"opts": r.best, "layout": names[r.layout], "ms": r.ms,
+                "from_cache": bool(r.from_cache), "timed": r.timed, "key": r.key.decode()}
 
     def md_run(self, q, p, params: MdParams, nsteps, max_records=64):
         """Velocity Verlet on device AoS q, p (in place); returns (records, stats)

@@ -471,7 +471,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     }
   } gg{&graph};
   LoopGraph loop;
-  if (gsteps > 1 && loop.build(s, b.flags.ptr + B_LOOP, b.flags.ptr + B_OVERFLOW,
+  if (gsteps > 1 && !prm->chunk_graphs && loop.build(s, b.flags.ptr + B_LOOP, b.flags.ptr + B_OVERFLOW,
                                [&](cudaStream_t) {
                                  cudaError_t ce = cudaSuccess;
                                  for (int k = 0; k < gsteps && ce == cudaSuccess; k++)

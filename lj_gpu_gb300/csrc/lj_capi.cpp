@@ -77,8 +77,8 @@ int check_opts(lj_ctx* ctx, const lj_force_opts* o) {
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "lanes must be 0 or a power of two <= 32");
   if (o->block != 0 && (o->block < 64 || o->block > 256 || (o->block % 32) != 0))
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "block must be 0 or a multiple of 32 in [64, 256]");
-  if (o->kernel < 0 || o->kernel > 4)
-    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kernel must be 0 (default) or 1..4");
+  if (o->kernel < 0 || o->kernel > 5)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kernel must be 0 (default) or 1..5");
   if (o->unroll < 0) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be >= 0");
   if (o->ff_all != 0 && o->ff_all != 1)
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "ff_all must be 0 or 1");
@@ -179,6 +179,7 @@ int build_aligned(lj_ctx* ctx) {
   DevList& f = ctx->full;
   f.avalid = false;
   f.svalid = f.savalid = false;
+  f.evalid = false;
   const int n = f.n;
   if (!f.valid || n == 0) return LJ_OK;
   cudaStream_t s = ctx->stream;
@@ -213,6 +214,7 @@ int install_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ptr,
   ctx->full.valid = false;
   ctx->full.avalid = false;
   ctx->full.svalid = ctx->full.savalid = false;
+  ctx->full.evalid = false;
   ctx->tiled.valid = false;
   LJ_CUDA(ctx, l.np.ensure((size_t)n), "alloc");
   LJ_CUDA(ctx, l.ptr.ensure((size_t)n), "alloc");
@@ -275,7 +277,7 @@ int install_csr(lj_ctx* ctx, int32_t n, const int32_t* np, const int32_t* ptr,
 int resolve_method(lj_ctx* ctx, const lj_force_opts* o, int* method) {
   int m = o->method;
   if (m == LJ_METHOD_AUTO) {
-    if (o->precision == LJ_PREC_FP64)
+    if (o->precision == LJ_PREC_FP64 && o->kernel != 5)
       m = ctx->half.valid ? LJ_METHOD_SCATTER_HALF : LJ_METHOD_GATHER_FULL;
     else
       m = LJ_METHOD_GATHER_FULL;
@@ -286,6 +288,21 @@ int resolve_method(lj_ctx* ctx, const lj_force_opts* o, int* method) {
   if (m == LJ_METHOD_GATHER_FULL && !ctx->full.valid)
     return fail(ctx, LJ_ERR_NO_LIST, "no neighbour list installed");
   *method = m;
+  return LJ_OK;
+}
+
+// The transposed copy of the full list for the ELL gather (kernel 5), built
+// from the installed CSR when missing (or when `refresh`, after the CSR was
+// uploaded again).
+int ensure_ell(lj_ctx* ctx, bool refresh = false) {
+  DevList& f = ctx->full;
+  if (f.evalid && !refresh) return LJ_OK;
+  f.evalid = false;
+  const size_t words = std::max<size_t>((size_t)f.n * (size_t)std::max(f.max_row, 0), 1);
+  LJ_CUDA(ctx, f.ell.ensure(words), "alloc");
+  LJ_CUDA(ctx, launch_csr_to_ell(f.np.ptr, f.ptr.ptr, f.list.ptr, f.n, f.n, f.ell.ptr,
+                                 ctx->stream), "transposed list");
+  f.evalid = true;
   return LJ_OK;
 }
 
@@ -306,11 +323,15 @@ cudaEvent_t* timing_slot(lj_ctx* ctx) {
 // A configuration chosen by lj_autotune_aos replaces the engine defaults when
 // the caller leaves method (AUTO) and every launch field at zero, for the
 // same precision, layout, boundary kind and list.
-const lj_force_opts* apply_tuned(lj_ctx* ctx, const lj_force_opts* o, int soa,
+int layout_of(const Particles& part) {
+  return part.soa ? LJ_LAYOUT_SOA : (part.stride == 8 ? LJ_LAYOUT_Z : LJ_LAYOUT_AOS);
+}
+
+const lj_force_opts* apply_tuned(lj_ctx* ctx, const lj_force_opts* o, int layout,
                                  lj_force_opts* scratch) {
   if (o->method != LJ_METHOD_AUTO || o->kernel || o->lanes || o->unroll || o->block) return o;
   for (const auto& t : ctx->tuned) {
-    if (t.precision == o->precision && t.soa == soa && t.periodic == (o->periodic != 0) &&
+    if (t.precision == o->precision && t.layout == layout && t.periodic == (o->periodic != 0) &&
         t.entries_half == ctx->half.entries && t.entries_full == ctx->full.entries &&
         t.n == (ctx->full.valid ? ctx->full.n : ctx->half.n)) {
       *scratch = *o;
@@ -329,7 +350,7 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
   int rc = check_opts(ctx, o_in);
   if (rc) return rc;
   lj_force_opts tuned_opts;
-  const lj_force_opts* o = apply_tuned(ctx, o_in, part.soa, &tuned_opts);
+  const lj_force_opts* o = apply_tuned(ctx, o_in, layout_of(part), &tuned_opts);
   int method = LJ_METHOD_GATHER_FULL;
   if ((rc = resolve_method(ctx, o, &method))) return rc;
   const DevList& l = method == LJ_METHOD_SCATTER_HALF ? ctx->half : ctx->full;
@@ -357,6 +378,14 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
     L.kernel = 2;  // no aligned copy: scalar index loads
   // the mixed scatter has kernels 1 (simple) and 2 (unrolled, vector atomics)
   if (L.kernel > 2 && method == LJ_METHOD_SCATTER_HALF) L.kernel = 2;
+  // kernel 5: gather over the transposed copy of the full list, one lane per row
+  if (L.kernel == 5) {
+    if (o->lanes > 1)
+      return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kernel 5 takes one lane per row (lanes 0 or 1)");
+    if (mixed && o->unroll && o->unroll != 2 && o->unroll != 4)
+      return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kernel 5 takes unroll 0, 2 or 4");
+    if ((rc = ensure_ell(ctx))) return rc;
+  }
   L.unroll = o->unroll ? o->unroll : 4;
   if (L.kernel == 4 && L.unroll != 4)
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kernel 4 takes 4 entries per lane (unroll 0 or 4)");
@@ -368,6 +397,10 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
   if (L.kernel == 3 && !(L.unroll == 2 || L.unroll == 4))
     return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unroll must be 2 or 4 for kernel 3");
   L.lanes = o->lanes ? o->lanes : default_lanes(o->precision, method, L.kernel, l.entries, l.n);
+  if (L.kernel == 5) {
+    L.lanes = 1;
+    L.csr = ctx->full.ecsr();
+  }
   if (L.kernel == 4) {  // kernel 2 over the 16-byte-aligned copy, vector index loads
     L.csr = ctx->full.acsr();
     L.kernel = 2;
@@ -456,12 +489,279 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
     }
   }
   if (tv) LJ_CUDA(ctx, cudaEventRecord(tv[1], ctx->stream), "event");
-  LJ_CUDA(ctx, launch_force(L, ctx->stream), "force launch");
+  if (L.kernel == 5) LJ_CUDA(ctx, launch_force_ell(L, ctx->stream), "force launch");
+  else LJ_CUDA(ctx, launch_force(L, ctx->stream), "force launch");
   if (tv) LJ_CUDA(ctx, cudaEventRecord(tv[2], ctx->stream), "event");
   return LJ_OK;
 }
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// ---- autotuner ---------------------------------------------------------------
+struct TuneCand {
+  int method, kernel, lanes, unroll, block;
+};
+
+// Launch shapes worth timing for this precision, method and installed lists.
+std::vector<TuneCand> tune_candidates(lj_ctx* ctx, const lj_force_opts* opts) {
+  std::vector<TuneCand> cands;
+  const bool mixed = opts->precision != LJ_PREC_FP64;
+  const bool ff = opts->precision == LJ_PREC_MIXED;  // two-float pair terms
+  const bool try_gather = ctx->full.valid && opts->method != LJ_METHOD_SCATTER_HALF;
+  const bool try_scatter = ctx->half.valid && opts->method != LJ_METHOD_GATHER_FULL;
+  for (int block : {128, 256}) {
+    if (try_gather) {
+      if (mixed) {
+        if (!ff && ctx->tiled.valid && block == 128)
+          for (int g : {2, 4, 8})
+            for (int u : {2, 4}) cands.push_back({LJ_METHOD_GATHER_FULL, 3, g, u, 128});
+        for (int g : {2, 4, 8})
+          for (int u : {2, 4, 8})
+            if (!(ff && u == 8)) cands.push_back({LJ_METHOD_GATHER_FULL, 2, g, u, block});
+        if (ctx->full.avalid)
+          for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 4, g, 4, block});
+        for (int g : {4, 8, 16}) cands.push_back({LJ_METHOD_GATHER_FULL, 1, g, 0, block});
+        for (int u : {2, 4}) cands.push_back({LJ_METHOD_GATHER_FULL, 5, 1, u, block});
+      } else {
+        if (block == 128) cands.push_back({LJ_METHOD_GATHER_FULL, 2, 0, 0, 128});
+        for (int g : {4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 1, g, 0, block});
+        cands.push_back({LJ_METHOD_GATHER_FULL, 5, 1, 0, block});
+      }
+    }
+    if (try_scatter) {
+      if (!mixed && block == 128)
+        for (int g : {1, 2, 4, 8}) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, g, 0, 128});
+      if (mixed)
+        for (int g : {2, 4, 8})
+          for (int u : {2, 4}) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, g, u, block});
+      if (!ff)  // two-float scatters always run kernel 2
+        for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_SCATTER_HALF, 1, g, 0, block});
+    }
+  }
+  return cands;
+}
+
+lj_force_opts with_shape(const lj_force_opts* opts, const TuneCand& c) {
+  lj_force_opts o = *opts;
+  o.method = c.method;
+  o.kernel = c.kernel;
+  o.lanes = c.lanes;
+  o.unroll = c.unroll;
+  o.block = c.block;
+  return o;
+}
+
+// Mean time of `reps` calls of shape c on `part`, each call after a write
+// larger than L2 (a force call on a list that does not fit in L2 -- or a
+// benchmark that flushes -- starts cold; warm-cache timings favour other
+// shapes).  One untimed call first (warm-up and validity).
+int time_shape(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts* opts,
+               const TuneCand& c, int reps, double* ms_out) {
+  const lj_force_opts o = with_shape(opts, c);
+  int rc = run_force(ctx, part, n, &o);
+  if (rc) return rc;
+  float ms = 0.f;
+  for (int r = 0; r < reps; r++) {
+    LJ_CUDA(ctx, cudaMemsetAsync(ctx->tune_flush.ptr, r & 0xff, ctx->tune_flush.cap, ctx->stream),
+            "flush");
+    LJ_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream), "event");
+    if ((rc = run_force(ctx, part, n, &o))) return rc;
+    LJ_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream), "event");
+    LJ_CUDA(ctx, cudaEventSynchronize(ctx->ev[1]), "sync");
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]);
+    ms += t;
+  }
+  *ms_out = ms / reps;
+  return LJ_OK;
+}
+
+// The particles of one layout for timing: AoS is the caller's q (momenta in
+// tune_p); SoA and z are copies of q the tuner makes (momenta zeroed).
+int tune_particles(lj_ctx* ctx, const double* q, int32_t n, int layout, Particles* part) {
+  *part = Particles{};
+  cudaStream_t s = ctx->stream;
+  if (layout == LJ_LAYOUT_AOS) {
+    part->q = q;
+    part->p = ctx->tune_p.ptr;
+    return LJ_OK;
+  }
+  if (layout == LJ_LAYOUT_SOA) {
+    LJ_CUDA(ctx, ctx->tune_soa.ensure(6 * (size_t)n), "alloc");
+    double* b = ctx->tune_soa.ptr;
+    for (int d = 0; d < 3; d++)
+      LJ_CUDA(ctx, cudaMemcpy2DAsync(b + (size_t)d * n, sizeof(double), q + d, 4 * sizeof(double),
+                                     sizeof(double), (size_t)n, cudaMemcpyDeviceToDevice, s),
+              "SoA copy");
+    LJ_CUDA(ctx, cudaMemsetAsync(b + 3 * (size_t)n, 0, 3 * sizeof(double) * (size_t)n, s),
+            "memset");
+    part->soa = 1;
+    part->qx = b;
+    part->qy = b + n;
+    part->qz = b + 2 * (size_t)n;
+    part->px = b + 3 * (size_t)n;
+    part->py = b + 4 * (size_t)n;
+    part->pz = b + 5 * (size_t)n;
+    return LJ_OK;
+  }
+  LJ_CUDA(ctx, ctx->tune_z.ensure(8 * (size_t)n), "alloc");
+  double* z = ctx->tune_z.ptr;
+  LJ_CUDA(ctx, cudaMemsetAsync(z, 0, 8 * sizeof(double) * (size_t)n, s), "memset");
+  LJ_CUDA(ctx, cudaMemcpy2DAsync(z, 8 * sizeof(double), q, 4 * sizeof(double), 4 * sizeof(double),
+                                 (size_t)n, cudaMemcpyDeviceToDevice, s),
+          "z copy");
+  part->stride = 8;
+  part->q = z;
+  part->p = z + 4;
+  return LJ_OK;
+}
+
+// The cache key of a tuning problem (see lj_tune_result::key).
+std::string tune_key(lj_ctx* ctx, int32_t n, const lj_force_opts* opts, int layouts) {
+  cudaDeviceProp prop{};
+  cudaGetDeviceProperties(&prop, ctx->device);
+  std::string gpu = prop.name;
+  for (char& ch : gpu)
+    if (ch == ' ' || ch == '\t' || ch == '|') ch = '_';
+  double mean = 0.0;
+  if (ctx->full.valid && ctx->full.n > 0) mean = (double)ctx->full.entries / ctx->full.n;
+  else if (ctx->half.valid && ctx->half.n > 0) mean = 2.0 * (double)ctx->half.entries / ctx->half.n;
+  const int nclass = n > 0 ? (int)std::floor(std::log2((double)n)) : 0;
+  const int rclass = mean > 0.0 ? (int)std::lround(2.0 * std::log2(mean)) : -1;
+  char buf[160];
+  std::snprintf(buf, sizeof buf, "%s|sm%d|n2^%d|row2^%d/2|prec%d|pbc%d|m%d|lay%d",
+                gpu.c_str(), prop.multiProcessorCount, nclass, rclass, opts->precision,
+                opts->periodic ? 1 : 0, opts->method, layouts);
+  return buf;
+}
+
+// Cache file: one line per entry, "key method kernel lanes unroll block
+// layout ms"; the last line of a key wins.
+bool cache_lookup(const char* path, const std::string& key, TuneCand* c, int* layout, double* ms) {
+  FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  char line[512];
+  bool found = false;
+  while (std::fgets(line, sizeof line, f)) {
+    char k[256];
+    TuneCand t{};
+    int lay = 0;
+    double m = 0.0;
+    if (std::sscanf(line, "%255s %d %d %d %d %d %d %lf", k, &t.method, &t.kernel, &t.lanes,
+                    &t.unroll, &t.block, &lay, &m) == 8 &&
+        key == k) {
+      *c = t;
+      *layout = lay;
+      *ms = m;
+      found = true;
+    }
+  }
+  std::fclose(f);
+  return found;
+}
+
+void remember_tuned(lj_ctx* ctx, const lj_force_opts* opts, int32_t n, int layout,
+                    const TuneCand& c) {
+  lj_ctx::Tuned t{};
+  t.precision = opts->precision;
+  t.layout = layout;
+  t.periodic = opts->periodic != 0;
+  t.n = n;
+  t.entries_half = ctx->half.entries;
+  t.entries_full = ctx->full.entries;
+  t.method = c.method;
+  t.kernel = c.kernel;
+  t.lanes = c.lanes;
+  t.unroll = c.unroll;
+  t.block = c.block;
+  auto& v = ctx->tuned;
+  v.erase(std::remove_if(v.begin(), v.end(), [&](const lj_ctx::Tuned& x) {
+            return x.precision == t.precision && x.layout == t.layout && x.periodic == t.periodic;
+          }),
+          v.end());
+  v.push_back(t);
+}
+
+int autotune(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts* opts, int reps,
+             int layouts, const char* cache_path, lj_tune_result* out) {
+  int rc = check_opts(ctx, opts);
+  if (rc) return rc;
+  if (n < 1 || !q || !aligned16(q)) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "bad q or n");
+  if (!ctx->half.valid && !ctx->full.valid) return fail(ctx, LJ_ERR_NO_LIST, "no list installed");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
+  *out = lj_tune_result{};
+  const std::string key = tune_key(ctx, n, opts, layouts);
+  std::snprintf(out->key, sizeof out->key, "%s", key.c_str());
+  TuneCand win{};
+  int win_layout = LJ_LAYOUT_AOS;
+  double best_ms = 1e300;
+  if (cache_path && cache_lookup(cache_path, key, &win, &win_layout, &best_ms)) {
+    out->from_cache = 1;
+  } else {
+    std::vector<TuneCand> cands = tune_candidates(ctx, opts);
+    if (cands.empty()) return fail(ctx, LJ_ERR_NO_LIST, "no list for the requested method");
+    LJ_CUDA(ctx, ctx->tune_p.ensure(4 * (size_t)n), "alloc");
+    LJ_CUDA(ctx, ctx->tune_flush.ensure((size_t)256 << 20), "alloc");  // > L2 (126 MB)
+    const bool was_timing = ctx->timing;
+    ctx->timing = false;
+    struct Timed {
+      TuneCand c;
+      double ms;
+    };
+    std::vector<Timed> aos;
+    Particles part{};
+    for (const TuneCand& c : cands) {
+      double ms = 0.0;
+      if ((rc = tune_particles(ctx, q, n, LJ_LAYOUT_AOS, &part)) ||
+          (rc = time_shape(ctx, part, n, opts, c, reps, &ms))) {
+        ctx->timing = was_timing;
+        return rc;
+      }
+      out->timed++;
+      aos.push_back({c, ms});
+    }
+    std::stable_sort(aos.begin(), aos.end(),
+                     [](const Timed& a, const Timed& b) { return a.ms < b.ms; });
+    if (layouts & (1 << LJ_LAYOUT_AOS)) {
+      win = aos[0].c;
+      best_ms = aos[0].ms;
+    }
+    // the other layouts: the three fastest AoS shapes again
+    for (int lay : {LJ_LAYOUT_SOA, LJ_LAYOUT_Z}) {
+      if (!(layouts & (1 << lay))) continue;
+      if ((rc = tune_particles(ctx, q, n, lay, &part))) {
+        ctx->timing = was_timing;
+        return rc;
+      }
+      for (size_t k = 0; k < aos.size() && k < 3; k++) {
+        double ms = 0.0;
+        if ((rc = time_shape(ctx, part, n, opts, aos[k].c, reps, &ms))) {
+          ctx->timing = was_timing;
+          return rc;
+        }
+        out->timed++;
+        if (ms < best_ms) {
+          best_ms = ms;
+          win = aos[k].c;
+          win_layout = lay;
+        }
+      }
+    }
+    ctx->timing = was_timing;
+    if (cache_path) {
+      if (FILE* f = std::fopen(cache_path, "a")) {
+        std::fprintf(f, "%s %d %d %d %d %d %d %.6g\n", key.c_str(), win.method, win.kernel,
+                     win.lanes, win.unroll, win.block, win_layout, best_ms);
+        std::fclose(f);
+      }
+    }
+  }
+  out->best = with_shape(opts, win);
+  out->layout = win_layout;
+  out->ms = best_ms;
+  remember_tuned(ctx, opts, n, win_layout, win);
+  return LJ_OK;
+}
 
 }  // namespace
 
@@ -1030,6 +1330,7 @@ int lj_list_build(lj_ctx* ctx, const double* q, int32_t n, double rs, const doub
   ctx->full.valid = false;
   ctx->full.avalid = false;
   ctx->full.svalid = ctx->full.savalid = false;
+  ctx->full.evalid = false;
   ctx->tiled.valid = false;
   int full_maxrow = 0;
   LJ_CUDA(ctx, ctx->err2.ensure(2), "alloc");
@@ -1130,117 +1431,22 @@ int lj_autotune_aos(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts
   if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
   ctx->err.clear();
   if (!best || reps < 1) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "best is NULL or reps < 1");
-  int rc = check_opts(ctx, opts);
+  lj_tune_result r{};
+  const int rc = autotune(ctx, q, n, opts, reps, 1 << LJ_LAYOUT_AOS, nullptr, &r);
   if (rc) return rc;
-  if (n < 1 || !q || !aligned16(q)) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "bad q or n");
-  if (!ctx->half.valid && !ctx->full.valid) return fail(ctx, LJ_ERR_NO_LIST, "no list installed");
-  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, LJ_ERR_CUDA, "set device");
-  LJ_CUDA(ctx, ctx->tune_p.ensure(4 * (size_t)n), "alloc");
-  LJ_CUDA(ctx, ctx->tune_flush.ensure((size_t)256 << 20), "alloc");  // > L2 (126 MB)
-  // candidate launch shapes
-  struct Cand { int method, kernel, lanes, unroll, block; };
-  std::vector<Cand> cands;
-  const bool mixed = opts->precision != LJ_PREC_FP64;
-  const bool ff = opts->precision == LJ_PREC_MIXED;  // two-float pair terms
-  const bool try_gather = ctx->full.valid && opts->method != LJ_METHOD_SCATTER_HALF;
-  const bool try_scatter = ctx->half.valid && opts->method != LJ_METHOD_GATHER_FULL;
-  for (int block : {128, 256}) {
-    if (try_gather) {
-      if (mixed) {
-        if (!ff && ctx->tiled.valid && block == 128)
-          for (int g : {2, 4, 8})
-            for (int u : {2, 4}) cands.push_back({LJ_METHOD_GATHER_FULL, 3, g, u, 128});
-        for (int g : {2, 4, 8})
-          for (int u : {2, 4, 8})
-            if (!(ff && u == 8)) cands.push_back({LJ_METHOD_GATHER_FULL, 2, g, u, block});
-        if (ctx->full.avalid)
-          for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 4, g, 4, block});
-        for (int g : {4, 8, 16}) cands.push_back({LJ_METHOD_GATHER_FULL, 1, g, 0, block});
-      } else {
-        if (block == 128) cands.push_back({LJ_METHOD_GATHER_FULL, 2, 0, 0, 128});
-        for (int g : {4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 1, g, 0, block});
-      }
-    }
-    if (try_scatter) {
-      if (!mixed && block == 128)
-        for (int g : {1, 2, 4, 8}) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, g, 0, 128});
-      if (mixed)
-        for (int g : {2, 4, 8})
-          for (int u : {2, 4}) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, g, u, block});
-      if (!ff)  // two-float scatters always run kernel 2
-        for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_SCATTER_HALF, 1, g, 0, block});
-    }
-  }
-  if (cands.empty()) return fail(ctx, LJ_ERR_NO_LIST, "no list for the requested method");
-  Particles part{};
-  part.q = q;
-  part.p = ctx->tune_p.ptr;
-  const bool was_timing = ctx->timing;
-  ctx->timing = false;
-  double best_ms = 1e300;
-  Cand win = cands[0];
-  for (const Cand& c : cands) {
-    lj_force_opts o = *opts;
-    o.method = c.method;
-    o.kernel = c.kernel;
-    o.lanes = c.lanes;
-    o.unroll = c.unroll;
-    o.block = c.block;
-    if ((rc = run_force(ctx, part, n, &o))) {  // warm-up (and validity)
-      ctx->timing = was_timing;
-      return rc;
-    }
-    // each call starts with a cold L2 (a write larger than it in between), as
-    // a force call on a list that does not fit in L2 -- or a benchmark that
-    // flushes -- sees it; warm-cache timings favour other shapes
-    float ms = 0.f;
-    for (int r = 0; r < reps; r++) {
-      LJ_CUDA(ctx, cudaMemsetAsync(ctx->tune_flush.ptr, r & 0xff, ctx->tune_flush.cap,
-                                   ctx->stream), "flush");
-      LJ_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream), "event");
-      if ((rc = run_force(ctx, part, n, &o))) {
-        ctx->timing = was_timing;
-        return rc;
-      }
-      LJ_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream), "event");
-      LJ_CUDA(ctx, cudaEventSynchronize(ctx->ev[1]), "sync");
-      float t = 0.f;
-      cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]);
-      ms += t;
-    }
-    if (ms / reps < best_ms) {
-      best_ms = ms / reps;
-      win = c;
-    }
-  }
-  ctx->timing = was_timing;
-  *best = *opts;
-  best->method = win.method;
-  best->kernel = win.kernel;
-  best->lanes = win.lanes;
-  best->unroll = win.unroll;
-  best->block = win.block;
-  if (ms_best) *ms_best = best_ms;
-  // remember the winner for calls that leave the launch fields at zero
-  lj_ctx::Tuned t{};
-  t.precision = opts->precision;
-  t.soa = 0;
-  t.periodic = opts->periodic != 0;
-  t.n = n;
-  t.entries_half = ctx->half.entries;
-  t.entries_full = ctx->full.entries;
-  t.method = win.method;
-  t.kernel = win.kernel;
-  t.lanes = win.lanes;
-  t.unroll = win.unroll;
-  t.block = win.block;
-  auto& v = ctx->tuned;
-  v.erase(std::remove_if(v.begin(), v.end(), [&](const lj_ctx::Tuned& x) {
-            return x.precision == t.precision && x.soa == t.soa && x.periodic == t.periodic;
-          }),
-          v.end());
-  v.push_back(t);
+  *best = r.best;
+  if (ms_best) *ms_best = r.ms;
   return LJ_OK;
+}
+
+int lj_autotune(lj_ctx* ctx, const double* q, int32_t n, const lj_force_opts* opts,
+                int32_t reps, int32_t layouts, const char* cache_path, lj_tune_result* out) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (!out || reps < 1) return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "out is NULL or reps < 1");
+  if (layouts < 0 || layouts > 7)
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "layouts must be a mask of 1 << LJ_LAYOUT_*");
+  return autotune(ctx, q, n, opts, reps, layouts ? layouts : 1 << LJ_LAYOUT_AOS, cache_path, out);
 }
 
 int lj_measure_aos(lj_ctx* ctx, const double* q_host, double* p_host, int32_t n,
@@ -1276,6 +1482,8 @@ int lj_measure_aos(lj_ctx* ctx, const double* q_host, double* p_host, int32_t n,
     if (ctx->host_kind == LJ_LIST_FULL && l.avalid)  // the gather reads the aligned copy
       LJ_CUDA(ctx, launch_copy_rows4(l.np.ptr, l.ptr.ptr, l.list.ptr, l.aoff.ptr, l.n,
                                      l.alist.ptr, l.aptr.ptr, s), "aligned copy");
+    if (ctx->host_kind == LJ_LIST_FULL && l.evalid && (rc = ensure_ell(ctx, true)))
+      return rc;  // and kernel 5 its transposed copy
   }
   LJ_CUDA(ctx, cudaEventRecord(ctx->ev[1], s), "event");
   Particles part{};

@@ -61,6 +61,11 @@ struct DevList {
   // their near counts; reset whenever the list changes
   DevBuf<int32_t> slist, snn, salist, sann;
   bool svalid = false, savalid = false;
+  // transposed copy for the ELL gather (kernel 5): entry k of row i at
+  // ell[i + k n], n x max_row words; built on first use, reset with the list
+  DevBuf<int32_t> ell;
+  bool evalid = false;
+  Csr ecsr() const { return Csr{n, entries, np.ptr, nullptr, ell.ptr, n, 0}; }
 };
 
 struct MdState;  // lj_md.cu
@@ -124,9 +129,11 @@ struct lj_ctx {
   } tiled;
   // autotuner (lj_autotune_aos): scratch p and the chosen shapes
   ljg::DevBuf<double> tune_p;
+  ljg::DevBuf<double> tune_soa;  // q and p as six arrays (SoA candidates)
+  ljg::DevBuf<double> tune_z;    // interleaved z[n][8] (z-layout candidates)
   ljg::DevBuf<unsigned char> tune_flush;  // written between timed tuner calls (> L2)
   struct Tuned {
-    int precision, soa, periodic, n;
+    int precision, layout, periodic, n;  // layout: LJ_LAYOUT_*
     int64_t entries_half, entries_full;
     int method, kernel, lanes, unroll, block;
   };

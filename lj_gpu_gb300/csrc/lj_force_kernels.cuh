@@ -254,26 +254,38 @@ __device__ __forceinline__ double df_fp64(double r2, const Fp64Consts& k) {
   return (r6 * inv) * fma(-k.c48, r6, k.c24);
 }
 
+// Address of entry k of row i: row-major rows (CSR, or padded rows when
+// C.ptr is null) at k0 + k, or with ELL the transposed ("ELL") list of the
+// reference, entry k of row i at i + k C.stride (C.stride = the column
+// length, cuda/force_cuda.cu:229-240).  ELL kernels run one lane per row, so
+// a warp's index loads of one step are consecutive words.
+template <bool ELL>
+__device__ __forceinline__ int64_t entry_addr(const Csr& C, int i, int64_t k0, int k) {
+  return ELL ? (int64_t)i + (int64_t)k * C.stride : k0 + k;
+}
+
 // ---------------------------------------------------------------------------
 // FP64 gather over the full list
 // ---------------------------------------------------------------------------
-template <int G, bool PBC, bool SOA>
+template <int G, bool PBC, bool SOA, bool ELL = false>
 __global__ void __launch_bounds__(256) k_gather_fp64(const Particles P, const Csr C,
                                                      const Fp64Consts K) {
+  static_assert(!ELL || G == 1, "the transposed list takes one lane per row");
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / G;
   const int lane = t & (G - 1);
   const bool valid = i < C.n;
-  int cnt = 0, k0 = 0;
+  int cnt = 0;
+  int64_t k0 = 0;
   double3 qi = make_double3(0, 0, 0);
   if (valid) {
     cnt = __ldg(C.np + i);
-    k0 = __ldg(C.ptr + i);
+    if (!ELL) k0 = __ldg(C.ptr + i);
     qi = load_q<SOA>(P, i);
   }
   double fx = 0.0, fy = 0.0, fz = 0.0;
   for (int k = lane; k < cnt; k += G) {
-    const int j = __ldg(C.list + k0 + k);
+    const int j = __ldg(C.list + entry_addr<ELL>(C, i, k0, k));
     const double3 d = sep_fp64<PBC>(qi, load_q<SOA>(P, j), K);
     const double r2 = r2_fp64(d);
     if (beyond_cutoff(r2, K.cl2_bits)) continue;
@@ -683,11 +695,14 @@ __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const C
 // l of a row takes the 4 consecutive entries base + 4 l .. + 3 with one
 // 16-byte load, which quarters the index-load instructions and the L1
 // wavefronts they cost (a 32-lane scalar index load touches one line per row).
-template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC = false, bool FF = false>
+// ELL (G = 1): the transposed list (entry_addr).
+template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC = false, bool FF = false,
+          bool ELL = false>
 __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const Csr C,
                                                         const int4* __restrict__ qfix,
                                                         const MixedConsts K0) {
   static_assert(!VEC || U == 4, "vector index loads take 4 entries per lane");
+  static_assert(!ELL || (G == 1 && !VEC), "the transposed list takes one lane per row");
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / G;
   const int lane = t & (G - 1);
@@ -702,7 +717,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
   int4 xi = make_int4(0, 0, 0, 0);
   if (valid) {
     cnt = __ldg(C.np + i);
-    k0 = row_start(C, i);
+    if (!ELL) k0 = row_start(C, i);
     xi = __ldg(qfix + i);
   }
   int cmax = cnt;
@@ -726,7 +741,9 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
     } else {
 #pragma unroll
       for (int u = 0; u < U; u++)
-        jn[u] = entry(base, u) < cnt ? __ldg(C.list + k0 + entry(base, u)) : 0;
+        jn[u] = entry(base, u) < cnt
+                    ? __ldg(C.list + entry_addr<ELL>(C, i, k0, entry(base, u)))
+                    : 0;
     }
   };
   int jn[U];

@@ -177,6 +177,10 @@ cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s);
 cudaError_t launch_partition_near(const ForceLaunch& L, const Csr& in, int32_t* out, int32_t* nn,
                                   const int32_t* guard, cudaStream_t s);
 cudaError_t launch_force(const ForceLaunch& L, cudaStream_t s);
+// Gather over the transposed full list (kernel 5): L.csr = {n, entries, np,
+// nullptr, ell, stride = n}; FP64, FP32 or two-float terms by L.precision,
+// unroll 2 or 4 for the mixed precisions.
+cudaError_t launch_force_ell(const ForceLaunch& L, cudaStream_t s);
 cudaError_t launch_force_pairs(const Particles& part, int n, const int32_t* ip,
                                const int32_t* jp, int64_t npairs, const Periodic& box,
                                double dt, double cl2, cudaStream_t s);

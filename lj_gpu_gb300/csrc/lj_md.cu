@@ -534,7 +534,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     m.graph = nullptr;
   }
   m.loop.reset();
-  if (gsteps > 1 &&
+  if (gsteps > 1 && !prm->chunk_graphs &&
       m.loop.build(s, m.flags.ptr + F_LOOP, m.flags.ptr + F_OVERFLOW,
                    [&](cudaStream_t cs) {
                      cudaError_t ce = cudaSuccess;

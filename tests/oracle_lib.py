@@ -167,6 +167,29 @@ def force_sorted_aos(q, p, npp, ptr, lst, cl2=9.0, dt=0.001, box=None, calls=1):
     return p
 
 
+def velocity_verlet(q, p, L, rc, dt, steps):
+    """FP64 velocity Verlet (m = 1) in the periodic cubic box L: kick dt/2,
+    drift, kick dt/2 per step, each kick the restated force_sorted
+    (cpu_ref/force_aos.cpp:192-224) over a half list rebuilt from the current
+    positions (radius rc + 0.2), so only the cutoff decides membership.
+    Returns new (q, p); the inputs are not modified."""
+    q, p = q.copy(), p.copy()
+    box = np.array([L, L, L], np.float64)
+    for _ in range(steps):
+        half = build_list(q, rc + 0.2, box=L)
+        force_sorted_aos(q, p, *half, cl2=rc * rc, dt=0.5 * dt, box=L)
+        oracle().lj_or_drift(q, p, q.shape[0], dt, box.ctypes.data)
+        half = build_list(q, rc + 0.2, box=L)
+        force_sorted_aos(q, p, *half, cl2=rc * rc, dt=0.5 * dt, box=L)
+    return q, p
+
+
+def periodic_diff(a, b, L):
+    """Minimum-image difference of the positions of two AoS arrays."""
+    d = a[:, :3] - b[:, :3]
+    return d - L * np.round(d / L)
+
+
 def force_sorted_soa(q, p, npp, ptr, lst, cl2=9.0, dt=0.001, box=None, calls=1):
     """q, p given as (n, 4) arrays; converted to the SoA rows the reference uses."""
     b, bp = _box(box)

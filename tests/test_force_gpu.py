@@ -60,14 +60,14 @@ def system(name):
 
 
 def run_engine(engine, q, half, box, precision, method, layout, calls, dt, lanes=0, ctx=None,
-               kernel=0, unroll=0):
+               kernel=0, unroll=0, ff_all=False):
     own = ctx is None
     ctx = ctx or engine.Context(0)
     try:
         npp, ptr, lst = half
         ctx.set_list_csr(dev(npp), dev(ptr), dev(lst), kind="half")
         opts = engine.make_opts(dt=dt, cl2=9.0, box=box, precision=precision, method=method,
-                                lanes=lanes, kernel=kernel, unroll=unroll)
+                                lanes=lanes, kernel=kernel, unroll=unroll, ff_all=ff_all)
         if layout == "aos":
             qd, pd = dev(q), dev(np.zeros_like(q))
             for _ in range(calls):
@@ -435,7 +435,7 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(engine, prec):
         qd = dev(q)
         opts = engine.make_opts(dt=0.005, cl2=9.0, box=box, precision=prec)
         best, ms = ctx.autotune(qd, opts, reps=2)
-        assert ms > 0 and best.method in (1, 2) and best.kernel in (1, 2, 3, 4)
+        assert ms > 0 and best.method in (1, 2) and best.kernel in (1, 2, 3, 4, 5)
         # the tuned shape is used by default-option calls and keeps parity
         for o in (opts, best):
             pd = dev(np.zeros_like(q))
@@ -491,6 +491,121 @@ def test_transposed_list_round_trip(engine):
         bad = ell.copy()
         with pytest.raises(engine.LJError):  # array too short for the rows
             ctx.set_list_ell(dev(npp), dev(bad[:width]), width, kind="full")
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+@pytest.mark.parametrize("layout", ["aos", "soa"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_fp32"])
+def test_transposed_list_gather_kernel5(engine, name, layout, prec):
+    """Kernel 5 reads the transposed copy of the full list (entry k of row i
+    at [i + k n], the layout of the reference's ELL kernels): the same bits
+    as the row-major list with one lane per row and the same terms (FP64:
+    kernel 1; mixed: kernel 2 with every pair in its own terms), and the
+    oracle's bars."""
+    q, box, half = system(name)
+    ref = oracle_p(q, half, box, 2, 0.005)
+    unrolls = [0] if prec == "fp64" else [2, 4]
+    with engine.Context(0) as ctx:
+        for u in unrolls:
+            got = run_engine(engine, q, half, box, prec, "gather", layout, 2, 0.005, ctx=ctx,
+                             kernel=5, unroll=u)
+            row = run_engine(engine, q, half, box, prec, "gather", layout, 2, 0.005, ctx=ctx,
+                             kernel=1 if prec == "fp64" else 2, lanes=1, unroll=u,
+                             ff_all=prec == "mixed")
+            assert np.array_equal(got, row), (u, np.abs(got - row).max())
+            e = ol.rel_errors(got, ref)
+            if prec == "fp64":
+                assert e["max_rel"] <= FP64_TOL, e
+            else:
+                check_mixed(e, prec, u)
+
+
+def test_kernel5_options_and_lists_from_ell(engine):
+    """Kernel 5 takes one lane per row and unroll 2 or 4 (mixed); a list
+    installed in the transposed layout runs it too, and a new list replaces
+    its transposed copy."""
+    q, box, half = system("pbc_rho0.5")
+    full = ol.build_list(q, 3.3, box=box, full=True)
+    n = q.shape[0]
+    npp, ptr, lst = full
+    ell = np.zeros(int(npp.max()) * n, np.int32)
+    for i in range(n):
+        ell[i + np.arange(npp[i]) * n] = lst[ptr[i]:ptr[i] + npp[i]]
+    ref = oracle_p(q, half, box, 1, 0.005)
+    with engine.Context(0) as ctx:
+        ctx.set_list_ell(dev(npp), dev(ell), n, kind="full")
+        qd = dev(q)
+        for prec in ("fp64", "mixed"):
+            pd = dev(np.zeros_like(q))
+            ctx.force_aos(qd, pd, engine.make_opts(dt=0.005, cl2=9.0, box=box, precision=prec,
+                                                   kernel=5))
+            e = ol.rel_errors(host(pd), ref)
+            assert e["max_rel"] <= (FP64_TOL if prec == "fp64" else MIXED_TOL["max_rel"]), e
+        for bad in (dict(lanes=4), dict(precision="mixed", unroll=8)):
+            kw = dict(dt=0.005, cl2=9.0, box=box, kernel=5)
+            kw.update(bad)
+            with pytest.raises(engine.LJError):
+                ctx.force_aos(qd, dev(np.zeros_like(q)), engine.make_opts(**kw))
+        # another list: its own transposed copy (a stale copy would not match)
+        q2, box2, half2 = system("pbc_rho1")
+        ctx.set_list_csr(dev(half2[0]), dev(half2[1]), dev(half2[2]))
+        pd = dev(np.zeros_like(q2))
+        ctx.force_aos(dev(q2), pd, engine.make_opts(dt=0.005, cl2=9.0, box=box2, kernel=5))
+        ref2 = oracle_p(q2, half2, box2, 1, 0.005)
+        assert ol.rel_errors(host(pd), ref2)["max_rel"] <= FP64_TOL
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_autotune_layouts_and_cache(engine, prec, tmp_path):
+    """lj_autotune over launch shapes, the transposed list and the AoS, SoA
+    and z layouts: the winner keeps parity in its layout, lands in the cache
+    file under the problem's key, and a second context with the same key
+    takes it from the cache without timing anything."""
+    q, box, half = system("pbc_rho1")
+    ref = oracle_p(q, half, box, 1, 0.005)
+    cache = tmp_path / "tune.txt"
+    results = []
+    for _ in range(2):
+        with engine.Context(0) as ctx:
+            ctx.set_list_csr(dev(half[0]), dev(half[1]), dev(half[2]))
+            qd = dev(q)
+            opts = engine.make_opts(dt=0.005, cl2=9.0, box=box, precision=prec)
+            r = ctx.autotune_layouts(qd, opts, reps=1, layouts=("aos", "soa", "z"), cache=cache)
+            results.append(r)
+            assert r["layout"] in ("aos", "soa", "z") and r["ms"] > 0
+            assert r["opts"].kernel in (1, 2, 3, 4, 5) and r["opts"].method in (1, 2)
+            # the winner, called in its layout with default launch fields and
+            # with its explicit shape, keeps parity
+            for o in (opts, r["opts"]):
+                if r["layout"] == "aos":
+                    pd = dev(np.zeros_like(q))
+                    ctx.force_aos(qd, pd, o)
+                    got = host(pd)
+                elif r["layout"] == "soa":
+                    qs = [dev(q[:, d].copy()) for d in range(3)]
+                    ps = [dev(np.zeros(q.shape[0])) for _ in range(3)]
+                    ctx.force_soa(*qs, *ps, o)
+                    got = np.stack([host(x) for x in ps] + [np.zeros(q.shape[0])], axis=1)
+                else:
+                    z = np.zeros((q.shape[0], 8))
+                    z[:, :4] = q
+                    zd = dev(z)
+                    ctx.force_z(zd, o)
+                    got = host(zd)[:, 4:8]
+                e = ol.rel_errors(got, ref)
+                if prec == "fp64":
+                    assert e["max_rel"] <= FP64_TOL, e
+                else:
+                    check_mixed(e, prec)
+    first, second = results
+    assert not first["from_cache"] and first["timed"] > 3
+    assert second["from_cache"] and second["timed"] == 0
+    assert second["key"] == first["key"] and f"prec{engine.make_opts(precision=prec).precision}" in first["key"]
+    assert second["layout"] == first["layout"]
+    for f in ("method", "kernel", "lanes", "unroll", "block"):
+        assert getattr(second["opts"], f) == getattr(first["opts"], f), f
+    lines = cache.read_text().splitlines()
+    assert len(lines) == 1 and lines[0].startswith(first["key"] + " ")
 
 
 @pytest.mark.parametrize("name", list(SYSTEMS))
@@ -616,7 +731,7 @@ def test_launch_option_checks(engine, fixture_rho05):
     with engine.Context(0) as ctx:
         ctx.set_list_csr(dev(f["np"]), dev(f["ptr"]), dev(f["list"]))
         qd, pd = dev(f["q"]), dev(np.zeros_like(f["q"]))
-        for kw in (dict(kernel=5), dict(kernel=-1), dict(unroll=-1),
+        for kw in (dict(kernel=6), dict(kernel=-1), dict(unroll=-1),
                    dict(precision="mixed", method="gather", kernel=4, unroll=2)):
             opts = engine.make_opts(**kw)
             with pytest.raises(engine.LJError) as e:

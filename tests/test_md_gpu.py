@@ -17,22 +17,8 @@ def _dev(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-def oracle_vv(q, p, L, rc, dt, steps):
-    q, p = q.copy(), p.copy()
-    O = ol.oracle()
-    box = np.array([L, L, L])
-    for _ in range(steps):
-        half = ol.build_list(q, rc + 0.2, box=L)
-        ol.force_sorted_aos(q, p, *half, cl2=rc * rc, dt=0.5 * dt, box=L)
-        O.lj_or_drift(q, p, q.shape[0], dt, box.ctypes.data)
-        half = ol.build_list(q, rc + 0.2, box=L)
-        ol.force_sorted_aos(q, p, *half, cl2=rc * rc, dt=0.5 * dt, box=L)
-    return q, p
-
-
-def periodic_diff(a, b, L):
-    d = a[:, :3] - b[:, :3]
-    return d - L * np.round(d / L)
+oracle_vv = ol.velocity_verlet
+periodic_diff = ol.periodic_diff
 
 
 @pytest.mark.parametrize("graph_steps", [1, 8])
