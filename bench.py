@@ -78,6 +78,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kick-lanes", type=int, default=0,
+                    help="MD workloads: lanes per row of the mixed gather kick (0: default)")
     ap.add_argument("--chunk-graphs", action="store_true",
                     help="MD workloads: launch the captured step chunks from the host "
                          "instead of the persistent WHILE-node graph, so that a profiler "
@@ -697,7 +699,7 @@ def run_md8m(args, dist):
         qd, pd = torch.from_numpy(q).to(dev), torch.from_numpy(p0).to(dev)
         ctx = lj.Context(dist.local, stream=stream)
         prm = lj.make_md_params(DT, RC, RS - RC, L, precision=prec, rebuild_every=REBUILD_8M,
-                                chunk_graphs=args.chunk_graphs)
+                                chunk_graphs=args.chunk_graphs, kick_lanes=args.kick_lanes)
         ctx.md_run(qd, pd, prm, W, max_records=0)  # warm-up: its own build + W steps
         ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         torch.cuda.synchronize()

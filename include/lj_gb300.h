@@ -300,7 +300,10 @@ typedef struct lj_md_params {
                              persistent graph (a WHILE node); 1: as chunk graphs
                              launched back to back from the host, whose kernels
                              profilers can capture one by one */
-  int32_t reserved[2];
+  int32_t kick_lanes;     /* lanes per row of the mixed gather kick: 0 = the
+                             default (1 for LJ_PREC_MIXED, 4 for
+                             LJ_PREC_MIXED_FP32), else 1, 2, 4 or 8 */
+  int32_t reserved;
 } lj_md_params;
 
 typedef struct lj_md_record {

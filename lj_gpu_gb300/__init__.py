@@ -92,7 +92,7 @@ class MdParams(C.Structure):
         ("dt", C.c_double), ("rc", C.c_double), ("skin", C.c_double), ("box", C.c_double * 3),
         ("precision", C.c_int32), ("record_every", C.c_int32), ("graph_steps", C.c_int32),
         ("rebuild_every", C.c_int32), ("ff_all", C.c_int32), ("chunk_graphs", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("kick_lanes", C.c_int32), ("reserved", C.c_int32),
     ]
 
 
@@ -107,7 +107,7 @@ class MdStats(C.Structure):
 
 
 def make_md_params(dt, rc, skin, box, precision="mixed", record_every=0, graph_steps=0,
-                   rebuild_every=0, ff_all=False, chunk_graphs=False):
+                   rebuild_every=0, ff_all=False, chunk_graphs=False, kick_lanes=0):
     m = MdParams()
     m.dt, m.rc, m.skin = float(dt), float(rc), float(skin)
     b = [float(box)] * 3 if isinstance(box, (int, float)) else [float(v) for v in box]
@@ -117,6 +117,7 @@ def make_md_params(dt, rc, skin, box, precision="mixed", record_every=0, graph_s
     m.rebuild_every = int(rebuild_every)
     m.ff_all = 1 if ff_all else 0
     m.chunk_graphs = 1 if chunk_graphs else 0
+    m.kick_lanes = int(kick_lanes)
     return m
 
 

@@ -380,8 +380,9 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     B_CUDA(ctx, cudaEventCreate(&e0), "event");
     B_CUDA(ctx, cudaEventCreate(&e1), "event");
     // lanes, entries in flight, 16-byte index loads
-    const int shapes[][3] = {{2, 4, 0}, {4, 2, 0}, {4, 4, 0}, {8, 2, 0}, {8, 4, 0},
-                             {2, 4, 1}, {4, 4, 1}, {8, 4, 1}};
+    const int shapes[][3] = {{1, 2, 0}, {1, 4, 0}, {2, 4, 0}, {4, 2, 0}, {4, 4, 0},
+                             {8, 2, 0}, {8, 4, 0}, {1, 4, 1}, {2, 4, 1}, {4, 4, 1},
+                             {8, 4, 1}};
     for (SizeClass& k : cls) {
       k.ms = 1e300;
       for (const auto& sh : shapes) {

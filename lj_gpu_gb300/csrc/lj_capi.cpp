@@ -112,6 +112,11 @@ Periodic make_periodic(const lj_force_opts* o) {
 //   FP64 gather   : kernel 2 (compacted, one warp per row)
 int default_lanes(int precision, int method, int kernel, int64_t entries, int n) {
   const double avg = n > 0 ? (double)entries / n : 0.0;
+  // two-float gathers are issue-bound: one lane per row wastes the fewest
+  // slots on row ends and group sums (1M rho = 1: 139 G pair/s against 115
+  // with 4 lanes); FP32 pair terms are bound by the L1 gathers and keep 4
+  if (kernel >= 2 && precision == LJ_PREC_MIXED && method == LJ_METHOD_GATHER_FULL)
+    return avg <= 24 ? 2 : 1;
   if (kernel >= 2 && precision != LJ_PREC_FP64) return avg <= 24 ? 2 : 4;
   if (precision == LJ_PREC_FP64 && method == LJ_METHOD_SCATTER_HALF) return avg <= 12 ? 2 : 4;
   if (avg <= 12) return 2;
@@ -515,11 +520,11 @@ std::vector<TuneCand> tune_candidates(lj_ctx* ctx, const lj_force_opts* opts) {
         if (!ff && ctx->tiled.valid && block == 128)
           for (int g : {2, 4, 8})
             for (int u : {2, 4}) cands.push_back({LJ_METHOD_GATHER_FULL, 3, g, u, 128});
-        for (int g : {2, 4, 8})
+        for (int g : {1, 2, 4, 8})
           for (int u : {2, 4, 8})
             if (!(ff && u == 8)) cands.push_back({LJ_METHOD_GATHER_FULL, 2, g, u, block});
         if (ctx->full.avalid)
-          for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 4, g, 4, block});
+          for (int g : {1, 2, 4, 8}) cands.push_back({LJ_METHOD_GATHER_FULL, 4, g, 4, block});
         for (int g : {4, 8, 16}) cands.push_back({LJ_METHOD_GATHER_FULL, 1, g, 0, block});
         for (int u : {2, 4}) cands.push_back({LJ_METHOD_GATHER_FULL, 5, 1, u, block});
       } else {
@@ -532,7 +537,7 @@ std::vector<TuneCand> tune_candidates(lj_ctx* ctx, const lj_force_opts* opts) {
       if (!mixed && block == 128)
         for (int g : {1, 2, 4, 8}) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, g, 0, 128});
       if (mixed)
-        for (int g : {2, 4, 8})
+        for (int g : {1, 2, 4, 8})
           for (int u : {2, 4}) cands.push_back({LJ_METHOD_SCATTER_HALF, 2, g, u, block});
       if (!ff)  // two-float scatters always run kernel 2
         for (int g : {2, 4, 8}) cands.push_back({LJ_METHOD_SCATTER_HALF, 1, g, 0, block});

@@ -307,6 +307,9 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   if (prm->precision != LJ_PREC_MIXED && prm->precision != LJ_PREC_MIXED_FP32 &&
       prm->precision != LJ_PREC_FP64)
     return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (!(prm->kick_lanes == 0 || prm->kick_lanes == 1 || prm->kick_lanes == 2 ||
+        prm->kick_lanes == 4 || prm->kick_lanes == 8))
+    return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "kick_lanes must be 0, 1, 2, 4 or 8");
   const double rs = prm->rc + prm->skin;
   for (int d = 0; d < 3; d++)
     if (!(prm->box[d] > 2.0 * rs))
@@ -403,7 +406,10 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   K.method = mixed ? LJ_METHOD_GATHER_FULL : LJ_METHOD_SCATTER_HALF;
   K.kernel = 2;
   K.unroll = 4;
-  K.lanes = mixed ? 4 : 4;
+  // two-float kicks take one lane per row by default (issue-bound: fewest
+  // slots lost at row ends), FP32 kicks four (bound by the L1 gathers)
+  K.lanes = prm->kick_lanes && mixed ? prm->kick_lanes
+                                     : (prm->precision == LJ_PREC_MIXED ? 1 : 4);
   K.block = 128;
   K.qfix = m.qfix.ptr;
   make_fixed_frame(K);
