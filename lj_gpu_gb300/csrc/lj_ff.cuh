@@ -176,4 +176,158 @@ struct AccFF {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Two pair terms at once: packed f32x2 instructions (sm_100 and later) carry
+// one pair in each 32-bit half of a 64-bit register.  Every packed operation
+// is the scalar code's IEEE operation (round to nearest, no flush) on each
+// half, so a pair's bits do not depend on which form evaluated it, and a step
+// costs fewer FP32 issue slots.  PTX has no packed negation, so the
+// operations with a negated operand stay scalar (f2_fms, f2_nfma).
+// ---------------------------------------------------------------------------
+typedef unsigned long long f2;  // low half: first pair, high half: second pair
+
+__device__ __forceinline__ f2 f2_pack(float a, float b) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_splat(float a) { return f2_pack(a, a); }
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+  f2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+  f2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+  f2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+  f2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+// a b - c and c - a b per half: two scalar FMAs, whose negated operand is
+// free (a packed negation would cost two integer XORs on the ALU pipe, the
+// busiest pipe of the two-float gathers)
+__device__ __forceinline__ f2 f2_fms(f2 a, f2 b, f2 c) {
+  float a0, a1, b0, b1, c0, c1;
+  f2_unpack(a, a0, a1);
+  f2_unpack(b, b0, b1);
+  f2_unpack(c, c0, c1);
+  return f2_pack(__fmaf_rn(a0, b0, -c0), __fmaf_rn(a1, b1, -c1));
+}
+__device__ __forceinline__ f2 f2_nfma(f2 a, f2 b, f2 c) {
+  float a0, a1, b0, b1, c0, c1;
+  f2_unpack(a, a0, a1);
+  f2_unpack(b, b0, b1);
+  f2_unpack(c, c0, c1);
+  return f2_pack(__fmaf_rn(-a0, b0, c0), __fmaf_rn(-a1, b1, c1));
+}
+
+struct ff2 {
+  f2 h, l;
+};
+
+__device__ __forceinline__ ff2 ff2_mul(ff2 a, ff2 b) {
+  const f2 p = f2_mul(a.h, b.h);
+  f2 e = f2_fms(a.h, b.h, p);
+  e = f2_fma(a.h, b.l, e);
+  e = f2_fma(a.l, b.h, e);
+  return ff2{p, e};
+}
+
+__device__ __forceinline__ ff2 ff2_sqr(ff2 a) {
+  const f2 p = f2_mul(a.h, a.h);
+  f2 e = f2_fms(a.h, a.h, p);
+  e = f2_fma(f2_add(a.h, a.h), a.l, e);
+  return ff2{p, e};
+}
+
+__device__ __forceinline__ ff2 ff2_two_sum(f2 a, f2 b) {
+  const f2 s = f2_add(a, b);
+  const f2 bb = f2_sub(s, a);
+  const f2 e = f2_add(f2_sub(a, f2_sub(s, bb)), f2_sub(b, bb));
+  return ff2{s, e};
+}
+
+// pair_sep_ff of two pairs (i, j0) and (i, j1): a + b per axis and S + s.
+template <bool ANISO>
+__device__ __forceinline__ void pair_sep_ff2(const int4& xi, int lix, int liy, int liz,
+                                             const int4& xj0, const int4& xj1, const float* uh,
+                                             const float* ul, f2 (&a)[3], f2 (&b)[3], f2& S,
+                                             f2& s) {
+  int l0[3], l1[3];
+  image_lo(xj0.w, l0[0], l0[1], l0[2]);
+  image_lo(xj1.w, l1[0], l1[1], l1[2]);
+  const int ci[3] = {xi.x, xi.y, xi.z}, c0[3] = {xj0.x, xj0.y, xj0.z},
+            c1[3] = {xj1.x, xj1.y, xj1.z}, li[3] = {lix, liy, liz};
+  const f2 fine = f2_splat(0.0009765625f);
+  f2 p[3], e[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    // sep_axis_ff of both pairs; the scaling of the fine part packed
+    const int dh0 = wrap_sub(c0[d], ci[d]), dh1 = wrap_sub(c1[d], ci[d]);
+    a[d] = f2_pack(__int2float_rn(dh0 & ~255), __int2float_rn(dh1 & ~255));
+    b[d] = f2_mul(f2_pack(__int2float_rn(((dh0 & 255) << kFineBits) + (l0[d] - li[d])),
+                          __int2float_rn(((dh1 & 255) << kFineBits) + (l1[d] - li[d]))),
+                  fine);
+    if (ANISO) {
+      const f2 h = f2_splat(uh[d]), l = f2_splat(ul[d]);
+      const f2 m = f2_mul(a[d], h);
+      f2 t = f2_fms(a[d], h, m);
+      t = f2_fma(b[d], h, t);
+      t = f2_fma(a[d], l, t);
+      a[d] = m;
+      b[d] = t;
+    }
+    p[d] = f2_mul(a[d], a[d]);
+    e[d] = f2_fms(a[d], a[d], p[d]);
+    e[d] = f2_fma(f2_add(a[d], a[d]), b[d], e[d]);
+    e[d] = f2_fma(b[d], b[d], e[d]);
+  }
+  const ff2 s1 = ff2_two_sum(p[0], p[1]);
+  const ff2 s2 = ff2_two_sum(s1.h, p[2]);
+  const f2 lo = f2_add(f2_add(e[0], e[1]), f2_add(e[2], f2_add(s1.l, s2.l)));
+  S = f2_add(s2.h, lo);
+  s = f2_sub(lo, f2_sub(S, s2.h));
+}
+
+// pair_g_ff of two pairs (the reciprocal seeds are scalar MUFU operations).
+template <bool ANISO>
+__device__ __forceinline__ ff2 pair_g_ff2(f2 S, f2 s_lo, float kh, float kl) {
+  float S0, S1, y0, y1;
+  f2_unpack(S, S0, S1);
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(S0));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y1) : "f"(S1));
+  const f2 y = f2_pack(y0, y1);
+  f2 e = f2_nfma(S, y, f2_splat(1.0f));
+  e = f2_nfma(s_lo, y, e);
+  ff2 inv{y, f2_mul(y, e)};
+  if (!ANISO) inv = ff2_mul(inv, ff2{f2_splat(kh), f2_splat(kl)});
+  const ff2 i2 = ff2_sqr(inv);
+  const ff2 i6 = ff2_mul(i2, inv);
+  const f2 m2 = f2_splat(-2.0f);
+  const f2 m = f2_mul(m2, i6.h);
+  ff2 w = ff2_two_sum(f2_splat(1.0f), m);
+  w.l = f2_fma(m2, i6.l, w.l);
+  return ff2_mul(ff2_sqr(i2), w);
+}
+
+// term_parts of two pairs for one axis.
+__device__ __forceinline__ void term_parts2(ff2 g, f2 a, f2 b, f2& p, f2& e) {
+  p = f2_mul(g.h, a);
+  e = f2_fms(g.h, a, p);
+  e = f2_fma(g.h, b, e);
+  e = f2_fma(g.l, a, e);
+}
+
 }  // namespace ljg

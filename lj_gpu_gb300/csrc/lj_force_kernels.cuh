@@ -630,6 +630,59 @@ __device__ __forceinline__ float pair_term_ff(const int4& xi, const int (&li)[3]
   return S;
 }
 
+// pair_term_ff (in_mode 0) of two pairs, (i, j0) at slot u and (i, j1) at
+// slot u + 1, with packed instructions (lj_ff.cuh): each row sum receives the
+// term of u and then that of u + 1, bit for bit as two pair_term_ff calls.
+template <bool ANISO>
+__device__ __forceinline__ void pair_term_ff2(const int4& xi, const int (&li)[3], const int4& xj0,
+                                              const int4& xj1, const MixedConsts& K,
+                                              RowSums<true>& acc, bool ok0, bool ok1,
+                                              unsigned& border, int u) {
+  f2 a[3], b[3], S, s;
+  pair_sep_ff2<ANISO>(xi, li[0], li[1], li[2], xj0, xj1, K.u_hi, K.u_lo, a, b, S, s);
+  float S0, S1;
+  f2_unpack(S, S0, S1);
+  const bool in0 = ok0 && S0 <= K.cl2_lo, in1 = ok1 && S1 <= K.cl2_lo;
+  if (ok0 && S0 > K.cl2_lo && S0 <= K.cl2_hi) border |= 1u << u;
+  if (ok1 && S1 > K.cl2_lo && S1 <= K.cl2_hi) border |= 2u << u;
+  ff2 g = pair_g_ff2<ANISO>(S, s, K.k_hi, K.k_lo);
+  float gh0, gh1, gl0, gl1;
+  f2_unpack(g.h, gh0, gh1);
+  f2_unpack(g.l, gl0, gl1);
+  if (!in0) gh0 = gl0 = 0.f;
+  if (!in1) gh1 = gl1 = 0.f;
+  g = ff2{f2_pack(gh0, gh1), f2_pack(gl0, gl1)};
+  AccFF* axes[3] = {&acc.x, &acc.y, &acc.z};
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    f2 p, e;
+    term_parts2(g, a[d], b[d], p, e);
+    float p0, p1, e0, e1;
+    f2_unpack(p, p0, p1);
+    f2_unpack(e, e0, e1);
+    axes[d]->add_parts(p0, e0);
+    axes[d]->add_parts(p1, e1);
+  }
+}
+
+// The two-float terms (in_mode 0) of the U slots of one step, two at a time
+// with packed instructions (PK, U even) or one at a time.
+template <bool ANISO, bool PK, int U>
+__device__ __forceinline__ void step_terms_ff(const int4& xi, const int (&li)[3],
+                                              const int4 (&xj)[U], const bool (&ok)[U],
+                                              const MixedConsts& K, RowSums<true>& acc,
+                                              unsigned& border) {
+  static_assert(!PK || U % 2 == 0, "packed terms go in pairs");
+  if constexpr (PK) {
+#pragma unroll
+    for (int u = 0; u < U; u += 2)
+      pair_term_ff2<ANISO>(xi, li, xj[u], xj[u + 1], K, acc, ok[u], ok[u + 1], border, u);
+  } else {
+#pragma unroll
+    for (int u = 0; u < U; u++) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, ok[u], border, u);
+  }
+}
+
 template <int G, bool PBC, bool SOA, bool ANISO, bool FF = false>
 __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const Csr C,
                                                       const int4* __restrict__ qfix,
@@ -697,7 +750,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(const Particles P, const C
 // wavefronts they cost (a 32-lane scalar index load touches one line per row).
 // ELL (G = 1): the transposed list (entry_addr).
 template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC = false, bool FF = false,
-          bool ELL = false>
+          bool ELL = false, bool PK = (FF && !ELL && U % 2 == 0)>
 __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const Csr C,
                                                         const int4* __restrict__ qfix,
                                                         const MixedConsts K0) {
@@ -763,7 +816,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed_u(const Particles P, const
     unsigned border = 0u;
     if constexpr (FF) {
 #pragma unroll
-      for (int u = 0; u < U; u++) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, ok[u], border, u);
+      step_terms_ff<ANISO, PK, U>(xi, li, xj, ok, K, acc, border);
       if (__any_sync(kFullMask, border != 0u)) {
 #pragma unroll
         for (int u = 0; u < U; u++) {
@@ -1005,10 +1058,10 @@ __global__ void __launch_bounds__(256, 3) k_gather_mixed_seg(const Particles P, 
   // this one's)
   if (__any_sync(kFullMask, missed) && (threadIdx.x & 31) == 0) atomicExch(close_flag, 1);
   // ---- near part: two-float terms
-  walk_row<G, U, VEC>(C, i, valid, lane, qfix, [&](const int4* xj, const int* jj, const bool* ok) {
+  walk_row<G, U, VEC>(C, i, valid, lane, qfix, [&](const int4 (&xj)[U], const int* jj,
+                                                    const bool (&ok)[U]) {
     unsigned border = 0u;
-#pragma unroll
-    for (int u = 0; u < U; u++) pair_term_ff<ANISO>(xi, li, xj[u], K, acc, 0, ok[u], border, u);
+    step_terms_ff<ANISO, U % 2 == 0, U>(xi, li, xj, ok, K, acc, border);
     if (__any_sync(kFullMask, border != 0u)) {
 #pragma unroll
       for (int u = 0; u < U; u++)
@@ -1162,8 +1215,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
       return !beyond_cutoff(r2_fp64(d64), cl2_bits);
     };
     if constexpr (FF) {
-#pragma unroll
-      for (int u = 0; u < U; u++) pair_term_ff<false>(xi, li, xj[u], K, acc, 0, ok[u], border, u);
+      step_terms_ff<false, U % 2 == 0, U>(xi, li, xj, ok, K, acc, border);
       if (__any_sync(kFullMask, border != 0u)) {
 #pragma unroll
         for (int u = 0; u < U; u++) {
