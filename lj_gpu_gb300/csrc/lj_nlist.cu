@@ -152,8 +152,9 @@ enum RowMode { ROWS_FULL = 0, ROWS_HALF = 1, ROWS_LOCAL = 2, ROWS_SPLIT = 3 };
 struct BuildStage {
   float4 xr[kStage];      // position relative to the cell origin, particle index bits in w
   int4 xi[kStage];        // fixed-point image, particle index in w
-  unsigned bal[kStage];   // hits of staged particle t among the chunk's candidates
-  unsigned nbal[kStage];  // ROWS_SPLIT: the near ones among them
+  // staged particle t: x = its hits among the chunk's candidates, y (ROWS_SPLIT)
+  // the near ones among them; one 8-byte store per test
+  uint2 bal[kStage];
   int js[32];             // the chunk's candidates (particle index)
   int loc[32];            // and their 16-bit local indices (ROWS_LOCAL)
   int nb_start[32];       // first slot of each walk cell
@@ -292,11 +293,9 @@ __device__ __forceinline__ void build_cell_rows(int c, int cell_base, const Cell
           const bool hit = (MODE != ROWS_HALF || j > ws.xi[t].w) && r2 < k.sl2_hi;
           const unsigned bal = __ballot_sync(kFullMask, hit);
           if (EXACT) band |= hit && !(r2 < k.sl2_lo);
-          if (MODE == ROWS_SPLIT) {
-            const unsigned nbal = __ballot_sync(kFullMask, r2 < k.near2);
-            if (lane == 0) ws.nbal[t] = nbal;
-          }
-          if (lane == 0) ws.bal[t] = bal;
+          const unsigned nbal =
+              MODE == ROWS_SPLIT ? __ballot_sync(kFullMask, r2 < k.near2) : 0u;
+          if (lane == 0) ws.bal[t] = make_uint2(bal, nbal);
         }
         __syncwarp();
         if (EXACT && __any_sync(kFullMask, band)) {
@@ -307,7 +306,7 @@ __device__ __forceinline__ void build_cell_rows(int c, int cell_base, const Cell
               const int i = ws.xi[t].w;
               const bool hit = (MODE != ROWS_HALF || j > i) && r2 < k.sl2_hi;
               if (hit && !(r2 < k.sl2_lo) && !within_fp64(q, i, j, k))
-                atomicAnd(&ws.bal[t], ~(1u << lane));
+                atomicAnd(&ws.bal[t].x, ~(1u << lane));
             }
           }
           __syncwarp();
@@ -317,27 +316,36 @@ __device__ __forceinline__ void build_cell_rows(int c, int cell_base, const Cell
       else tests(std::false_type{});
       // this chunk's hits of staged particle t (particle i) onto its rows
       auto append = [&](int t, int i, int& len, int& len2) {
-        unsigned mine = ws.bal[t];
+        const uint2 bn = ws.bal[t];
+        unsigned mine = bn.x;
         if (MODE != ROWS_HALF) {  // a particle is its own candidate once
           const int d = self_pref + (a - s0) + t - base;
           if (d >= 0 && d < 32) mine &= ~(1u << d);
         }
-        const unsigned nearm = MODE == ROWS_SPLIT ? ws.nbal[t] : 0u;
+        const unsigned nearm = bn.y;
         const size_t rb = (size_t)(MODE == ROWS_LOCAL ? a + t : i) * (size_t)out.maxrow;
         const size_t rb2 = MODE == ROWS_SPLIT ? (size_t)i * (size_t)out.maxrow2 : 0;
-        while (mine) {
-          const int b = __ffs(mine) - 1;
-          mine &= mine - 1u;
-          if (MODE == ROWS_SPLIT && !((nearm >> b) & 1u)) {
-            if (len2 < out.maxrow2) out.rows2[rb2 + len2] = ws.js[b];
-            len2++;
-            continue;
-          }
+        // near hits, then far hits (ROWS_SPLIT), each in candidate order: two
+        // branch-free loops, so lanes whose hits differ in kind do not run
+        // both paths every iteration
+        unsigned mn = MODE == ROWS_SPLIT ? (mine & nearm) : mine;
+        while (mn) {
+          const int b = __ffs(mn) - 1;
+          mn &= mn - 1u;
           if (len < out.maxrow) {
             if (MODE == ROWS_LOCAL) out.lrows[rb + len] = (uint16_t)ws.loc[b];
             else out.rows[rb + len] = ws.js[b];
           }
           len++;
+        }
+        if (MODE == ROWS_SPLIT) {
+          unsigned mf = mine & ~nearm;
+          while (mf) {
+            const int b = __ffs(mf) - 1;
+            mf &= mf - 1u;
+            if (len2 < out.maxrow2) out.rows2[rb2 + len2] = ws.js[b];
+            len2++;
+          }
         }
       };
       if (lane < ni) append(lane, i0, len0, far0);
