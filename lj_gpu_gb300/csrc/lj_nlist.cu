@@ -37,8 +37,8 @@ __device__ __forceinline__ bool off_guard(const int32_t* guard) {
 
 // Grids are capped near one resident wave (152 SMs) and the kernels stride
 // over their work: a guarded launch whose flag is off then costs one short
-// wave of exiting blocks instead of one block per 256 particles.
-constexpr int kResidentBlocks = 152 * 12;     // 128-thread blocks (40 registers: 12 resident)
+// wave of exiting blocks instead of one block per 256 particles.  The row
+// builds take their cap from their own occupancy (one_wave).
 constexpr int kResidentBlocks256 = 152 * 8;   // 256-thread blocks
 
 __global__ void k_bin(const double* __restrict__ q, int n, CellGrid g, int32_t* __restrict__ cell,
@@ -474,6 +474,26 @@ __global__ void k_minmax(const double* __restrict__ q, int n, unsigned long long
   }
 }
 
+// Blocks of `kernel` that the whole GPU holds at once with `block` threads:
+// the grid of a grid-stride kernel that should run as exactly one wave (a
+// partial second wave would run its blocks at low occupancy after the
+// first).  Computed once per kernel instantiation (occupancy queries do not
+// touch a stream, so this is safe during stream capture).
+template <typename Kernel>
+int one_wave(Kernel kernel, int block) {
+  static const int blocks = [&] {
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 152;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, 0) != cudaSuccess ||
+        per < 1)
+      per = 1;
+    return sms * per;
+  }();
+  return blocks;
+}
+
 int grid_of(int64_t work, int block, int cap) {
   int64_t g = (work + block - 1) / block;
   if (g < 1) g = 1;
@@ -562,15 +582,17 @@ cudaError_t launch_build_rows(const BuildArgs& a, bool half, int maxrow, int32_t
                               const int32_t* guard) {
   if (a.n == 0) return cudaSuccess;
   const BuildConsts k = make_build_consts(a);
-  const int blocks = grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, kResidentBlocks);
   RowOut out{};
   out.rows = rows;
   out.cnt = cnt;
   out.maxrow = maxrow;
   out.overflow = overflow;
   auto go = [&](auto mode, auto aniso, auto exact) {
-    k_build_rows<decltype(mode)::value, decltype(aniso)::value, decltype(exact)::value>
-        <<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, out, guard);
+    const auto kfn =
+        k_build_rows<decltype(mode)::value, decltype(aniso)::value, decltype(exact)::value>;
+    const int blocks =
+        grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, one_wave(kfn, kBuildBlock));
+    kfn<<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, out, guard);
     return cudaGetLastError();
   };
   using H = std::integral_constant<int, ROWS_HALF>;
@@ -590,7 +612,8 @@ cudaError_t launch_build_rows_local(const BuildArgs& a, int maxrow, int maxc_shi
                                     cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   const BuildConsts k = make_build_consts(a);
-  const int blocks = grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, kResidentBlocks);
+  const int blocks = grid_of((int64_t)a.grid.ncells * 32, kBuildBlock,
+                             one_wave(k_build_rows<ROWS_LOCAL, false, false>, kBuildBlock));
   RowOut out{};
   out.lrows = rows;
   out.cnt = cnt;
@@ -608,7 +631,6 @@ cudaError_t launch_build_rows_split(const BuildArgs& a, int maxrow, int32_t* row
                                     int32_t* overflow, cudaStream_t s, const int32_t* guard) {
   if (a.n == 0) return cudaSuccess;
   const BuildConsts k = make_build_consts(a);
-  const int blocks = grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, kResidentBlocks);
   RowOut out{};
   out.rows = rows;
   out.cnt = cnt;
@@ -617,13 +639,14 @@ cudaError_t launch_build_rows_split(const BuildArgs& a, int maxrow, int32_t* row
   out.cnt2 = cnt2;
   out.maxrow2 = maxrow2;
   out.overflow = overflow;
-  if (a.aniso)
-    k_build_rows<ROWS_SPLIT, true, false>
-        <<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, out, guard);
-  else
-    k_build_rows<ROWS_SPLIT, false, false>
-        <<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, out, guard);
-  return cudaGetLastError();
+  auto go = [&](auto kfn) {
+    const int blocks =
+        grid_of((int64_t)a.grid.ncells * 32, kBuildBlock, one_wave(kfn, kBuildBlock));
+    kfn<<<blocks, kBuildBlock, 0, s>>>(a.q, a.grid, a.start, a.order, a.cq, k, out, guard);
+    return cudaGetLastError();
+  };
+  if (a.aniso) return go(k_build_rows<ROWS_SPLIT, true, false>);
+  return go(k_build_rows<ROWS_SPLIT, false, false>);
 }
 
 cudaError_t launch_compact_padded(const int32_t* cnt, const int32_t* rows, int maxrow,
@@ -650,7 +673,8 @@ cudaError_t launch_build_rows_batch(const double* q, const ReplicaInfo* reps,
                                     const int64_t* start, const int32_t* order, const int4* cq,
                                     int maxrow, int32_t* rows, int32_t* cnt, int32_t* overflow,
                                     cudaStream_t s, const int32_t* guard) {
-  const int blocks = grid_of((int64_t)ncells * 32, kBuildBlock, kResidentBlocks);
+  const int blocks =
+      grid_of((int64_t)ncells * 32, kBuildBlock, one_wave(k_build_rows_batch, kBuildBlock));
   k_build_rows_batch<<<blocks, kBuildBlock, 0, s>>>(q, reps, cell_rid, ncells, sl2, start, order,
                                                     cq, maxrow, rows, cnt, overflow, guard);
   return cudaGetLastError();
