@@ -134,3 +134,42 @@ def test_md_in_a_non_cubic_box(engine):
     d = out["mixed"][0][:, :3] - out["fp64"][0][:, :3]
     d -= box * np.round(d / box)
     assert np.abs(d).max() < 1e-5
+
+
+def test_loop_graph_and_chunk_graphs_agree_bit_for_bit(engine):
+    """The persistent WHILE-node loop and the host-launched chunk graphs run
+    the same captured steps: identical positions and momenta, the same
+    records (to the rounding of their atomic sums), and the stats say which
+    form ran.  kick_lanes = 4 (four lanes per row in the
+    two-float kick) sums in another order: within the mixed bars of the
+    default's momenta, and against the oracle's FP64 integrator."""
+    import torch
+    q, L = ol.init_fcc_periodic(6, 1.0, 0.05, seed=41)  # 864 particles
+    p = engine.init_momenta(q.shape[0], 1.0, seed=6)
+    rc, skin, dt, steps = 2.5, 0.3, 0.005, 60
+    out = {}
+    for name, kw in (("loop", {}), ("chunks", {"chunk_graphs": True}),
+                     ("lanes4", {"kick_lanes": 4})):
+        qd, pd = _dev(q), _dev(p)
+        prm = engine.make_md_params(dt, rc, skin, L, precision="mixed", record_every=20,
+                                    graph_steps=8, **kw)
+        with engine.Context(0) as ctx:
+            recs, stats = ctx.md_run(qd, pd, prm, steps)
+        torch.cuda.synchronize()
+        out[name] = (qd.cpu().numpy(), pd.cpu().numpy(), recs, stats)
+    assert out["loop"][3]["loop_graph"] == 1 and out["chunks"][3]["loop_graph"] == 0
+    assert np.array_equal(out["loop"][0], out["chunks"][0])
+    assert np.array_equal(out["loop"][1], out["chunks"][1])
+    # energy records are sums with atomics (their order varies run to run)
+    for a, b in zip(out["loop"][2], out["chunks"][2]):
+        assert a[0] == b[0] and abs(a[1] - b[1]) <= 1e-12 * abs(b[1])
+        assert abs(a[2] - b[2]) <= 1e-12 * abs(b[2])
+    assert out["loop"][3]["rebuilds"] == out["chunks"][3]["rebuilds"] >= 1
+    qo, po = oracle_vv(q, p, L, rc, dt, steps)
+    for name in ("loop", "lanes4"):
+        assert np.abs(periodic_diff(out[name][0], qo, L)).max() < 1e-7, name
+        assert ol.rel_errors(out[name][1], po)["max_rel_rms"] < 1e-6, name
+    assert ol.rel_errors(out["lanes4"][1], out["loop"][1])["max_rel_rms"] < 1e-7
+    with engine.Context(0) as ctx:
+        with pytest.raises(engine.LJError):
+            ctx.md_run(_dev(q), _dev(p), engine.make_md_params(dt, rc, skin, L, kick_lanes=3), 1)
