@@ -491,6 +491,20 @@ def run_ours(args, dist, density=DENSITY, ncell=NCELL):
     ctx2.close()
     t_image64_ms, t_pair64_ms = stage_times(best_fp64, max(3, min(args.steps, 20)))
 
+    # force error of the mixed default (and the FP64 scatter) against the
+    # oracle's FP64 force_sorted over the device-built half list
+    ferr = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_lib as ol
+        half = ctx.get_list_csr("half")
+        po = ol.force_sorted_aos(q, np.zeros_like(q), *half, cl2=RC * RC, dt=1.0, box=L)
+        ferr = {}
+        for prec in ("mixed", "fp64"):
+            pm = torch.zeros_like(qd)
+            ctx.force_aos(qd, pm, lj.make_opts(dt=1.0, cl2=RC * RC, box=L, precision=prec))
+            ferr[prec] = per_particle_errors(pm[:, :3].cpu().numpy(), po[:, :3])
+        ferr["reference"] = "oracle FP64 force_sorted, default launch shapes"
     # e2e: the reference's measure() through the C ABI with pinned host buffers
     e2e = None
     if args.e2e_steps > 0:
@@ -575,6 +589,7 @@ def run_ours(args, dist, density=DENSITY, ncell=NCELL):
                    "l2": "flushed before every timed call (512 MiB write)",
                    "list_build_s": t_build, "parallelism": f"replicas x{dist.world}"},
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64": fp64,
+        "force_error": ferr,
         "variants": dict({k: round(v["gpairs"], 3) for k, v in results.items()},
                          **{"mixed/gather/aos/shuffled_rows": round(shuffled, 3)}),
         "autotuned": tuned,
@@ -588,9 +603,11 @@ def run_ours(args, dist, density=DENSITY, ncell=NCELL):
 # ---------------------------------------------------------------------------
 # MD workloads
 # ---------------------------------------------------------------------------
-def force_errors(torch, lj, L, qd, rs=RS):
-    """Mixed vs FP64 forces of the engine on the same positions (the FP64 path
-    is held to 1e-12 of the oracle by the parity tests)."""
+def force_errors(torch, lj, L, qd, rs=RS, oracle=False):
+    """Mixed against FP64 forces on the same positions and device-built list:
+    the engine's FP64 path (held to 1e-12 of the oracle by the parity tests),
+    and with `oracle` also the oracle's FP64 gather on the host cores
+    (`vs_oracle`)."""
     ctx = lj.Context(qd.device.index or 0, stream=torch.cuda.current_stream())
     ctx.build_list(qd, rs, box=L)
     out = {}
@@ -603,10 +620,20 @@ def force_errors(torch, lj, L, qd, rs=RS):
     r = torch.linalg.norm(out["fp64"], dim=1)
     rms = torch.sqrt(torch.mean(r * r))
     per = d / r
+    res = {"max_rel": float(per.max()), "rms_rel": float(torch.sqrt(torch.mean(per * per))),
+           "max_rel_rms": float(d.max() / rms), "global_rel": float(torch.linalg.norm(d) /
+                                                                    torch.linalg.norm(r))}
+    if oracle:
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_lib as ol
+        npp, ptr_, lst = ctx.get_list_csr("full")
+        qh = qd.cpu().numpy()
+        po = np.zeros_like(qh)
+        ol.force_gather_aos(qh, po, npp, ptr_, lst, cl2=RC * RC, dt=1.0, box=L,
+                            threads=ol.oracle().lj_or_max_threads())
+        res["vs_oracle"] = per_particle_errors(out["mixed"].cpu().numpy(), po[:, :3])
     ctx.close()
-    return {"max_rel": float(per.max()), "rms_rel": float(torch.sqrt(torch.mean(per * per))),
-            "max_rel_rms": float(d.max() / rms), "global_rel": float(torch.linalg.norm(d) /
-                                                                     torch.linalg.norm(r))}
+    return res
 
 
 def md_step_bytes(P, N, rebuilds_per_step, mixed=True):
@@ -631,7 +658,7 @@ def run_precision(args, dist):
     N = q.shape[0]
     p = lj.init_momenta(N, 1.0, SEED + 1)
     qd, pd = torch.from_numpy(q).to(dev), torch.from_numpy(p).to(dev)
-    errors = [dict(step=0, **force_errors(torch, lj, L, qd))]
+    errors = [dict(step=0, **force_errors(torch, lj, L, qd, oracle=not args.no_cpu_baseline))]
     ctx = lj.Context(dist.local, stream=torch.cuda.current_stream())
     prm = lj.make_md_params(DT, RC, RS - RC, L, precision="mixed", record_every=100,
                             chunk_graphs=args.chunk_graphs)
@@ -643,7 +670,8 @@ def run_precision(args, dist):
         ms += st["ms_total"]
         rebuilds += st["rebuilds"]
         records += [(r[0] + 100 * seg, r[1], r[2]) for r in recs if seg == 0 or r[0] > 0]
-        errors.append(dict(step=100 * (seg + 1), **force_errors(torch, lj, L, qd)))
+        errors.append(dict(step=100 * (seg + 1),
+                           **force_errors(torch, lj, L, qd, oracle=not args.no_cpu_baseline)))
     e0 = records[0][1] + records[0][2]
     drift = max(abs(r[1] + r[2] - e0) for r in records) / abs(e0)
     ctx.build_list(qd, RS, box=L, kinds=("half",))
@@ -657,6 +685,9 @@ def run_precision(args, dist):
             "gpairs": P / (ms / 1000 * 1e-3) / 1e9,
             "hbm_gbs": sb / (ms / 1000 * 1e-3) / 1e9,
             "hbm_frac": sb / (ms / 1000 * 1e-3) / 1e9 / hbm,
+            "max_rel_force_error": max(e["max_rel"] for e in errors),
+            "max_rel_force_error_vs_oracle": max((e["vs_oracle"]["max_rel"] for e in errors
+                                                  if "vs_oracle" in e), default=None),
             "max_rel_rms_force_error": max(e["max_rel_rms"] for e in errors),
             "global_rel_force_error": max(e["global_rel"] for e in errors),
             "force_errors": errors, "energy_drift_rel": drift,
@@ -664,7 +695,8 @@ def run_precision(args, dist):
             "clocks": merge_clocks(clock_samples),
             "note": "the cut, unshifted potential (the reference's) jumps when pairs cross "
                     "rc, so total energy drifts in FP64 too; force errors are against the "
-                    "engine's FP64 path on the same positions"}
+                    "engine's FP64 path and (vs_oracle) the oracle's FP64 gather on the same "
+                    "positions and list"}
 
 
 def per_particle_errors(test, ref):
@@ -902,6 +934,32 @@ def run_batch(args, dist):
         a, b = offs[r], offs[r + 1]
         ctx.build_list(qd[a:b].contiguous(), 2.8, box=boxes[r], kinds=("half",))
         pairs += ctx.list_info("half")[1]
+    # force errors at the final positions of a sample of replicas (smallest,
+    # largest, the first of each density): the engine's mixed force against
+    # the oracle's FP64 force_sorted over the same list
+    sizes = np.diff(offs)
+    sample = sorted({int(np.argmin(sizes)), int(np.argmax(sizes))} |
+                    {next(r for r in range(512) if specs[r][1] == rho) for rho in (0.5, 0.8, 1.0)})
+    errors = None
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_lib as ol
+        worst = {"max_rel": 0.0, "rms_rel": 0.0, "max_rel_rms": 0.0}
+        for r in sample:
+            a, b = offs[r], offs[r + 1]
+            qr = qd[a:b].contiguous()
+            ctx.build_list(qr, 2.8, box=boxes[r], kinds=("half",))
+            half = ctx.get_list_csr("half")
+            pm = torch.zeros_like(qr)
+            ctx.force_aos(qr, pm, lj.make_opts(dt=1.0, cl2=2.5 * 2.5, box=boxes[r],
+                                                precision="mixed", method="gather"))
+            qh = qr.cpu().numpy()
+            po = ol.force_sorted_aos(qh, np.zeros_like(qh), *half, cl2=2.5 * 2.5, dt=1.0,
+                                     box=boxes[r][0])
+            e = per_particle_errors(pm[:, :3].cpu().numpy(), po[:, :3])
+            worst = {k: max(worst[k], e[k]) for k in worst}
+        errors = dict(worst, replicas=sample, reference="oracle FP64 force_sorted",
+                      positions="final batched MD state")
     ctx.close()
     e0 = en[0, :, 0] + en[0, :, 1]
     e1 = en[-1, :, 0] + en[-1, :, 1]
@@ -917,6 +975,7 @@ def run_batch(args, dist):
             "size_classes": [{"rows": int(s[0]), "lanes": int(s[1]), "entries_in_flight": int(s[2])}
                              for s in shapes if s[0] > 0],
             "energy_change_rel_max": float(np.max(np.abs(e1 - e0) / np.abs(e0))),
+            "force_error": errors,
             "clocks": cs.summary(),
             "note": "graph-captured step chunks with flag-guarded on-device rebuilds; per-class "
                     "gather shapes timed at start-up"}
