@@ -164,14 +164,16 @@ constexpr double kBandFF = 6e-7;    // two-float r2 rounded to float vs float ed
 // coarse units; the fine image's is kCoarseQuantumErr / 1024
 constexpr double kCoarseQuantumErr = 2.0;
 // Near/far split of the two-float gathers (lengths, sigma = 1): rows are
-// ordered near-first at r < kFarSplit (k_partition_near), and any pair found
-// closer than kFarCheck is evaluated in two-float arithmetic wherever it sits
-// in its row.  FP32 terms for every pair beyond 2.2 sigma keep the net force
-// of each particle within ~3e-6 (108,000 particles, rho 0.5) to ~1e-6 (8M,
-// rho 1) of FP64; the 0.3 sigma margin lets positions move that far (a Verlet
-// skin) before far terms fall back to two-float evaluation.
-constexpr double kFarSplit = 2.5;
-constexpr double kFarCheck = 2.2;
+// ordered near-first at r < kFarSplit (k_partition_near, or the MD build's
+// split rows), and any pair found closer than kFarCheck is evaluated in
+// two-float arithmetic wherever it sits in its row.  FP32 terms for every
+// pair beyond 2.0 sigma keep the net force of each particle within 2.4e-6
+// (108,000 particles, rho 0.5), 6.4e-7 (1M, rho 1, over 1,000 MD steps) and
+// 8.1e-7 (8M, rho 1) of FP64, against a bar of 1e-5; the 0.3 sigma margin
+// lets positions move that far (a Verlet skin) before far terms fall back to
+// two-float evaluation.
+constexpr double kFarSplit = 2.3;
+constexpr double kFarCheck = 2.0;
 
 // ---------------------------------------------------------------------------
 // Open-box frame chosen on the device.  A bounds pass (k_open_bounds) folds

@@ -972,7 +972,7 @@ __device__ __forceinline__ void walk_row(const Csr& C, int i, bool valid, int la
 // the MD build).  The far part runs first in FP32 terms from the coarse image
 // (the FP32 kernels' arithmetic and cutoff band) into compensated FP32 sums,
 // which then seed the two-float sums of the near part's two-float terms.  A
-// far entry closer than K.near2 (2.2 sigma) -- a pair that moved in since
+// far entry closer than K.near2 (2.0 sigma) -- a pair that moved in since
 // the rows were split -- is skipped there and raises close_flag[0], and
 // k_seg_close_terms then adds its two-float term, so the split decides the
 // speed, never the precision.

@@ -686,7 +686,7 @@ def test_kernel4_measure_uses_the_uploaded_list(engine, fixture_rho05, prec):
 @pytest.mark.parametrize("name", list(SYSTEMS))
 @pytest.mark.parametrize("kernel", [2, 4])
 def test_two_float_split_and_full_terms(engine, name, kernel):
-    """The two-float gather's near/far split (FP32 terms beyond 2.5 sigma,
+    """The two-float gather's near/far split (FP32 terms beyond 2.3 sigma,
     the default) and two-float terms for every pair (ff_all) both meet the
     per-particle bar; they differ only by the far terms' FP32 rounding."""
     q, box, half = system(name)
@@ -709,7 +709,7 @@ def test_split_order_from_other_positions_keeps_precision(engine):
     """The near-first order is made from the positions of the first call;
     later calls with particles moved by up to 0.45 sigma (past the 0.3 sigma
     margin) still meet the per-particle bar: pairs that came closer than
-    2.2 sigma are evaluated in two-float terms wherever they sit."""
+    2.0 sigma are evaluated in two-float terms wherever they sit."""
     q, box = ol.init_fcc_periodic(6, 1.0, 0.05, seed=20240601)
     rng = np.random.default_rng(8)
     q2 = q.copy()

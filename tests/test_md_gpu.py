@@ -82,12 +82,13 @@ def test_mixed_md_tracks_fp64_and_conserves(engine):
 
 def test_md_list_overflow_is_reported(engine):
     # 500 particles packed into a corner of a large box: the capacity estimate
-    # from the mean density is far too small, and the run must say so
+    # from the mean density is far too small (64 entries for ~150 partners
+    # within rc + skin = 3.3), and the run must say so
     q, _ = ol.init_fcc_periodic(5, 1.0, 0.05, seed=3)
     L = 40.0
     p = np.zeros_like(q)
     qd, pd = _dev(q), _dev(p)
-    prm = engine.make_md_params(0.005, 2.5, 0.3, L, precision="mixed")
+    prm = engine.make_md_params(0.005, 3.0, 0.3, L, precision="mixed")
     with engine.Context(0) as ctx:
         with pytest.raises(engine.LJError) as e:
             ctx.md_run(qd, pd, prm, 5)
