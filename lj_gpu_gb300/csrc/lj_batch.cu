@@ -6,7 +6,9 @@
 // step (lj_md.cu) runs once over the whole batch: drift, flag-guarded rebuild
 // (binning, cell offsets, placement, per-cell ordering, row build), and the
 // mixed gather, which is launched once per size class of rows with the launch
-// shape the class's own timing picked.  Steps between energy records are
+// shape the class's own timing picked.  Two-float kicks split every row into
+// a near part (two-float terms) and a far part (FP32 terms) when the skin
+// allows it (BatchState::split).  Steps between energy records are
 // replayed from a captured CUDA graph.
 #include <algorithm>
 #include <cmath>
@@ -83,13 +85,14 @@ __global__ void k_batch_set(int32_t* flags, int word, int value) {
   if (threadIdx.x == 0 && blockIdx.x == 0) flags[word] = value;
 }
 
-// Per-replica energies: kinetic (FP64) and potential over pairs j > i with
-// r2 <= rc^2 (FP32 from the image with Kahan sums; FP64 re-decision of the
-// cutoff band), each replica into its own pair of accumulators.
+// Per-replica energies: kinetic (FP64, when `kinetic`) and potential over
+// the pairs j > i of the rows of c with r2 <= rc^2 (FP32 from the image with
+// Kahan sums; FP64 re-decision of the cutoff band), each replica into its
+// own pair of accumulators.  Split rows take one launch per part.
 __global__ void __launch_bounds__(256) k_batch_energy(
     const double* __restrict__ q, const double* __restrict__ p, const int4* __restrict__ qfix,
     Csr c, const int32_t* __restrict__ rid, const ReplicaInfo* __restrict__ reps, double cl2,
-    double* __restrict__ out) {
+    double* __restrict__ out, bool kinetic) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.n) return;
   const int r = rid[i];
@@ -125,7 +128,7 @@ __global__ void __launch_bounds__(256) k_batch_energy(
     comp = (t - s) - y;
     s = t;
   }
-  atomicAdd(out + 2 * r, kin);
+  if (kinetic) atomicAdd(out + 2 * r, kin);
   const double u = (double)s - (double)comp;
   if (u != 0.0) atomicAdd(out + 2 * r + 1, u);
 }
@@ -141,8 +144,12 @@ void split(double v, float& hi, float& lo) {
 
 struct BatchState {
   int n = 0, R = 0, ncells = 0, maxrow = 0;
+  // split rows (two-float kicks with skin <= kFarSplit - kFarCheck): rows /
+  // cnt hold every row's near part, rows2 / cnt2 its far part (maxrow each)
+  bool split = false;
   DevBuf<ReplicaInfo> reps;
   DevBuf<int32_t> rid, cell_rid, flags, cell, count, cursor, order, order2, cnt, rows, classrows;
+  DevBuf<int32_t> rows2, cnt2;
   DevBuf<int4> qfix, qref, cq, cq2;
   DevBuf<int64_t> start;
   DevBuf<unsigned char> scan_tmp;
@@ -191,7 +198,9 @@ cudaError_t batch_rebuild(BatchState& b, const double* q, double sl2, cudaStream
     return e;
   if ((e = launch_build_rows_batch(q, b.reps.ptr, b.cell_rid.ptr, b.ncells, sl2, b.start.ptr,
                                    b.order2.ptr, b.cq2.ptr, b.maxrow, b.rows.ptr, b.cnt.ptr,
-                                   b.flags.ptr + B_OVERFLOW, s, g)))
+                                   b.split ? b.rows2.ptr : nullptr,
+                                   b.split ? b.cnt2.ptr : nullptr, b.flags.ptr + B_OVERFLOW, s,
+                                   g)))
     return e;
   k_batch_copy_ref<<<std::min(gridn(b.n, 256), 152 * 8), 256, 0, s>>>(b.qfix.ptr, b.qref.ptr, b.n, b.flags.ptr);
   k_batch_finish<<<1, 32, 0, s>>>(b.flags.ptr);
@@ -201,10 +210,11 @@ cudaError_t batch_rebuild(BatchState& b, const double* q, double sl2, cudaStream
 cudaError_t batch_kick(BatchState& b, const Particles& part, const std::vector<SizeClass>& cls,
                        double dt, double cl2, bool ff, cudaStream_t s) {
   const Csr c{b.n, 0, b.cnt.ptr, nullptr, b.rows.ptr, (int64_t)b.maxrow, 1};
+  const Csr far{b.n, 0, b.cnt2.ptr, nullptr, b.rows2.ptr, (int64_t)b.maxrow, 1};
   for (const SizeClass& k : cls) {
     cudaError_t e = launch_force_batch(part, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                        b.classrows.ptr + k.first, k.count, dt, cl2, k.lanes,
-                                       k.unroll, k.vec, ff, s);
+                                       k.unroll, k.vec, ff, s, b.split ? &far : nullptr);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -294,6 +304,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     I.cl2f_hi = (float)(cl2u * (1 + bf));
     I.sl2u_lo = (float)(sl2u * (1 - bs));
     I.sl2u_hi = (float)(sl2u * (1 + bs));
+    I.near2u = (float)(kFarSplit * kFarSplit / u2);
     I.unit = u;
     I.cell_base = ncells;
     I.offset = off;
@@ -333,6 +344,13 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
   B_CUDA(ctx, b.order2.ensure((size_t)n_total), "alloc");
   B_CUDA(ctx, b.cnt.ensure((size_t)n_total), "alloc");
   B_CUDA(ctx, b.rows.ensure((size_t)n_total * b.maxrow), "alloc");
+  // two-float kicks split the rows when no far pair can come inside
+  // kFarCheck before the next rebuild (pairs approach by at most the skin)
+  b.split = ff && !prm->ff_all && prm->skin <= kFarSplit - kFarCheck + 1e-12;
+  if (b.split) {
+    B_CUDA(ctx, b.rows2.ensure((size_t)n_total * b.maxrow), "alloc");
+    B_CUDA(ctx, b.cnt2.ensure((size_t)n_total), "alloc");
+  }
   B_CUDA(ctx, b.qfix.ensure((size_t)n_total), "alloc");
   B_CUDA(ctx, b.qref.ensure((size_t)n_total), "alloc");
   B_CUDA(ctx, b.cq.ensure((size_t)n_total), "alloc");
@@ -376,6 +394,8 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     Particles tp = part;
     tp.p = b.ptmp.ptr;
     const Csr c{b.n, 0, b.cnt.ptr, nullptr, b.rows.ptr, (int64_t)b.maxrow, 1};
+    const Csr far{b.n, 0, b.cnt2.ptr, nullptr, b.rows2.ptr, (int64_t)b.maxrow, 1};
+    const Csr* fp = b.split ? &far : nullptr;
     cudaEvent_t e0, e1;
     B_CUDA(ctx, cudaEventCreate(&e0), "event");
     B_CUDA(ctx, cudaEventCreate(&e1), "event");
@@ -388,12 +408,12 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
       for (const auto& sh : shapes) {
         cudaError_t e = launch_force_batch(tp, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                            b.classrows.ptr + k.first, k.count, prm->dt, cl2,
-                                           sh[0], sh[1], sh[2] != 0, ff, s);
+                                           sh[0], sh[1], sh[2] != 0, ff, s, fp);
         cudaEventRecord(e0, s);
         for (int rep = 0; rep < 3 && e == cudaSuccess; rep++)
           e = launch_force_batch(tp, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                  b.classrows.ptr + k.first, k.count, prm->dt, cl2, sh[0], sh[1],
-                                 sh[2] != 0, ff, s);
+                                 sh[2] != 0, ff, s, fp);
         cudaEventRecord(e1, s);
         if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
           cudaEventDestroy(e0);
@@ -438,7 +458,12 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     B_CUDA(ctx, cudaMemsetAsync(b.energy.ptr, 0, 2 * sizeof(double) * R, s), "memset");
     const Csr c{b.n, 0, b.cnt.ptr, nullptr, b.rows.ptr, (int64_t)b.maxrow, 1};
     k_batch_energy<<<gridn(n_total, 256), 256, 0, s>>>(q, p, b.qfix.ptr, c, b.rid.ptr, b.reps.ptr,
-                                                      cl2, b.energy.ptr);
+                                                      cl2, b.energy.ptr, true);
+    if (b.split) {
+      const Csr far{b.n, 0, b.cnt2.ptr, nullptr, b.rows2.ptr, (int64_t)b.maxrow, 1};
+      k_batch_energy<<<gridn(n_total, 256), 256, 0, s>>>(q, p, b.qfix.ptr, far, b.rid.ptr,
+                                                        b.reps.ptr, cl2, b.energy.ptr, false);
+    }
     B_CUDA(ctx, cudaGetLastError(), "energy");
     B_CUDA(ctx, cudaMemcpyAsync(energies + (size_t)nrec * 2 * R, b.energy.ptr,
                                 2 * sizeof(double) * R, cudaMemcpyDeviceToHost, s), "energy");

@@ -39,7 +39,8 @@ cudaError_t launch_force_tiled(const ForceLaunch& L, const TiledList& T, const i
 cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* qfix,
                                const int32_t* rid, const ReplicaInfo* reps,
                                const int32_t* rows, int nrows, double dt, double cl2, int lanes,
-                               int unroll, bool vec, bool ff, cudaStream_t s) {
+                               int unroll, bool vec, bool ff, cudaStream_t s, const Csr* far) {
+  if (far && (!ff || (vec && (far->ptr || far->stride % 4 != 0)))) return cudaErrorInvalidValue;
   if (vec && (unroll != 4 || c.ptr || c.stride % 4 != 0)) return cudaErrorInvalidValue;
   if (nrows <= 0) return cudaSuccess;
   long long cl2_bits;
@@ -52,6 +53,15 @@ cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* 
       constexpr int G = decltype(g)::value;
       auto run = [&](auto F) {
         constexpr bool FF = decltype(F)::value;
+        if (far) {  // split rows: far part in FP32 terms, near part in two-float terms
+          if (U == 4 && vec)
+            k_gather_mixed_batch_seg<G, 4, true><<<blocks, block, 0, s>>>(
+                part, c, *far, qfix, rid, reps, rows, nrows, dt, cl2_bits);
+          else
+            k_gather_mixed_batch_seg<G, U, false><<<blocks, block, 0, s>>>(
+                part, c, *far, qfix, rid, reps, rows, nrows, dt, cl2_bits);
+          return;
+        }
         if (U == 4 && vec)
           k_gather_mixed_batch<G, 4, true, FF>
               <<<blocks, block, 0, s>>>(part, c, qfix, rid, reps, rows, nrows, dt, cl2_bits);

@@ -1267,6 +1267,123 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
   kick_group<false, G, FF>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, fs, 0);
 }
 
+// Batched segment gather over the split rows of the replica batch: as
+// k_gather_mixed_seg, with the row's replica constants, over the rows of one
+// size class.  The far part (F) runs first in FP32 terms, whose compensated
+// sums seed the two-float sums of the near part (C).  The batch splits its
+// rows only when the skin is at most kFarSplit - kFarCheck: a rebuild comes
+// before any particle moves more than skin / 2, so no far pair comes inside
+// kFarCheck before the next rebuild and every far entry takes its FP32 term.
+template <int G, int U, bool VEC>
+__global__ void __launch_bounds__(256, 3) k_gather_mixed_batch_seg(
+    const Particles P, const Csr C, const Csr F, const int4* __restrict__ qfix,
+    const int32_t* __restrict__ rid, const ReplicaInfo* __restrict__ reps,
+    const int32_t* __restrict__ rows, int nrows, double dt, long long cl2_bits) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int g = t / G;
+  const int lane = t & (G - 1);
+  const bool valid = g < nrows;
+  int i = 0, r = 0;
+  int4 xi = make_int4(0, 0, 0, 0);
+  MixedConsts K{};
+  if (valid) {
+    i = __ldg(rows + g);
+    xi = __ldg(qfix + i);
+    r = __ldg(rid + i);
+    const ReplicaInfo& R = reps[r];
+    K.k_hi = R.k_hi;
+    K.k_lo = R.k_lo;
+    K.cl2_lo = R.cl2f_lo;  // two-float terms
+    K.cl2_hi = R.cl2f_hi;
+    K.cl2s_lo = R.cl2u_lo;  // FP32 terms
+    K.cl2s_hi = R.cl2u_hi;
+  }
+  int li[3];
+  image_lo(xi.w, li[0], li[1], li[2]);
+  // the rare FP64 cutoff decision (replica constants read here)
+  auto inside_fp64 = [&](int j) {
+    const ReplicaInfo& R = reps[r];
+    Fp64Consts f64{};
+    f64.cl2_bits = cl2_bits;
+    for (int d = 0; d < 3; d++) {
+      f64.len[d] = R.len[d];
+      f64.half_bits[d] = R.half_bits[d];
+    }
+    const double3 d64 = sep_fp64<true>(load_q<false>(P, i), load_q<false>(P, j), f64);
+    return !beyond_cutoff(r2_fp64(d64), cl2_bits);
+  };
+  // ---- far part: FP32 terms
+  RowSums<true> acc;
+  {
+    RowSums<false> acc32;
+    acc32.init();
+    walk_row<G, U, VEC>(F, i, valid, lane, qfix, [&](const int4* xj, const int* jj,
+                                                     const bool* ok) {
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      unsigned border = 0u;
+      float3 d[U];
+      float r2[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        d[u] = sep_mixed<false>(xi, xj[u], K);
+        r2[u] = fmaf(d[u].z, d[u].z, fmaf(d[u].y, d[u].y, d[u].x * d[u].x));
+        const bool in = ok[u] && r2[u] <= K.cl2s_lo;
+        if (ok[u] && r2[u] > K.cl2s_lo && r2[u] <= K.cl2s_hi) border |= 1u << u;
+        float df = df_mixed<false>(r2[u], K);
+        df = in ? df : 0.0f;
+        sx = fmaf(df, d[u].x, sx);
+        sy = fmaf(df, d[u].y, sy);
+        sz = fmaf(df, d[u].z, sz);
+      }
+      if (__any_sync(kFullMask, border != 0u)) {
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          if (!(border & (1u << u)) || !inside_fp64(jj[u])) continue;
+          const float df = df_mixed<false>(r2[u], K);
+          sx = fmaf(df, d[u].x, sx);
+          sy = fmaf(df, d[u].y, sy);
+          sz = fmaf(df, d[u].z, sz);
+        }
+      }
+      acc32.x.add(sx);
+      acc32.y.add(sy);
+      acc32.z.add(sz);
+    });
+    // FP32 terms carry the 24 of df; the two-float sums and kick do not
+    float h[6];
+    acc32.get(h[0], h[1], h[2], h[3], h[4], h[5]);
+    const float r24 = 0.041666668f;
+    acc.x.hi = __fmul_rn(h[0], r24);
+    acc.x.lo = __fmul_rn(h[1], r24);
+    acc.y.hi = __fmul_rn(h[2], r24);
+    acc.y.lo = __fmul_rn(h[3], r24);
+    acc.z.hi = __fmul_rn(h[4], r24);
+    acc.z.lo = __fmul_rn(h[5], r24);
+  }
+  // ---- near part: two-float terms
+  walk_row<G, U, VEC>(C, i, valid, lane, qfix, [&](const int4 (&xj)[U], const int* jj,
+                                                   const bool (&ok)[U]) {
+    unsigned border = 0u;
+    step_terms_ff<false, U % 2 == 0, U>(xi, li, xj, ok, K, acc, border);
+    if (__any_sync(kFullMask, border != 0u)) {
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if ((border & (1u << u)) && inside_fp64(jj[u]))
+          pair_term_ff<false>(xi, li, xj[u], K, acc, 1, true, border, u);
+    }
+  });
+  float hx, lx, hy, ly, hz, lz;
+  acc.get(hx, lx, hy, ly, hz, lz);
+  if (G > 1) {
+    group_reduce_comp<G>(hx, lx);
+    group_reduce_comp<G>(hy, ly);
+    group_reduce_comp<G>(hz, lz);
+  }
+  const double kf = valid ? reps[r].unit * dt * 24.0 : 0.0;
+  const double fs[3] = {kf, kf, kf};
+  kick_group<false, G, true>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, fs, 0);
+}
+
 // Cell-tiled mixed gather (kernel 3).  One CTA per cell: it copies the
 // fixed-point positions of its (up to 27) neighbour cells -- contiguous runs of
 // the cell-ordered image -- into shared memory, then walks the rows of its

@@ -397,12 +397,15 @@ __global__ void k_bin_batch(const double* __restrict__ q, int n, const int32_t* 
 
 // Batched row build (full rows): as k_build_rows, with the cell's replica
 // supplying the local grid and the membership constants.
+// SPLIT: rows in a near and a far part (ROWS_SPLIT) at the replica's near2u.
+template <bool SPLIT>
 __global__ void __launch_bounds__(kBuildBlock) k_build_rows_batch(
     const double* __restrict__ q, const ReplicaInfo* __restrict__ reps,
     const int32_t* __restrict__ cell_rid, int ncells, double sl2,
     const int64_t* __restrict__ start, const int32_t* __restrict__ order,
     const int4* __restrict__ cq, int maxrow, int32_t* __restrict__ rows,
-    int32_t* __restrict__ cnt, int32_t* __restrict__ overflow, const int32_t* guard) {
+    int32_t* __restrict__ cnt, int32_t* __restrict__ rows2, int32_t* __restrict__ cnt2,
+    int32_t* __restrict__ overflow, const int32_t* guard) {
   if (off_guard(guard)) return;
   __shared__ BuildStage stage[kBuildWarps];
   const int lane = threadIdx.x & 31;
@@ -423,13 +426,18 @@ __global__ void __launch_bounds__(kBuildBlock) k_build_rows_batch(
       k.half_bits[d] = R.half_bits[d];
     }
     k.sl2 = sl2;
+    k.near2 = R.near2u;
     RowOut out{};
     out.rows = rows;
     out.cnt = cnt;
     out.maxrow = maxrow;
+    out.rows2 = rows2;
+    out.cnt2 = cnt2;
+    out.maxrow2 = maxrow;
     out.overflow = overflow;
-    build_cell_rows<ROWS_FULL, false, false>(c - R.cell_base, R.cell_base, g, start, order, cq,
-                                             q, k, out, stage[threadIdx.x >> 5], lane);
+    build_cell_rows<SPLIT ? ROWS_SPLIT : ROWS_FULL, false, false>(
+        c - R.cell_base, R.cell_base, g, start, order, cq, q, k, out, stage[threadIdx.x >> 5],
+        lane);
   }
 }
 
@@ -671,13 +679,16 @@ cudaError_t launch_bin_batch(const double* q, int n, const int32_t* rid, const R
 cudaError_t launch_build_rows_batch(const double* q, const ReplicaInfo* reps,
                                     const int32_t* cell_rid, int ncells, double sl2,
                                     const int64_t* start, const int32_t* order, const int4* cq,
-                                    int maxrow, int32_t* rows, int32_t* cnt, int32_t* overflow,
-                                    cudaStream_t s, const int32_t* guard) {
-  const int blocks =
-      grid_of((int64_t)ncells * 32, kBuildBlock, one_wave(k_build_rows_batch, kBuildBlock));
-  k_build_rows_batch<<<blocks, kBuildBlock, 0, s>>>(q, reps, cell_rid, ncells, sl2, start, order,
-                                                    cq, maxrow, rows, cnt, overflow, guard);
-  return cudaGetLastError();
+                                    int maxrow, int32_t* rows, int32_t* cnt, int32_t* rows2,
+                                    int32_t* cnt2, int32_t* overflow, cudaStream_t s,
+                                    const int32_t* guard) {
+  auto go = [&](auto kfn) {
+    const int blocks = grid_of((int64_t)ncells * 32, kBuildBlock, one_wave(kfn, kBuildBlock));
+    kfn<<<blocks, kBuildBlock, 0, s>>>(q, reps, cell_rid, ncells, sl2, start, order, cq, maxrow,
+                                       rows, cnt, rows2, cnt2, overflow, guard);
+    return cudaGetLastError();
+  };
+  return rows2 ? go(k_build_rows_batch<true>) : go(k_build_rows_batch<false>);
 }
 
 }  // namespace ljg

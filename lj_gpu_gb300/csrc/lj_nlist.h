@@ -75,10 +75,13 @@ cudaError_t launch_compact_padded(const int32_t* cnt, const int32_t* rows, int m
 cudaError_t launch_bin_batch(const double* q, int n, const int32_t* rid, const ReplicaInfo* reps,
                              int ncells, int32_t* cell, int32_t* count, cudaStream_t s,
                              const int32_t* guard = nullptr);
+// rows2 / cnt2 (optional, each part maxrow wide): rows in a near part (r2 at
+// the build below each replica's near2u, into rows / cnt) and a far part.
 cudaError_t launch_build_rows_batch(const double* q, const ReplicaInfo* reps,
                                     const int32_t* cell_rid, int ncells, double sl2,
                                     const int64_t* start, const int32_t* order, const int4* cq,
-                                    int maxrow, int32_t* rows, int32_t* cnt, int32_t* overflow,
-                                    cudaStream_t s, const int32_t* guard = nullptr);
+                                    int maxrow, int32_t* rows, int32_t* cnt, int32_t* rows2,
+                                    int32_t* cnt2, int32_t* overflow, cudaStream_t s,
+                                    const int32_t* guard = nullptr);
 
 }  // namespace ljg
