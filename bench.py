@@ -500,10 +500,10 @@ def run_ours(args, dist, density=DENSITY, ncell=NCELL):
         half = ctx.get_list_csr("half")
         po = ol.force_sorted_aos(q, np.zeros_like(q), *half, cl2=RC * RC, dt=1.0, box=L)
         ferr = {}
-        for prec in ("mixed", "fp64"):
+        for fprec in ("mixed", "fp64"):
             pm = torch.zeros_like(qd)
-            ctx.force_aos(qd, pm, lj.make_opts(dt=1.0, cl2=RC * RC, box=L, precision=prec))
-            ferr[prec] = per_particle_errors(pm[:, :3].cpu().numpy(), po[:, :3])
+            ctx.force_aos(qd, pm, lj.make_opts(dt=1.0, cl2=RC * RC, box=L, precision=fprec))
+            ferr[fprec] = per_particle_errors(pm[:, :3].cpu().numpy(), po[:, :3])
         ferr["reference"] = "oracle FP64 force_sorted, default launch shapes"
     # e2e: the reference's measure() through the C ABI with pinned host buffers
     e2e = None
@@ -518,17 +518,18 @@ def run_ours(args, dist, density=DENSITY, ncell=NCELL):
         opts = lj.make_opts(dt=DT, cl2=RC * RC, box=L, precision=prec, method=method)
         ctx.measure_aos(hq, hp, opts, calls=100)  # warm-up
         dist.barrier()
-        tot = 0.0
+        tot = calc = 0.0
         for _ in range(args.e2e_steps):
-            ms_total, _ = ctx.measure_aos(hq, hp, opts, calls=100)
+            ms_total, ms_calc = ctx.measure_aos(hq, hp, opts, calls=100)
             tot += ms_total
+            calc += ms_calc
         dist.barrier()
         t_step = dist.max(tot / args.e2e_steps / 1e3, dev)
         h2d = hq.numel() * 8 * 2 + (h_np.numel() + h_ptr.numel() + h_lst.numel()) * 4
         e2e = {"value": dist.world * P * 100 / t_step / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(hp.numel() * 8),
                "step": "lj_measure_aos: H2D q,p,CSR + 100 force calls + D2H p",
-               "ms_per_step": t_step * 1e3}
+               "ms_per_step": t_step * 1e3, "force_calls_ms": calc / args.e2e_steps}
 
     hbm, peak_kind = peaks()
     alg = pair_kernel_bytes(method, layout, P, N)
