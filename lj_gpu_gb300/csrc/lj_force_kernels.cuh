@@ -981,14 +981,18 @@ __global__ void __launch_bounds__(256, 3) k_gather_mixed_seg(const Particles P, 
                                                           const Csr F,
                                                           const int4* __restrict__ qfix,
                                                           const MixedConsts K0,
-                                                          int32_t* close_flag) {
+                                                          int32_t* close_flag,
+                                                          const int32_t* __restrict__ rowperm) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = t / G;
+  const int row = t / G;
   const int lane = t & (G - 1);
   // launched as a programmatic dependent of the image pass
   asm volatile("griddepcontrol.wait;" ::: "memory");
   const MixedConsts K = PBC ? K0 : frame_consts(K0);
-  const bool valid = i < C.n;
+  const bool valid = row < C.n;
+  // rows visited in `rowperm` order when given (the MD loop passes the cell
+  // order of its last build, so a warp's rows stay neighbours in space)
+  const int i = valid && rowperm ? __ldg(rowperm + row) : row;
   const int4 xi = valid ? __ldg(qfix + i) : make_int4(0, 0, 0, 0);
   int li[3];
   image_lo(xi.w, li[0], li[1], li[2]);

@@ -20,10 +20,12 @@ cudaError_t launch_mixed_ff_split(const ForceLaunch& L, const MixedConsts& K, cu
         cudaError_t e;
         if (L.aniso)
           e = launch_dependent(k_gather_mixed_seg<G, U, P.value, S.value, true, V>, blocks,
-                               block, s, L.part, L.csr, L.far, L.qfix, K, L.close_flag);
+                               block, s, L.part, L.csr, L.far, L.qfix, K, L.close_flag,
+                               L.rowperm);
         else
           e = launch_dependent(k_gather_mixed_seg<G, U, P.value, S.value, false, V>, blocks,
-                               block, s, L.part, L.csr, L.far, L.qfix, K, L.close_flag);
+                               block, s, L.part, L.csr, L.far, L.qfix, K, L.close_flag,
+                               L.rowperm);
         if (e != cudaSuccess) return e;
         // far entries that came inside 2.0 sigma (a no-op unless the flag is up)
         const int cb = (int)std::min<long long>(((long long)n * G + 255) / 256, 152 * 4);

@@ -109,6 +109,9 @@ struct ForceLaunch {
   Csr far;
   // two device words, zero between calls (k_seg_close_terms clears them)
   int32_t* close_flag;
+  // split rows: the order in which the segment gather visits them (nullptr:
+  // row order); the MD loop passes the cell order of its last build
+  const int32_t* rowperm;
   // mixed precision only
   int4* qfix;      // n entries, written by the fixed-image pass
   float* fscratch; // 4 n floats, one float4 per particle (scatter-half mixed only)

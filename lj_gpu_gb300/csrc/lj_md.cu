@@ -394,7 +394,13 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   K.csr = mixed ? Csr{n, m.cap, m.cnt.ptr, nullptr, m.rows.ptr, (int64_t)m.maxrow, 1}
                 : Csr{n, m.cap, m.cnt.ptr, m.ptr.ptr, m.list.ptr, 0, 0};
   K.split = m.split ? 1 : 0;
-  if (m.split) K.far = Csr{n, m.cap2, m.cnt2.ptr, nullptr, m.rows2.ptr, (int64_t)m.maxrow_far, 1};
+  if (m.split) {
+    K.far = Csr{n, m.cap2, m.cnt2.ptr, nullptr, m.rows2.ptr, (int64_t)m.maxrow_far, 1};
+    // rows visited in the cell order of the last build (k_sort_cells' slot
+    // order): a warp's rows stay neighbours in space however far the
+    // particles have moved from their initial order
+    K.rowperm = m.order2.ptr;
+  }
   K.close_flag = m.flags.ptr + F_CLOSE;
   K.box.on = 1;
   for (int d = 0; d < 3; d++) {
