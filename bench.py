@@ -850,16 +850,25 @@ def run_md8m(args, dist):
                 "traffic_source": (f"profiles/{prof}, scaled by list entries from the 1,000,188-"
                                    "particle capture") if traffic else None,
                 "peak_kind": peak_kind,
-                "kernel": "k_gather_mixed_seg (FP32 far part, two-float near part; 4 lanes per "
-                          "row, 4 entries in flight), timed in force calls at the final MD "
+                "kernel": "k_gather_mixed_seg (FP32 far part, two-float near part; one lane "
+                          "per row, 4 entries in flight), timed in force calls at the final MD "
                           "positions",
                 "algorithmic_bytes_per_launch": alg, "kernel_ms": mx["pair_ms"],
                 "position_image_ms": mx["image_ms"],
                 "md_step_bytes": md_step_bytes(P, N, 1 / REBUILD_8M),
                 "md_step_frac": md_step_bytes(P, N, 1 / REBUILD_8M) / mx["t_step"] / 1e9 / hbm}
-    iss = profiled_metric(prof, "smsp__issue_active.avg.pct_of_peak_sustained_active")
-    if iss is not None:
-        roofline["issue_active_frac"] = iss / 100
+    # what bounds the kernel instead of HBM, from the same capture: issue, the
+    # ALU pipe and the L1 data pipe
+    for key, metric in (("issue_active_frac", "smsp__issue_active.avg.pct_of_peak_sustained_active"),
+                        ("alu_pipe_frac", "sm__pipe_alu_cycles_active.avg.pct_of_peak_sustained_active"),
+                        ("fma_pipe_frac", "sm__pipe_fma_cycles_active.avg.pct_of_peak_sustained_active"),
+                        ("l1_data_pipe_frac",
+                         "l1tex__data_pipe_lsu_wavefronts.avg.pct_of_peak_sustained_elapsed")):
+        v = profiled_metric(prof, metric)
+        if v is not None:
+            roofline[key] = v / 100
+    roofline["limiter"] = ("instruction issue and the ALU and L1 data pipes (two-float pair "
+                           "terms); HBM is not the bound")
     fp_prof = "force_fp64_scatter_md_1m.txt"
     fp_pipe = profiled_metric(fp_prof, "sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active")
     fp64 = {"value": dist.world * fp["P"] / fp["t_step"] / 1e9, "ms_per_step": fp["t_step"] * 1e3,

@@ -606,6 +606,15 @@ def test_autotune_layouts_and_cache(engine, prec, tmp_path):
         assert getattr(second["opts"], f) == getattr(first["opts"], f), f
     lines = cache.read_text().splitlines()
     assert len(lines) == 1 and lines[0].startswith(first["key"] + " ")
+    # another density is another key: timed, and appended to the same file
+    q2, box2, half2 = system("pbc_rho0.5")
+    with engine.Context(0) as ctx:
+        ctx.set_list_csr(dev(half2[0]), dev(half2[1]), dev(half2[2]))
+        r = ctx.autotune_layouts(dev(q2), engine.make_opts(dt=0.005, cl2=9.0, box=box2,
+                                                           precision=prec),
+                                 reps=1, layouts=("aos", "soa", "z"), cache=cache)
+    assert r["key"] != first["key"] and not r["from_cache"] and r["timed"] > 3
+    assert len(cache.read_text().splitlines()) == 2
 
 
 @pytest.mark.parametrize("name", list(SYSTEMS))
