@@ -534,12 +534,12 @@ def run_ours(args, dist, density=DENSITY, ncell=NCELL):
     hbm, peak_kind = peaks()
     alg = pair_kernel_bytes(method, layout, P, N)
     achieved = alg / (t_pair_ms * 1e-3) / 1e9
-    # DRAM traffic per launch from the committed ncu capture of this kernel on
-    # this workload (the AoS and SoA gathers at rho 0.5); other workloads and
-    # kernels have none
+    # DRAM traffic per launch from a committed ncu capture of this kernel on
+    # this workload: the 108,000-particle captures under profiles/ are of the
+    # FP32-term gather (LJ_PREC_MIXED_FP32), not of the two-float default
+    # timed here, so this line carries none
     prof = f"force_mixed_gather_{layout}_108k_rho0.5.txt"
-    matches = density == DENSITY and method == "gather"
-    traffic = profiled_traffic(prof) if matches else None
+    traffic = None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
                 "traffic_source": f"profiles/{prof}" if traffic else None,
@@ -581,7 +581,7 @@ def run_ours(args, dist, density=DENSITY, ncell=NCELL):
         "metric": METRIC, "value": dist.world * P / head["s_per_call"] / 1e9, "unit": UNIT,
         "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": head["s_per_call"] * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math, f64 q/p",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 two-float pair math, f64 q/p",
         "data": "synthetic",
         "config": {"workload": WORKLOAD.replace("rho=0.5", f"rho={density}").replace(
                        "L=60", f"L={L:.4g}"), "N": N, "pairs_half": P, "pairs_full": P_full,
