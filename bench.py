@@ -856,6 +856,7 @@ def run_md8m(args, dist):
                 "algorithmic_bytes_per_launch": alg, "kernel_ms": mx["pair_ms"],
                 "position_image_ms": mx["image_ms"],
                 "md_step_bytes": md_step_bytes(P, N, 1 / REBUILD_8M),
+                "md_step_gbs": md_step_bytes(P, N, 1 / REBUILD_8M) / mx["t_step"] / 1e9,
                 "md_step_frac": md_step_bytes(P, N, 1 / REBUILD_8M) / mx["t_step"] / 1e9 / hbm}
     # what bounds the kernel instead of HBM, from the same capture: issue, the
     # ALU pipe and the L1 data pipe
@@ -872,6 +873,9 @@ def run_md8m(args, dist):
     fp_prof = "force_fp64_scatter_md_1m.txt"
     fp_pipe = profiled_metric(fp_prof, "sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active")
     fp64 = {"value": dist.world * fp["P"] / fp["t_step"] / 1e9, "ms_per_step": fp["t_step"] * 1e3,
+            "ns_per_particle_step": fp["t_step"] * 1e9 / N,
+            "md_step_hbm_gbs": md_step_bytes(fp["P"], N, 1 / REBUILD_8M, mixed=False)
+            / fp["t_step"] / 1e9,
             "pairs_half": fp["P"], "pair_kernel_ms": fp["pair_ms"],
             "kernel": "k_scatter_fp64_c (compacted half-list scatter)",
             "md_step_hbm_frac": md_step_bytes(fp["P"], N, 1 / REBUILD_8M, mixed=False)
@@ -883,6 +887,7 @@ def run_md8m(args, dist):
     line = {
         "metric": METRIC, "value": dist.world * P / mx["t_step"] / 1e9, "unit": UNIT,
         "n_gpus": dist.world, "steps": K, "warmup": W, "ms_per_step": mx["t_step"] * 1e3,
+        "ns_per_step": mx["t_step"] * 1e9, "ns_per_particle_step": mx["t_step"] * 1e9 / N,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 two-float pair math, f64 q/p", "data": "synthetic",
         "config": {"workload": md_workload(ncell), "N": N, "box": L, "pairs_half": P,
