@@ -53,8 +53,14 @@ NCELL, DENSITY, JITTER, SEED = 30, 0.5, 0.05, 20240601
 RC, RS, DT = 3.0, 3.3, 0.005
 METRIC = "G pair-interactions/s, mixed vs plain FP64, same GB300, force rel err <=1e-5"
 UNIT = "G pair-interactions/s"
-WORKLOAD = ("LJ force call, FCC 108,000 particles, rho=0.5, periodic L=60, rc=3.0, "
-            "search 3.3, i-sorted int32 CSR, dt=0.005")
+
+
+def force_workload(n, density, box):
+    return (f"LJ force call, FCC {n:,} particles, rho={density:g}, periodic L={box:.4g}, "
+            "rc=3.0, search 3.3, i-sorted int32 CSR, dt=0.005")
+
+
+WORKLOAD = force_workload(4 * NCELL ** 3, DENSITY, 60.0)
 NCELL_8M, REBUILD_8M, E2E_CHUNK = 126, 20, 20
 NCELL_MD = {"md_8m": 126, "md_1m": 63}
 PAIRS_HALF_1M = 74_033_514  # half-list pairs of the md_1m capture under profiles/
@@ -80,6 +86,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kick-lanes", type=int, default=0,
                     help="MD workloads: lanes per row of the mixed gather kick (0: default)")
+    ap.add_argument("--l2-window", type=float, default=0.0,
+                    help="force-call workloads: run on a side stream with an L2 persistence "
+                         "window of this hit ratio over the position image "
+                         "(lj_ctx_set_l2_window)")
     ap.add_argument("--chunk-graphs", action="store_true",
                     help="MD workloads: launch the captured step chunks from the host "
                          "instead of the persistent WHILE-node graph, so that a profiler "
@@ -373,6 +383,8 @@ def run_ours(args, dist, density=DENSITY, ncell=NCELL):
     qd = torch.from_numpy(q).to(dev)
     qs = [torch.from_numpy(np.ascontiguousarray(q[:, d])).to(dev) for d in range(3)]
     ctx = lj.Context(dist.local, stream=stream)
+    if args.l2_window:
+        ctx.set_l2_window(args.l2_window)
     t0 = time.perf_counter()
     ctx.build_list(qd, RS, box=L)
     torch.cuda.synchronize()
@@ -583,8 +595,7 @@ def run_ours(args, dist, density=DENSITY, ncell=NCELL):
         "ms_per_step": head["s_per_call"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 two-float pair math, f64 q/p",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD.replace("rho=0.5", f"rho={density}").replace(
-                       "L=60", f"L={L:.4g}"), "N": N, "pairs_half": P, "pairs_full": P_full,
+        "config": {"workload": force_workload(N, density, L), "N": N, "pairs_half": P, "pairs_full": P_full,
                    "max_row_half": max_half, "max_row_full": max_full, "box": L,
                    "variant": best_mixed, "step": "one force call",
                    "l2": "flushed before every timed call (512 MiB write)",
@@ -1112,10 +1123,20 @@ def main():
             line = run_precision(args, dist)
         elif args.workload == "batch_512":
             line = run_batch(args, dist)
-        elif args.workload == "rho1_1m":
-            line = run_ours(args, dist, 1.0, ncell=63)
         else:
-            line = run_ours(args, dist, 1.0 if args.workload == "rho1_108k" else DENSITY)
+            import contextlib
+            import torch
+            # the L2 window is a stream attribute: a side stream for that run
+            side = (torch.cuda.stream(torch.cuda.Stream(device=dist.local)) if args.l2_window
+                    else contextlib.nullcontext())
+            with side:
+                if args.workload == "rho1_1m":
+                    line = run_ours(args, dist, 1.0, ncell=63)
+                else:
+                    line = run_ours(args, dist,
+                                    1.0 if args.workload == "rho1_108k" else DENSITY)
+            if line is not None and args.l2_window:
+                line["config"]["l2_window_hit_ratio"] = args.l2_window
     if dist.rank == 0 and line is not None:
         print(json.dumps(line))
     dist.close()

@@ -123,6 +123,17 @@ int lj_ctx_set_timing(lj_ctx* ctx, int32_t on);
 /* ms[0]: position-image passes, ms[1]: pair kernels, ms[2]: both, summed
  * over *calls force calls since the last reset (synchronises). */
 int lj_ctx_get_timing(lj_ctx* ctx, double* ms, int64_t* calls);
+/* L2 persistence for the randomly gathered j positions (the benchmark spec's
+ * "L2 persistence windows"): with hit_ratio in (0, 1], the pair kernel of
+ * every later mixed force call on ctx runs with an access-policy window over
+ * the fixed-point position image (persisting hits for that fraction of it,
+ * streaming misses), and the context reserves that many bytes of L2 as
+ * persisting (its own limit, restored when the context is destroyed).
+ * 0 (the default) turns it off.  A cache hint: results are unchanged.  The
+ * window is an attribute of the context's stream, so force calls on a
+ * context without one (lj_ctx_set_stream) return LJ_ERR_UNSUPPORTED while
+ * it is on.  The MD loop's captured graphs do not use it. */
+int lj_ctx_set_l2_window(lj_ctx* ctx, double hit_ratio);
 
 /* ---- neighbour lists ---------------------------------------------------- */
 /* Installs an i-sorted CSR list for n particles (replaces the reference's

@@ -133,6 +133,7 @@ _SIGNATURES = {
     "lj_ctx_last_error": (C.c_char_p, [_P]),
     "lj_ctx_set_stream": (C.c_int, [_P, _P]),
     "lj_ctx_set_timing": (C.c_int, [_P, C.c_int32]),
+    "lj_ctx_set_l2_window": (C.c_int, [_P, C.c_double]),
     "lj_ctx_get_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "lj_list_set_csr": (C.c_int, [_P, C.c_int32, _P, _P, _P, C.c_int64, C.c_int32, C.c_int32]),
     "lj_list_set_pairs": (C.c_int, [_P, C.c_int32, _P, _P, C.c_int64, C.c_int32]),
@@ -270,6 +271,11 @@ class Context:
     def set_stream(self, stream):
         s = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream or 0)
         self._check(lib().lj_ctx_set_stream(self._h, s), "set_stream")
+
+    def set_l2_window(self, hit_ratio):
+        """L2 persistence window over the position image for mixed force calls
+        (lj_ctx_set_l2_window); 0 turns it off."""
+        self._check(lib().lj_ctx_set_l2_window(self._h, float(hit_ratio)), "set_l2_window")
 
     def set_timing(self, on=True):
         self._check(lib().lj_ctx_set_timing(self._h, 1 if on else 0), "set_timing")

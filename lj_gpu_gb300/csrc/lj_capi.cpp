@@ -351,6 +351,40 @@ const lj_force_opts* apply_tuned(lj_ctx* ctx, const lj_force_opts* o, int layout
   return o;
 }
 
+// Access-policy window over the n-entry position image on the context's
+// stream (lj_ctx_set_l2_window): persisting hits for l2_hit_ratio of it,
+// within the device's largest window and the persisting L2 this context
+// reserves on first use.
+int set_l2_window(lj_ctx* ctx, const int4* image, int32_t n) {
+  if (!ctx->stream)
+    return fail(ctx, LJ_ERR_UNSUPPORTED,
+                "the L2 window is a stream attribute: set a stream (lj_ctx_set_stream) first");
+  int dev = ctx->device, max_window = 0, max_persist = 0;
+  LJ_CUDA(ctx, cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dev),
+          "attribute");
+  LJ_CUDA(ctx, cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev),
+          "attribute");
+  const size_t bytes = std::min<size_t>((size_t)n * sizeof(int4), (size_t)max_window);
+  if (bytes == 0 || max_persist <= 0) return LJ_OK;  // no persisting L2 on this part
+  if (!ctx->l2_limit_set) {
+    LJ_CUDA(ctx, cudaDeviceGetLimit(&ctx->l2_limit_prev, cudaLimitPersistingL2CacheSize),
+            "limit");
+    LJ_CUDA(ctx, cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize,
+                                    std::min<size_t>(bytes, (size_t)max_persist)),
+            "limit");
+    ctx->l2_limit_set = true;
+  }
+  cudaStreamAttrValue v{};
+  v.accessPolicyWindow.base_ptr = const_cast<int4*>(image);
+  v.accessPolicyWindow.num_bytes = bytes;
+  v.accessPolicyWindow.hitRatio = (float)ctx->l2_hit_ratio;
+  v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+  v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+  LJ_CUDA(ctx, cudaStreamSetAttribute(ctx->stream, cudaStreamAttributeAccessPolicyWindow, &v),
+          "window");
+  return LJ_OK;
+}
+
 int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts* o_in) {
   int rc = check_opts(ctx, o_in);
   if (rc) return rc;
@@ -493,10 +527,18 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
       L.split = 1;
     }
   }
+  const bool window = ctx->l2_hit_ratio > 0.0 && L.qfix && n > 0;
+  if (window && (rc = set_l2_window(ctx, L.qfix, n))) return rc;
   if (tv) LJ_CUDA(ctx, cudaEventRecord(tv[1], ctx->stream), "event");
   if (L.kernel == 5) LJ_CUDA(ctx, launch_force_ell(L, ctx->stream), "force launch");
   else LJ_CUDA(ctx, launch_force(L, ctx->stream), "force launch");
   if (tv) LJ_CUDA(ctx, cudaEventRecord(tv[2], ctx->stream), "event");
+  if (window) {  // later launches on the stream run without the window
+    cudaStreamAttrValue off{};
+    off.accessPolicyWindow.num_bytes = 0;
+    LJ_CUDA(ctx, cudaStreamSetAttribute(ctx->stream, cudaStreamAttributeAccessPolicyWindow, &off),
+            "window off");
+  }
   return LJ_OK;
 }
 
@@ -822,6 +864,10 @@ void lj_ctx_destroy(lj_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   else cudaDeviceSynchronize();
+  if (ctx->l2_limit_set) {  // the persisting-L2 reservation this context made
+    cudaCtxResetPersistingL2Cache();
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, ctx->l2_limit_prev);
+  }
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : ctx->tev) cudaEventDestroy(e);
@@ -829,6 +875,15 @@ void lj_ctx_destroy(lj_ctx* ctx) {
 }
 
 const char* lj_ctx_last_error(const lj_ctx* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int lj_ctx_set_l2_window(lj_ctx* ctx, double hit_ratio) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (!(hit_ratio >= 0.0 && hit_ratio <= 1.0))
+    return fail(ctx, LJ_ERR_INVALID_ARGUMENT, "hit_ratio must be in [0, 1]");
+  ctx->l2_hit_ratio = hit_ratio;
+  return LJ_OK;
+}
 
 int lj_ctx_set_timing(lj_ctx* ctx, int32_t on) {
   if (!ctx) return LJ_ERR_INVALID_ARGUMENT;

@@ -113,6 +113,12 @@ struct lj_ctx {
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   // per-stage timing (lj_ctx_set_timing): event triples around force calls
   bool timing = false;
+  // L2 access-policy window over the position image for mixed force calls
+  // (lj_ctx_set_l2_window); the persisting-L2 limit found before the first
+  // use is restored at destroy
+  double l2_hit_ratio = 0.0;
+  bool l2_limit_set = false;
+  size_t l2_limit_prev = 0;
   std::vector<cudaEvent_t> tev;  // pool, 3 per recorded call
   size_t tev_used = 0;
   double t_ms[3] = {0, 0, 0};

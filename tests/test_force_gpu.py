@@ -735,6 +735,43 @@ def test_split_order_from_other_positions_keeps_precision(engine):
             check_mixed(ol.rel_errors(host(pd), ref), "mixed", "moved")
 
 
+@pytest.mark.parametrize("kernel", [2, 4])
+def test_l2_window_keeps_results(engine, kernel):
+    """The L2 persistence window over the position image is a cache hint:
+    mixed force calls give the same bits with it and without it.  It is a
+    stream attribute, so a context on the default stream refuses the call
+    while it is on; ratios outside [0, 1] are rejected."""
+    torch = _torch()
+    q, box, half = system("pbc_rho1")
+    opts = engine.make_opts(dt=0.005, cl2=9.0, box=box, precision="mixed", method="gather",
+                            kernel=kernel, unroll=4)
+    out = {}
+    side = torch.cuda.Stream()
+    for ratio in (0.0, 1.0, 0.5):
+        with engine.Context(0) as ctx:
+            ctx.set_stream(side)
+            ctx.set_l2_window(ratio)
+            ctx.set_list_csr(dev(half[0]), dev(half[1]), dev(half[2]), kind="half")
+            qd = dev(q)
+            torch.cuda.synchronize()
+            pd = torch.zeros_like(qd)
+            for _ in range(2):
+                ctx.force_aos(qd, pd, opts)
+            side.synchronize()
+            out[ratio] = pd.cpu().numpy()
+    assert np.array_equal(out[0.0], out[1.0]) and np.array_equal(out[0.0], out[0.5])
+    with engine.Context(0) as ctx:
+        for bad in (-0.1, 1.5):
+            with pytest.raises(engine.LJError) as e:
+                ctx.set_l2_window(bad)
+            assert e.value.status == engine.LJ_ERR_INVALID_ARGUMENT
+        ctx.set_l2_window(1.0)
+        ctx.set_list_csr(dev(half[0]), dev(half[1]), dev(half[2]), kind="half")
+        with pytest.raises(engine.LJError) as e:
+            ctx.force_aos(dev(q), dev(np.zeros_like(q)), opts)
+        assert e.value.status == engine.LJ_ERR_UNSUPPORTED
+
+
 def test_launch_option_checks(engine, fixture_rho05):
     f = fixture_rho05
     with engine.Context(0) as ctx:
