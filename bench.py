@@ -63,7 +63,7 @@ def force_workload(n, density, box):
 WORKLOAD = force_workload(4 * NCELL ** 3, DENSITY, 60.0)
 NCELL_8M, REBUILD_8M, E2E_CHUNK = 126, 20, 20
 NCELL_MD = {"md_8m": 126, "md_1m": 63}
-PAIRS_HALF_1M = 74_033_514  # half-list pairs of the md_1m capture under profiles/
+PAIRS_HALF_1M = 73_261_786  # half-list pairs of the md_1m capture under profiles/
 
 
 def md_workload(ncell):

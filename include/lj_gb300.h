@@ -94,7 +94,7 @@ typedef struct lj_force_opts {
                          their list form is missing (see lj_force.cu)       */
   int32_t unroll;     /* entries per lane in flight (kernel 2), 0 = default   */
   int32_t ff_all;     /* LJ_PREC_MIXED gathers (kernels 2 and 4): 0 = pairs
-                         beyond 2.3 sigma of the first call's positions in
+                         beyond 2.1 sigma of the first call's positions in
                          FP32 terms, any pair closer than 2.0 sigma in
                          two-float terms (the default); 1 = every pair in
                          two-float terms                                     */
@@ -304,9 +304,11 @@ typedef struct lj_md_params {
   int32_t graph_steps;    /* steps per captured CUDA graph (0: 20, 1: no graph) */
   int32_t rebuild_every;  /* 0: rebuild when a particle moved > skin/2 since the
                              last build; k > 0: also every k steps */
-  int32_t ff_all;         /* LJ_PREC_MIXED: 0 = pairs beyond 2.3 sigma at the
-                             last rebuild in FP32 terms (the default), 1 =
-                             every pair in two-float terms */
+  int32_t ff_all;         /* LJ_PREC_MIXED: 0 = pairs beyond 2.1 sigma at
+                             the last rebuild (2.3 in the replica batch) in
+                             FP32 terms, any pair closer than 2.0 sigma in
+                             two-float terms (the default), 1 = every pair
+                             in two-float terms */
   int32_t chunk_graphs;   /* 0: the steps between records run as one launch of a
                              persistent graph (a WHILE node); 1: as chunk graphs
                              launched back to back from the host, whose kernels

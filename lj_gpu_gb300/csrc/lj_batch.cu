@@ -144,7 +144,7 @@ void split(double v, float& hi, float& lo) {
 
 struct BatchState {
   int n = 0, R = 0, ncells = 0, maxrow = 0;
-  // split rows (two-float kicks with skin <= kFarSplit - kFarCheck): rows /
+  // split rows (two-float kicks with skin <= kFarSplitBatch - kFarCheck): rows /
   // cnt hold every row's near part, rows2 / cnt2 its far part (maxrow each)
   bool split = false;
   DevBuf<ReplicaInfo> reps;
@@ -304,7 +304,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     I.cl2f_hi = (float)(cl2u * (1 + bf));
     I.sl2u_lo = (float)(sl2u * (1 - bs));
     I.sl2u_hi = (float)(sl2u * (1 + bs));
-    I.near2u = (float)(kFarSplit * kFarSplit / u2);
+    I.near2u = (float)(kFarSplitBatch * kFarSplitBatch / u2);
     I.unit = u;
     I.cell_base = ncells;
     I.offset = off;
@@ -346,7 +346,7 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
   B_CUDA(ctx, b.rows.ensure((size_t)n_total * b.maxrow), "alloc");
   // two-float kicks split the rows when no far pair can come inside
   // kFarCheck before the next rebuild (pairs approach by at most the skin)
-  b.split = ff && !prm->ff_all && prm->skin <= kFarSplit - kFarCheck + 1e-12;
+  b.split = ff && !prm->ff_all && prm->skin <= kFarSplitBatch - kFarCheck + 1e-12;
   if (b.split) {
     B_CUDA(ctx, b.rows2.ensure((size_t)n_total * b.maxrow), "alloc");
     B_CUDA(ctx, b.cnt2.ensure((size_t)n_total), "alloc");

@@ -513,12 +513,14 @@ int run_force(lj_ctx* ctx, const Particles& part, int32_t n, const lj_force_opts
         ok = true;
       }
       if (!ctx->closef_zeroed) {
-        LJ_CUDA(ctx, ctx->closef.ensure(2), "alloc");
-        LJ_CUDA(ctx, cudaMemsetAsync(ctx->closef.ptr, 0, 2 * sizeof(int32_t), ctx->stream),
+        LJ_CUDA(ctx, ctx->closef.ensure(3), "alloc");
+        LJ_CUDA(ctx, cudaMemsetAsync(ctx->closef.ptr, 0, 3 * sizeof(int32_t), ctx->stream),
                 "memset");
         ctx->closef_zeroed = true;
       }
+      LJ_CUDA(ctx, ctx->closeq.ensure((size_t)n), "alloc");
       L.close_flag = ctx->closef.ptr;
+      L.close_rows = ctx->closeq.ptr;
       // near part [0, nn), far part [nn, np) of every row
       L.csr.list = buf.ptr;
       L.far = L.csr;

@@ -97,7 +97,7 @@ struct lj_ctx {
   ljg::DevBuf<long long> oframe;
   bool oframe_armed = false;
   // the segment gather's close-entry flag (two words, zeroed once)
-  ljg::DevBuf<int32_t> closef;
+  ljg::DevBuf<int32_t> closef, closeq;
   bool closef_zeroed = false;
   ljg::DevBuf<int32_t> err2;
   ljg::DevBuf<int32_t> tmp_i32a, tmp_i32b;

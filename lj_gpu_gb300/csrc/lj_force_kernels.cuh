@@ -973,15 +973,17 @@ __device__ __forceinline__ void walk_row(const Csr& C, int i, bool valid, int la
 // (the FP32 kernels' arithmetic and cutoff band) into compensated FP32 sums,
 // which then seed the two-float sums of the near part's two-float terms.  A
 // far entry closer than K.near2 (2.0 sigma) -- a pair that moved in since
-// the rows were split -- is skipped there and raises close_flag[0], and
-// k_seg_close_terms then adds its two-float term, so the split decides the
-// speed, never the precision.
+// the rows were split -- is skipped there: its row goes once onto the close
+// queue (close_rows, count in close_flag[2]) and raises close_flag[0], and
+// k_seg_close_terms then adds the two-float terms of the queued rows' close
+// entries, so the split decides the speed, never the precision.
 template <int G, int U, bool PBC, bool SOA, bool ANISO, bool VEC>
 __global__ void __launch_bounds__(256, 3) k_gather_mixed_seg(const Particles P, const Csr C,
                                                           const Csr F,
                                                           const int4* __restrict__ qfix,
                                                           const MixedConsts K0,
                                                           int32_t* close_flag,
+                                                          int32_t* __restrict__ close_rows,
                                                           const int32_t* __restrict__ rowperm) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int row = t / G;
@@ -1059,8 +1061,24 @@ __global__ void __launch_bounds__(256, 3) k_gather_mixed_seg(const Particles P, 
   }
   // rare: far entries that moved inside K.near2 since the split are left to
   // k_seg_close_terms (its own kernel, so that its registers do not add to
-  // this one's)
-  if (__any_sync(kFullMask, missed) && (threadIdx.x & 31) == 0) atomicExch(close_flag, 1);
+  // this one's); the first lane of each row group with such an entry queues
+  // the row, one slot per row (the queue holds n rows)
+  {
+    const unsigned mb = __ballot_sync(kFullMask, missed);
+    if (mb) {
+      const int wl = threadIdx.x & 31;
+      const unsigned gmask = G == 32 ? kFullMask : ((1u << G) - 1u);
+      const bool lead = (wl & (G - 1)) == 0 && ((mb >> wl) & gmask) != 0u;
+      const unsigned lm = __ballot_sync(kFullMask, lead);
+      int slot = 0;
+      if (wl == 0) {
+        slot = atomicAdd(close_flag + 2, __popc(lm));
+        atomicExch(close_flag, 1);
+      }
+      slot = __shfl_sync(kFullMask, slot, 0) + __popc(lm & ((1u << wl) - 1u));
+      if (lead) close_rows[slot] = i;
+    }
+  }
   // ---- near part: two-float terms
   walk_row<G, U, VEC>(C, i, valid, lane, qfix, [&](const int4 (&xj)[U], const int* jj,
                                                     const bool (&ok)[U]) {
@@ -1084,21 +1102,26 @@ __global__ void __launch_bounds__(256, 3) k_gather_mixed_seg(const Particles P, 
 }
 
 // The two-float terms of the far-part entries closer than K.near2 (FP32 r2,
-// the far walk's own test) of every row, kicked into p, when
-// k_gather_mixed_seg raised flag[0]; otherwise every block returns at once.
-// Rows in a grid-stride loop, G lanes per row, one entry per lane and step.
-// The last block to finish clears flag[0] and its counter flag[1].
+// the far walk's own test) of the rows k_gather_mixed_seg queued (rows[0,
+// flag[2]), each row once), kicked into p, when it raised flag[0]; otherwise
+// every block returns at once.  A warp per queued row (G = 32, one entry per
+// lane and step), so that a few queued rows do not wait on one lane walking
+// a whole row.  The last block to finish clears flag[0], its counter flag[1]
+// and the queue length flag[2].
 template <int G, bool PBC, bool SOA, bool ANISO>
 __global__ void __launch_bounds__(256) k_seg_close_terms(const Particles P, const Csr F,
                                                          const int4* __restrict__ qfix,
-                                                         const MixedConsts K0, int32_t* flag) {
+                                                         const MixedConsts K0, int32_t* flag,
+                                                         const int32_t* __restrict__ queue) {
   if (*(volatile int32_t*)flag == 0) return;
   const MixedConsts K = PBC ? K0 : frame_consts(K0);
   const int lane = threadIdx.x & (G - 1);
   const int groups = (gridDim.x * blockDim.x) / G;
-  const int rows = (F.n + groups - 1) / groups * groups;  // whole warps take every pass
-  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) / G; i < rows; i += groups) {
-    const bool valid = i < F.n;
+  const int queued = min(*(volatile int32_t*)(flag + 2), F.n);
+  const int rows = (queued + groups - 1) / groups * groups;  // whole warps take every pass
+  for (int r = (blockIdx.x * blockDim.x + threadIdx.x) / G; r < rows; r += groups) {
+    const bool valid = r < queued;
+    const int i = valid ? __ldg(queue + r) : 0;
     const int4 xi = valid ? __ldg(qfix + i) : make_int4(0, 0, 0, 0);
     int li[3];
     image_lo(xi.w, li[0], li[1], li[2]);
@@ -1131,6 +1154,7 @@ __global__ void __launch_bounds__(256) k_seg_close_terms(const Particles P, cons
     if (atomicAdd(flag + 1, 1) == (int)gridDim.x - 1) {
       flag[0] = 0;
       flag[1] = 0;
+      flag[2] = 0;
     }
   }
 }
@@ -1275,7 +1299,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
 // k_gather_mixed_seg, with the row's replica constants, over the rows of one
 // size class.  The far part (F) runs first in FP32 terms, whose compensated
 // sums seed the two-float sums of the near part (C).  The batch splits its
-// rows only when the skin is at most kFarSplit - kFarCheck: a rebuild comes
+// rows only when the skin is at most kFarSplitBatch - kFarCheck: a rebuild comes
 // before any particle moves more than skin / 2, so no far pair comes inside
 // kFarCheck before the next rebuild and every far entry takes its FP32 term.
 template <int G, int U, bool VEC>

@@ -21,20 +21,21 @@ cudaError_t launch_mixed_ff_split(const ForceLaunch& L, const MixedConsts& K, cu
         if (L.aniso)
           e = launch_dependent(k_gather_mixed_seg<G, U, P.value, S.value, true, V>, blocks,
                                block, s, L.part, L.csr, L.far, L.qfix, K, L.close_flag,
-                               L.rowperm);
+                               L.close_rows, L.rowperm);
         else
           e = launch_dependent(k_gather_mixed_seg<G, U, P.value, S.value, false, V>, blocks,
                                block, s, L.part, L.csr, L.far, L.qfix, K, L.close_flag,
-                               L.rowperm);
+                               L.close_rows, L.rowperm);
         if (e != cudaSuccess) return e;
-        // far entries that came inside 2.0 sigma (a no-op unless the flag is up)
-        const int cb = (int)std::min<long long>(((long long)n * G + 255) / 256, 152 * 4);
+        // queued rows with far entries that came inside 2.0 sigma, a warp per
+        // row (a no-op unless the flag is up)
+        const int cb = (int)std::min<long long>(((long long)n * 32 + 255) / 256, 152 * 4);
         if (L.aniso)
-          k_seg_close_terms<G, P.value, S.value, true>
-              <<<cb, 256, 0, s>>>(L.part, L.far, L.qfix, K, L.close_flag);
+          k_seg_close_terms<32, P.value, S.value, true>
+              <<<cb, 256, 0, s>>>(L.part, L.far, L.qfix, K, L.close_flag, L.close_rows);
         else
-          k_seg_close_terms<G, P.value, S.value, false>
-              <<<cb, 256, 0, s>>>(L.part, L.far, L.qfix, K, L.close_flag);
+          k_seg_close_terms<32, P.value, S.value, false>
+              <<<cb, 256, 0, s>>>(L.part, L.far, L.qfix, K, L.close_flag, L.close_rows);
         return cudaGetLastError();
       });
     });

@@ -107,8 +107,10 @@ struct ForceLaunch {
   // k_gather_mixed_seg
   int split;
   Csr far;
-  // two device words, zero between calls (k_seg_close_terms clears them)
+  // three device words, zero between calls (k_seg_close_terms clears them),
+  // and the close queue: n row slots
   int32_t* close_flag;
+  int32_t* close_rows;
   // split rows: the order in which the segment gather visits them (nullptr:
   // row order); the MD loop passes the cell order of its last build
   const int32_t* rowperm;

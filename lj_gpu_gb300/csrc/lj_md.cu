@@ -38,8 +38,8 @@ enum {
   F_COUNT = 3,    // rebuilds done
   F_MAXROW = 4,   // longest row of the last build
   F_STEP = 5,     // steps taken (drives rebuild_every)
-  F_CLOSE = 6,    // two words for k_seg_close_terms
-  F_LOOP = 8,     // chunks left in the persistent loop
+  F_CLOSE = 6,    // three words for k_seg_close_terms (6..8)
+  F_LOOP = 9,     // chunks left in the persistent loop
   F_WORDS = 10
 };
 
@@ -185,6 +185,7 @@ struct MdState {
   // split two-float kicks: rows / cnt hold every row's near part, rows2 /
   // cnt2 the far part (launch_build_rows_split)
   DevBuf<int32_t> rows2, cnt2;
+  DevBuf<int32_t> closeq;  // rows with far entries inside 2.0 sigma (k_gather_mixed_seg)
   int64_t cap2 = 0;
   bool split = false;
   DevBuf<int64_t> start, off;
@@ -378,6 +379,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   if (m.split) {
     MD_CUDA(ctx, m.rows2.ensure((size_t)m.cap2), "alloc");
     MD_CUDA(ctx, m.cnt2.ensure(n), "alloc");
+    MD_CUDA(ctx, m.closeq.ensure(n), "alloc");
   }
   // the compacted half list holds about half of the padded capacity
   const int64_t half_cap = std::min<int64_t>(m.cap, 0x7fffffffll);
@@ -402,6 +404,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     K.rowperm = m.order2.ptr;
   }
   K.close_flag = m.flags.ptr + F_CLOSE;
+  K.close_rows = m.split ? m.closeq.ptr : nullptr;
   K.box.on = 1;
   for (int d = 0; d < 3; d++) {
     K.box.len[d] = prm->box[d];

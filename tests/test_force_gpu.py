@@ -695,7 +695,7 @@ def test_kernel4_measure_uses_the_uploaded_list(engine, fixture_rho05, prec):
 @pytest.mark.parametrize("name", list(SYSTEMS))
 @pytest.mark.parametrize("kernel", [2, 4])
 def test_two_float_split_and_full_terms(engine, name, kernel):
-    """The two-float gather's near/far split (FP32 terms beyond 2.3 sigma,
+    """The two-float gather's near/far split (FP32 terms beyond 2.1 sigma,
     the default) and two-float terms for every pair (ff_all) both meet the
     per-particle bar; they differ only by the far terms' FP32 rounding."""
     q, box, half = system(name)
@@ -714,11 +714,13 @@ def test_two_float_split_and_full_terms(engine, name, kernel):
         assert ol.rel_errors(out[True], ref)["max_rel"] <= 1e-7
 
 
-def test_split_order_from_other_positions_keeps_precision(engine):
+@pytest.mark.parametrize("lanes", [0, 2, 8, 32])
+def test_split_order_from_other_positions_keeps_precision(engine, lanes):
     """The near-first order is made from the positions of the first call;
-    later calls with particles moved by up to 0.45 sigma (past the 0.3 sigma
-    margin) still meet the per-particle bar: pairs that came closer than
-    2.0 sigma are evaluated in two-float terms wherever they sit."""
+    later calls with particles moved by up to 0.45 sigma (far past the 0.1
+    sigma margin of the 2.1 sigma split) still meet the per-particle bar:
+    the rows whose far pairs came closer than 2.0 sigma are queued, each
+    once whatever the lanes per row, and those pairs get two-float terms."""
     q, box = ol.init_fcc_periodic(6, 1.0, 0.05, seed=20240601)
     rng = np.random.default_rng(8)
     q2 = q.copy()
@@ -727,7 +729,7 @@ def test_split_order_from_other_positions_keeps_precision(engine):
     with engine.Context(0) as ctx:
         ctx.set_list_csr(dev(half[0]), dev(half[1]), dev(half[2]), kind="half")
         opts = engine.make_opts(dt=0.005, cl2=9.0, box=box, precision="mixed",
-                                method="gather")
+                                method="gather", lanes=lanes)
         for pos in (q, q2, q):
             pd = dev(np.zeros_like(q))
             ctx.force_aos(dev(pos), pd, opts)
