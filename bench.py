@@ -1082,10 +1082,15 @@ def run_reference(args, dist):
         config = {"workload": workload, "N": n, "rows_per_step": row1, "pairs_half": P,
                   "step": "force call over 1/16 of the rows", "parallelism": "host cores"}
     else:
-        q, L = ol.init_fcc_periodic(NCELL, DENSITY, JITTER, SEED)
+        # the system of the chosen workload: 1,000,188 particles at rho 1 for
+        # the 1M workloads, 108,000 at rho 1 or 0.5 otherwise (the replica
+        # batch has no counterpart in the reference: the 108k force call)
+        big = args.workload in ("md_1m", "precision_1m", "rho1_1m")
+        ncell = 63 if big else NCELL
+        rho = 1.0 if big or args.workload == "rho1_108k" else DENSITY
+        q, L = ol.init_fcc_periodic(ncell, rho, JITTER, SEED)
         full = ol.build_list(q, RS, box=L, full=True)
-        half = ol.build_list(q, RS, box=L)
-        P = len(half[2])
+        P = len(full[2]) // 2
         p = np.zeros_like(q)
         for _ in range(args.warmup):
             ol.force_gather_aos(q, p, *full, cl2=RC * RC, dt=DT, box=L, threads=threads)
@@ -1093,9 +1098,10 @@ def run_reference(args, dist):
         ol.force_gather_aos(q, p, *full, cl2=RC * RC, dt=DT, box=L, calls=args.steps,
                             threads=threads)
         t = time.perf_counter() - t0
-        workload, sample = WORKLOAD, ("every step is one full force call of the workload "
-                                      "(C restatement of the reference routine, OpenMP "
-                                      "gather)")
+        workload = (md_workload(ncell) if args.workload in NCELL_MD
+                    else force_workload(q.shape[0], rho, L))
+        sample = ("every step is one full force call of the workload's system (C "
+                  "restatement of the reference routine, OpenMP gather)")
         config = {"workload": workload, "N": q.shape[0], "pairs_half": P,
                   "step": "one force call", "parallelism": "host cores"}
     v = P * args.steps / t / 1e9
