@@ -345,6 +345,17 @@ int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_params* 
               int32_t nsteps, lj_md_record* records, int32_t max_records, int32_t* n_records,
               lj_md_stats* stats);
 
+/* lj_md_run over host arrays (AoS double[n][4], updated in place; page-locked
+ * memory lets the copies overlap the run): q is copied to the device before
+ * the initial list build, p beside that build on a second stream; at the end
+ * q goes back beside the final half kick and p after it.  Returns once q and
+ * p are back on the host.  Mirrors the reference's measure()
+ * (cuda/force_cuda.cu:319-342: copy in, run, copy out) for the MD loop;
+ * stats->ms_total includes the copies. */
+int lj_md_run_host(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_params* params,
+                   int32_t nsteps, lj_md_record* records, int32_t max_records,
+                   int32_t* n_records, lj_md_stats* stats);
+
 /* ---- replica batches (project extension) --------------------------------- */
 /* Many independent periodic systems of uneven size in one velocity-Verlet
  * loop (mixed precision): q, p hold the replicas back to back (AoS device

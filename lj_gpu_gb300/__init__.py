@@ -176,6 +176,9 @@ _SIGNATURES = {
     "lj_md_run": (C.c_int, [_P, _P, _P, C.c_int32, C.POINTER(MdParams), C.c_int32,
                             C.POINTER(MdRecord), C.c_int32, C.POINTER(C.c_int32),
                             C.POINTER(MdStats)]),
+    "lj_md_run_host": (C.c_int, [_P, _P, _P, C.c_int32, C.POINTER(MdParams), C.c_int32,
+                                 C.POINTER(MdRecord), C.c_int32, C.POINTER(C.c_int32),
+                                 C.POINTER(MdStats)]),
     "lj_force_mixed_noalloc_aos": (C.c_int, [_P, _P, C.c_int32, C.c_double, C.c_double, _P,
                                              _P, _P, _P, _P]),
 }
@@ -397,6 +400,32 @@ class Context:
         s = lib().lj_md_run(self._h, ptr(q), ptr(p), q.shape[0], C.byref(params), int(nsteps),
                             recs, max_records, C.byref(nrec), C.byref(st))
         self._check(s, "md_run")
+        return ([(recs[k].step, recs[k].kinetic, recs[k].potential) for k in range(nrec.value)],
+                {"steps": st.steps, "rebuilds": st.rebuilds, "ms_total": st.ms_total,
+                 "list_capacity": st.list_capacity, "launches": st.launches,
+                 "loop_graph": st.loop_graph})
+
+    def md_run_host(self, q, p, params: MdParams, nsteps, max_records=64):
+        """lj_md_run_host: velocity Verlet over host AoS (n, 4) float64 arrays
+        (numpy arrays or CPU tensors, page-locked for overlapped copies),
+        updated in place; returns (records, stats) as md_run."""
+        import numpy as np
+        for a in (q, p):
+            arr = a.numpy() if hasattr(a, "numpy") else a
+            if not (isinstance(arr, np.ndarray) and arr.dtype == np.float64 and arr.ndim == 2
+                    and arr.shape[1] == 4 and arr.flags.c_contiguous):
+                raise ValueError("q and p must be C-contiguous float64 arrays of shape (n, 4)")
+        hq = q.numpy() if hasattr(q, "numpy") else q
+        hp = p.numpy() if hasattr(p, "numpy") else p
+        if hq.shape != hp.shape:
+            raise ValueError("q and p must have the same shape")
+        recs = (MdRecord * max(1, max_records))()
+        nrec = C.c_int32()
+        st = MdStats()
+        s = lib().lj_md_run_host(self._h, hq.ctypes.data, hp.ctypes.data, hq.shape[0],
+                                 C.byref(params), int(nsteps), recs, max_records,
+                                 C.byref(nrec), C.byref(st))
+        self._check(s, "md_run_host")
         return ([(recs[k].step, recs[k].kinetic, recs[k].potential) for k in range(nrec.value)],
                 {"steps": st.steps, "rebuilds": st.rebuilds, "ms_total": st.ms_total,
                  "list_capacity": st.list_capacity, "launches": st.launches,

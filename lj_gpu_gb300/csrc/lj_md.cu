@@ -266,7 +266,22 @@ struct DriftArgs {
   int rebuild_every;
 };
 
-cudaError_t md_step(MdState& m, const DriftArgs& d, const ForceLaunch& kick, cudaStream_t s) {
+// Host buffers of lj_md_run_host.  q goes to the device on the run's stream
+// before the initial build; p on a side stream, waited for before its first
+// use, so that its copy runs beside the build.  At the end q, final once the
+// last drift has run, goes back on the side stream beside the final half
+// kick, and p on the run's stream.
+struct HostIo {
+  double* q;
+  double* p;
+  size_t bytes;
+  cudaStream_t side;
+  cudaEvent_t ev_in, ev_p, ev_q, ev_side_done;
+  bool q_queued = false;  // the copy of q back to the host is queued
+};
+
+cudaError_t md_step(MdState& m, const DriftArgs& d, const ForceLaunch& kick, cudaStream_t s,
+                    HostIo* io = nullptr) {
   k_md_drift<<<grid1(m.n, 256), 256, 0, s>>>(
       d.q, d.p, m.n, d.dt, d.len[0], d.len[1], d.len[2], kick.axis[0], kick.axis[1],
       kick.axis[2], m.qfix.ptr, m.qref.ptr, d.unit[0], d.unit[1], d.unit[2], d.half_skin2,
@@ -274,6 +289,12 @@ cudaError_t md_step(MdState& m, const DriftArgs& d, const ForceLaunch& kick, cud
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if ((e = md_rebuild(m, kick.method == LJ_METHOD_SCATTER_HALF, kick, s))) return e;
+  if (io) {  // the last step: q is final, its copy back runs beside the kick
+    if ((e = cudaEventRecord(io->ev_q, s)) || (e = cudaStreamWaitEvent(io->side, io->ev_q, 0)) ||
+        (e = cudaMemcpyAsync(io->q, d.q, io->bytes, cudaMemcpyDeviceToHost, io->side)))
+      return e;
+    io->q_queued = true;
+  }
   return launch_force(kick, s);
 }
 
@@ -293,9 +314,11 @@ int64_t graph_kernels(cudaGraph_t g) {
 
 }  // namespace
 
-extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_params* prm,
-                         int32_t nsteps, lj_md_record* records, int32_t max_records,
-                         int32_t* n_records, lj_md_stats* stats) {
+// lj_md_run over device q, p; with io, over the host buffers it names (the
+// device q, p are then the context's staging arrays).
+static int md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_params* prm,
+                  int32_t nsteps, lj_md_record* records, int32_t max_records,
+                  int32_t* n_records, lj_md_stats* stats, HostIo* io) {
   if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
   ctx->err.clear();
   if (n_records) *n_records = 0;
@@ -468,6 +491,14 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
     }
   } evg{t0, t1};
   MD_CUDA(ctx, cudaEventRecord(t0, s), "event");
+  if (io) {
+    MD_CUDA(ctx, cudaEventRecord(io->ev_in, s), "event");  // after the caller's earlier work
+    MD_CUDA(ctx, cudaMemcpyAsync(q, io->q, io->bytes, cudaMemcpyHostToDevice, s), "H2D q");
+    MD_CUDA(ctx, cudaStreamWaitEvent(io->side, io->ev_in, 0), "wait");
+    MD_CUDA(ctx, cudaMemcpyAsync(p, io->p, io->bytes, cudaMemcpyHostToDevice, io->side),
+            "H2D p");
+    MD_CUDA(ctx, cudaEventRecord(io->ev_p, io->side), "event");
+  }
 
   // ---- initial image and list (one captured graph, so that its kernels are
   // counted) -------------------------------------------------------------------
@@ -536,6 +567,7 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
 
   int32_t f[F_WORDS];
   int rc;
+  if (io) MD_CUDA(ctx, cudaStreamWaitEvent(s, io->ev_p, 0), "wait");  // p's first use follows
   if ((rc = read_flags(f))) return rc;
   if (f[F_OVERFLOW])
     return lj_fail(ctx, LJ_ERR_LIST_OVERFLOW, "a neighbour row exceeds %d entries", m.maxrow);
@@ -596,7 +628,8 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
       plain -= m.graph_steps;
     }
     for (; plain > 0; plain--) MD_CUDA(ctx, md_step(m, D, Kfull, s), "step");
-    MD_CUDA(ctx, md_step(m, D, Khalf, s), "step");  // p(stop), synchronous
+    MD_CUDA(ctx, md_step(m, D, Khalf, s, stop == nsteps ? io : nullptr),
+            "step");  // p(stop), synchronous
     if ((rc = read_flags(f))) return rc;
     if (f[F_OVERFLOW])
       return lj_fail(ctx, LJ_ERR_LIST_OVERFLOW,
@@ -608,6 +641,13 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
       kicks++;
     }
     step = stop;
+  }
+  if (io) {
+    if (!io->q_queued)
+      MD_CUDA(ctx, cudaMemcpyAsync(io->q, q, io->bytes, cudaMemcpyDeviceToHost, s), "D2H q");
+    MD_CUDA(ctx, cudaMemcpyAsync(io->p, p, io->bytes, cudaMemcpyDeviceToHost, s), "D2H p");
+    MD_CUDA(ctx, cudaEventRecord(io->ev_side_done, io->side), "event");
+    MD_CUDA(ctx, cudaStreamWaitEvent(s, io->ev_side_done, 0), "wait");
   }
   MD_CUDA(ctx, cudaEventRecord(t1, s), "event");
   if ((rc = read_flags(f))) return rc;
@@ -623,5 +663,49 @@ extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_
   }
   if (n_records) *n_records = nrec;
   if (!ctx->stream) MD_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+  return LJ_OK;
+}
+
+extern "C" int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_params* prm,
+                         int32_t nsteps, lj_md_record* records, int32_t max_records,
+                         int32_t* n_records, lj_md_stats* stats) {
+  return md_run(ctx, q, p, n, prm, nsteps, records, max_records, n_records, stats, nullptr);
+}
+
+extern "C" int lj_md_run_host(lj_ctx* ctx, double* q, double* p, int32_t n,
+                              const lj_md_params* prm, int32_t nsteps, lj_md_record* records,
+                              int32_t max_records, int32_t* n_records, lj_md_stats* stats) {
+  if (!ctx) return LJ_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (n_records) *n_records = 0;
+  if (!q || !p || n < 1) return lj_fail(ctx, LJ_ERR_INVALID_ARGUMENT, "bad MD arguments");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return lj_fail(ctx, LJ_ERR_CUDA, "set device");
+  const size_t bytes = sizeof(double) * 4 * (size_t)n;
+  MD_CUDA(ctx, ctx->mq.ensure(4 * (size_t)n), "alloc");
+  MD_CUDA(ctx, ctx->mp.ensure(4 * (size_t)n), "alloc");
+  HostIo io{q, p, bytes, nullptr, {}, {}, {}, {}};
+  // the side stream and events live for this call; the guard waits for every
+  // copy on the side stream before the host buffers are handed back
+  struct Guard {
+    HostIo& io;
+    ~Guard() {
+      if (io.side) {
+        cudaStreamSynchronize(io.side);
+        cudaStreamDestroy(io.side);
+      }
+      for (cudaEvent_t e : {io.ev_in, io.ev_p, io.ev_q, io.ev_side_done})
+        if (e) cudaEventDestroy(e);
+    }
+  } guard{io};
+  MD_CUDA(ctx, cudaStreamCreateWithFlags(&io.side, cudaStreamNonBlocking), "stream");
+  for (cudaEvent_t* e : {&io.ev_in, &io.ev_p, &io.ev_q, &io.ev_side_done})
+    MD_CUDA(ctx, cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event");
+  const int rc = md_run(ctx, ctx->mq.ptr, ctx->mp.ptr, n, prm, nsteps, records, max_records,
+                        n_records, stats, &io);
+  // the run's stream may still hold copies of the host buffers (on errors too)
+  cudaStream_t s = ctx->stream ? ctx->stream : (ctx->md ? ctx->md->own_stream : nullptr);
+  const cudaError_t se = s ? cudaStreamSynchronize(s) : cudaSuccess;
+  if (rc) return rc;
+  MD_CUDA(ctx, se, "sync");
   return LJ_OK;
 }

@@ -80,6 +80,53 @@ def test_mixed_md_tracks_fp64_and_conserves(engine):
     assert sm["rebuilds"] >= 2
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_md_run_host_matches_the_device_run(engine, precision):
+    """lj_md_run_host (host arrays in and out, the copies overlapped with the
+    initial build and the final half kick) integrates as lj_md_run on device
+    copies: identical positions and momenta for the mixed gather (to the
+    rounding of the FP64 scatter's atomic sums for FP64), the same records,
+    with page-locked tensors or plain numpy arrays; zero steps return q and p
+    unchanged; a list overflow is reported as from lj_md_run."""
+    import torch
+    q, L = ol.init_fcc_periodic(6, 1.0, 0.05, seed=21)  # 864 particles
+    p = engine.init_momenta(q.shape[0], 1.0, seed=9)
+    prm = engine.make_md_params(0.005, 2.5, 0.3, L, precision=precision, record_every=20,
+                                graph_steps=8)
+    qd, pd = _dev(q), _dev(p)
+    with engine.Context(0) as ctx:
+        recs_d, st_d = ctx.md_run(qd, pd, prm, 50)
+    torch.cuda.synchronize()
+    ref_q, ref_p = qd.cpu().numpy(), pd.cpu().numpy()
+    pinned = (torch.from_numpy(q.copy()).pin_memory(), torch.from_numpy(p.copy()).pin_memory())
+    plain = (q.copy(), p.copy())
+    for hq, hp in (pinned, plain):
+        with engine.Context(0) as ctx:
+            recs_h, st_h = ctx.md_run_host(hq, hp, prm, 50)
+        hq_ = hq.numpy() if hasattr(hq, "numpy") else hq
+        hp_ = hp.numpy() if hasattr(hp, "numpy") else hp
+        if precision == "mixed":  # the gather kick is deterministic
+            assert np.array_equal(hq_, ref_q) and np.array_equal(hp_, ref_p)
+        else:  # the FP64 scatter adds with atomics: last bits vary run to run
+            assert np.abs(periodic_diff(hq_, ref_q, L)).max() < 1e-10
+            assert ol.rel_errors(hp_, ref_p)["max_rel_rms"] < 1e-9
+        assert [r[0] for r in recs_h] == [r[0] for r in recs_d] == [0, 20, 40, 50]
+        for a, b in zip(recs_h, recs_d):
+            assert abs(a[1] - b[1]) <= 1e-12 * abs(b[1]) and abs(a[2] - b[2]) <= 1e-12 * abs(b[2])
+        assert st_h["rebuilds"] == st_d["rebuilds"]
+    q0, p0 = q.copy(), p.copy()
+    with engine.Context(0) as ctx:
+        ctx.md_run_host(q0, p0, prm, 0)
+    assert np.array_equal(q0, q) and np.array_equal(p0, p)
+    # the overflow case of test_md_list_overflow_is_reported, through the host entry
+    qc, _ = ol.init_fcc_periodic(5, 1.0, 0.05, seed=3)
+    with engine.Context(0) as ctx:
+        with pytest.raises(engine.LJError) as e:
+            ctx.md_run_host(qc.copy(), np.zeros_like(qc),
+                            engine.make_md_params(0.005, 3.0, 0.3, 40.0, precision="mixed"), 5)
+        assert e.value.status == engine.LJ_ERR_LIST_OVERFLOW
+
+
 def test_md_list_overflow_is_reported(engine):
     # 500 particles packed into a corner of a large box: the capacity estimate
     # from the mean density is far too small (64 entries for ~150 partners
