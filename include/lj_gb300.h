@@ -305,10 +305,9 @@ typedef struct lj_md_params {
   int32_t rebuild_every;  /* 0: rebuild when a particle moved > skin/2 since the
                              last build; k > 0: also every k steps */
   int32_t ff_all;         /* LJ_PREC_MIXED: 0 = pairs beyond 2.1 sigma at
-                             the last rebuild (2.3 in the replica batch) in
-                             FP32 terms, any pair closer than 2.0 sigma in
-                             two-float terms (the default), 1 = every pair
-                             in two-float terms */
+                             the last rebuild in FP32 terms, any pair closer
+                             than 2.0 sigma in two-float terms (the
+                             default), 1 = every pair in two-float terms */
   int32_t chunk_graphs;   /* 0: the steps between records run as one launch of a
                              persistent graph (a WHILE node); 1: as chunk graphs
                              launched back to back from the host, whose kernels

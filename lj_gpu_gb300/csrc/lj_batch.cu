@@ -144,12 +144,13 @@ void split(double v, float& hi, float& lo) {
 
 struct BatchState {
   int n = 0, R = 0, ncells = 0, maxrow = 0;
-  // split rows (two-float kicks with skin <= kFarSplitBatch - kFarCheck): rows /
-  // cnt hold every row's near part, rows2 / cnt2 its far part (maxrow each)
+  // split rows (two-float kicks): rows / cnt hold every row's near part,
+  // rows2 / cnt2 its far part (maxrow each); closef (three words) and closeq
+  // (a slot per particle) the close queue of far entries inside kFarCheck
   bool split = false;
   DevBuf<ReplicaInfo> reps;
   DevBuf<int32_t> rid, cell_rid, flags, cell, count, cursor, order, order2, cnt, rows, classrows;
-  DevBuf<int32_t> rows2, cnt2;
+  DevBuf<int32_t> rows2, cnt2, closef, closeq;
   DevBuf<int4> qfix, qref, cq, cq2;
   DevBuf<int64_t> start;
   DevBuf<unsigned char> scan_tmp;
@@ -214,7 +215,8 @@ cudaError_t batch_kick(BatchState& b, const Particles& part, const std::vector<S
   for (const SizeClass& k : cls) {
     cudaError_t e = launch_force_batch(part, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                        b.classrows.ptr + k.first, k.count, dt, cl2, k.lanes,
-                                       k.unroll, k.vec, ff, s, b.split ? &far : nullptr);
+                                       k.unroll, k.vec, ff, s, b.split ? &far : nullptr,
+                                       b.closef.ptr, b.closeq.ptr);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -304,7 +306,8 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
     I.cl2f_hi = (float)(cl2u * (1 + bf));
     I.sl2u_lo = (float)(sl2u * (1 - bs));
     I.sl2u_hi = (float)(sl2u * (1 + bs));
-    I.near2u = (float)(kFarSplitBatch * kFarSplitBatch / u2);
+    I.near2u = (float)(kFarSplit * kFarSplit / u2);
+    I.nearc2u = (float)(kFarCheck * kFarCheck / u2);
     I.unit = u;
     I.cell_base = ncells;
     I.offset = off;
@@ -344,12 +347,15 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
   B_CUDA(ctx, b.order2.ensure((size_t)n_total), "alloc");
   B_CUDA(ctx, b.cnt.ensure((size_t)n_total), "alloc");
   B_CUDA(ctx, b.rows.ensure((size_t)n_total * b.maxrow), "alloc");
-  // two-float kicks split the rows when no far pair can come inside
-  // kFarCheck before the next rebuild (pairs approach by at most the skin)
-  b.split = ff && !prm->ff_all && prm->skin <= kFarSplitBatch - kFarCheck + 1e-12;
+  // two-float kicks split the rows; far pairs that come inside kFarCheck
+  // before the next rebuild go through the close queue
+  b.split = ff && !prm->ff_all;
   if (b.split) {
     B_CUDA(ctx, b.rows2.ensure((size_t)n_total * b.maxrow), "alloc");
     B_CUDA(ctx, b.cnt2.ensure((size_t)n_total), "alloc");
+    B_CUDA(ctx, b.closef.ensure(3), "alloc");
+    B_CUDA(ctx, b.closeq.ensure((size_t)n_total), "alloc");
+    B_CUDA(ctx, cudaMemsetAsync(b.closef.ptr, 0, 3 * sizeof(int32_t), s), "memset");
   }
   B_CUDA(ctx, b.qfix.ensure((size_t)n_total), "alloc");
   B_CUDA(ctx, b.qref.ensure((size_t)n_total), "alloc");
@@ -408,12 +414,13 @@ extern "C" int lj_batch_run(lj_ctx* ctx, double* q, double* p, int32_t n_total,
       for (const auto& sh : shapes) {
         cudaError_t e = launch_force_batch(tp, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                            b.classrows.ptr + k.first, k.count, prm->dt, cl2,
-                                           sh[0], sh[1], sh[2] != 0, ff, s, fp);
+                                           sh[0], sh[1], sh[2] != 0, ff, s, fp, b.closef.ptr,
+                                           b.closeq.ptr);
         cudaEventRecord(e0, s);
         for (int rep = 0; rep < 3 && e == cudaSuccess; rep++)
           e = launch_force_batch(tp, c, b.qfix.ptr, b.rid.ptr, b.reps.ptr,
                                  b.classrows.ptr + k.first, k.count, prm->dt, cl2, sh[0], sh[1],
-                                 sh[2] != 0, ff, s, fp);
+                                 sh[2] != 0, ff, s, fp, b.closef.ptr, b.closeq.ptr);
         cudaEventRecord(e1, s);
         if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
           cudaEventDestroy(e0);

@@ -169,14 +169,11 @@ constexpr double kCoarseQuantumErr = 2.0;
 // two-float arithmetic wherever it sits in its row.  FP32 terms for every
 // pair beyond 2.0 sigma keep the net force of each particle within 2.2e-6
 // (108,000 particles, rho 0.5), 1.1e-6 (1M, rho 1, over 1,000 MD steps) and
-// 2.4e-6 (8M, rho 1) of FP64, against a bar of 1e-5.  Single systems split
-// at 2.1 sigma: the few rows whose far pairs come inside 2.0 sigma before
-// the next rebuild are queued and their close terms added by a second pass
-// (k_seg_close_terms).  The batch kernel has no such pass, so its split
-// keeps a margin of a whole Verlet skin (0.3 sigma): no far pair can come
-// inside 2.0 sigma before the rebuild that positions moving that far force.
+// 2.4e-6 (8M, rho 1) of FP64, against a bar of 1e-5.  Rows split at 2.1
+// sigma: the few rows whose far pairs come inside 2.0 sigma before the next
+// rebuild are queued and their close terms added by a second pass
+// (k_seg_close_terms, k_batch_close_terms).
 constexpr double kFarSplit = 2.1;
-constexpr double kFarSplitBatch = 2.3;
 constexpr double kFarCheck = 2.0;
 
 // ---------------------------------------------------------------------------

@@ -39,8 +39,11 @@ cudaError_t launch_force_tiled(const ForceLaunch& L, const TiledList& T, const i
 cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* qfix,
                                const int32_t* rid, const ReplicaInfo* reps,
                                const int32_t* rows, int nrows, double dt, double cl2, int lanes,
-                               int unroll, bool vec, bool ff, cudaStream_t s, const Csr* far) {
-  if (far && (!ff || (vec && (far->ptr || far->stride % 4 != 0)))) return cudaErrorInvalidValue;
+                               int unroll, bool vec, bool ff, cudaStream_t s, const Csr* far,
+                               int32_t* close_flag, int32_t* close_rows) {
+  if (far && (!ff || !close_flag || !close_rows ||
+              (vec && (far->ptr || far->stride % 4 != 0))))
+    return cudaErrorInvalidValue;
   if (vec && (unroll != 4 || c.ptr || c.stride % 4 != 0)) return cudaErrorInvalidValue;
   if (nrows <= 0) return cudaSuccess;
   long long cl2_bits;
@@ -56,10 +59,17 @@ cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* 
         if (far) {  // split rows: far part in FP32 terms, near part in two-float terms
           if (U == 4 && vec)
             k_gather_mixed_batch_seg<G, 4, true><<<blocks, block, 0, s>>>(
-                part, c, *far, qfix, rid, reps, rows, nrows, dt, cl2_bits);
+                part, c, *far, qfix, rid, reps, rows, nrows, dt, cl2_bits, close_flag,
+                close_rows);
           else
             k_gather_mixed_batch_seg<G, U, false><<<blocks, block, 0, s>>>(
-                part, c, *far, qfix, rid, reps, rows, nrows, dt, cl2_bits);
+                part, c, *far, qfix, rid, reps, rows, nrows, dt, cl2_bits, close_flag,
+                close_rows);
+          // queued rows with far entries inside kFarCheck, a warp per row (a
+          // no-op unless the flag is up)
+          const int cb = (int)std::min<long long>(((long long)nrows * 32 + 255) / 256, 152 * 4);
+          k_batch_close_terms<32><<<cb, 256, 0, s>>>(part, *far, qfix, rid, reps, dt, cl2_bits,
+                                                     close_flag, close_rows);
           return;
         }
         if (U == 4 && vec)

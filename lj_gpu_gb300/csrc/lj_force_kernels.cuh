@@ -967,6 +967,28 @@ __device__ __forceinline__ void walk_row(const Csr& C, int i, bool valid, int la
   }
 }
 
+// Close queue of the segment gathers: the first lane of each row group with
+// a far entry inside kFarCheck (`missed` on any lane of the group) puts row
+// i onto close_rows, one slot per row (warp-aggregated on the length
+// close_flag[2]), and raises close_flag[0].  Called by whole warps.
+template <int G>
+__device__ __forceinline__ void queue_close_row(bool missed, int i, int32_t* close_flag,
+                                                int32_t* close_rows) {
+  const unsigned mb = __ballot_sync(kFullMask, missed);
+  if (!mb) return;
+  const int wl = threadIdx.x & 31;
+  const unsigned gmask = G == 32 ? kFullMask : ((1u << G) - 1u);
+  const bool lead = (wl & (G - 1)) == 0 && ((mb >> wl) & gmask) != 0u;
+  const unsigned lm = __ballot_sync(kFullMask, lead);
+  int slot = 0;
+  if (wl == 0) {
+    slot = atomicAdd(close_flag + 2, __popc(lm));
+    atomicExch(close_flag, 1);
+  }
+  slot = __shfl_sync(kFullMask, slot, 0) + __popc(lm & ((1u << wl) - 1u));
+  if (lead) close_rows[slot] = i;
+}
+
 // Segment gather (LJ_PREC_MIXED over rows in two parts): C holds every row's
 // near part, F its far part (k_partition_near's order, or the split rows of
 // the MD build).  The far part runs first in FP32 terms from the coarse image
@@ -1063,22 +1085,7 @@ __global__ void __launch_bounds__(256, 3) k_gather_mixed_seg(const Particles P, 
   // k_seg_close_terms (its own kernel, so that its registers do not add to
   // this one's); the first lane of each row group with such an entry queues
   // the row, one slot per row (the queue holds n rows)
-  {
-    const unsigned mb = __ballot_sync(kFullMask, missed);
-    if (mb) {
-      const int wl = threadIdx.x & 31;
-      const unsigned gmask = G == 32 ? kFullMask : ((1u << G) - 1u);
-      const bool lead = (wl & (G - 1)) == 0 && ((mb >> wl) & gmask) != 0u;
-      const unsigned lm = __ballot_sync(kFullMask, lead);
-      int slot = 0;
-      if (wl == 0) {
-        slot = atomicAdd(close_flag + 2, __popc(lm));
-        atomicExch(close_flag, 1);
-      }
-      slot = __shfl_sync(kFullMask, slot, 0) + __popc(lm & ((1u << wl) - 1u));
-      if (lead) close_rows[slot] = i;
-    }
-  }
+  queue_close_row<G>(missed, i, close_flag, close_rows);
   // ---- near part: two-float terms
   walk_row<G, U, VEC>(C, i, valid, lane, qfix, [&](const int4 (&xj)[U], const int* jj,
                                                     const bool (&ok)[U]) {
@@ -1298,15 +1305,15 @@ __global__ void __launch_bounds__(256) k_gather_mixed_batch(
 // Batched segment gather over the split rows of the replica batch: as
 // k_gather_mixed_seg, with the row's replica constants, over the rows of one
 // size class.  The far part (F) runs first in FP32 terms, whose compensated
-// sums seed the two-float sums of the near part (C).  The batch splits its
-// rows only when the skin is at most kFarSplitBatch - kFarCheck: a rebuild comes
-// before any particle moves more than skin / 2, so no far pair comes inside
-// kFarCheck before the next rebuild and every far entry takes its FP32 term.
+// sums seed the two-float sums of the near part (C).  A far entry closer
+// than the replica's kFarCheck is skipped there and its row queued (once)
+// for k_batch_close_terms, as in the single-system segment gather.
 template <int G, int U, bool VEC>
 __global__ void __launch_bounds__(256, 3) k_gather_mixed_batch_seg(
     const Particles P, const Csr C, const Csr F, const int4* __restrict__ qfix,
     const int32_t* __restrict__ rid, const ReplicaInfo* __restrict__ reps,
-    const int32_t* __restrict__ rows, int nrows, double dt, long long cl2_bits) {
+    const int32_t* __restrict__ rows, int nrows, double dt, long long cl2_bits,
+    int32_t* close_flag, int32_t* __restrict__ close_rows) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int g = t / G;
   const int lane = t & (G - 1);
@@ -1325,6 +1332,7 @@ __global__ void __launch_bounds__(256, 3) k_gather_mixed_batch_seg(
     K.cl2_hi = R.cl2f_hi;
     K.cl2s_lo = R.cl2u_lo;  // FP32 terms
     K.cl2s_hi = R.cl2u_hi;
+    K.near2 = R.nearc2u;
   }
   int li[3];
   image_lo(xi.w, li[0], li[1], li[2]);
@@ -1341,6 +1349,7 @@ __global__ void __launch_bounds__(256, 3) k_gather_mixed_batch_seg(
     return !beyond_cutoff(r2_fp64(d64), cl2_bits);
   };
   // ---- far part: FP32 terms
+  bool missed = false;
   RowSums<true> acc;
   {
     RowSums<false> acc32;
@@ -1355,8 +1364,10 @@ __global__ void __launch_bounds__(256, 3) k_gather_mixed_batch_seg(
       for (int u = 0; u < U; u++) {
         d[u] = sep_mixed<false>(xi, xj[u], K);
         r2[u] = fmaf(d[u].z, d[u].z, fmaf(d[u].y, d[u].y, d[u].x * d[u].x));
-        const bool in = ok[u] && r2[u] <= K.cl2s_lo;
-        if (ok[u] && r2[u] > K.cl2s_lo && r2[u] <= K.cl2s_hi) border |= 1u << u;
+        const bool use = ok[u] && !(r2[u] < K.near2);  // closer ones: the close pass
+        if (ok[u] && r2[u] < K.near2) missed = true;
+        const bool in = use && r2[u] <= K.cl2s_lo;
+        if (use && r2[u] > K.cl2s_lo && r2[u] <= K.cl2s_hi) border |= 1u << u;
         float df = df_mixed<false>(r2[u], K);
         df = in ? df : 0.0f;
         sx = fmaf(df, d[u].x, sx);
@@ -1388,6 +1399,7 @@ __global__ void __launch_bounds__(256, 3) k_gather_mixed_batch_seg(
     acc.z.hi = __fmul_rn(h[4], r24);
     acc.z.lo = __fmul_rn(h[5], r24);
   }
+  queue_close_row<G>(missed, i, close_flag, close_rows);
   // ---- near part: two-float terms
   walk_row<G, U, VEC>(C, i, valid, lane, qfix, [&](const int4 (&xj)[U], const int* jj,
                                                    const bool (&ok)[U]) {
@@ -1410,6 +1422,75 @@ __global__ void __launch_bounds__(256, 3) k_gather_mixed_batch_seg(
   const double kf = valid ? reps[r].unit * dt * 24.0 : 0.0;
   const double fs[3] = {kf, kf, kf};
   kick_group<false, G, true>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, fs, 0);
+}
+
+// The close pass of the replica batch: as k_seg_close_terms over the rows
+// k_gather_mixed_batch_seg queued, a warp per row, with the row's replica
+// constants (two-float cutoff band, pair-unit scale, FP64 box, kick scale).
+template <int G>
+__global__ void __launch_bounds__(256) k_batch_close_terms(
+    const Particles P, const Csr F, const int4* __restrict__ qfix,
+    const int32_t* __restrict__ rid, const ReplicaInfo* __restrict__ reps, double dt,
+    long long cl2_bits, int32_t* flag, const int32_t* __restrict__ queue) {
+  if (*(volatile int32_t*)flag == 0) return;
+  const int lane = threadIdx.x & (G - 1);
+  const int groups = (gridDim.x * blockDim.x) / G;
+  const int queued = min(*(volatile int32_t*)(flag + 2), F.n);
+  const int nr = (queued + groups - 1) / groups * groups;  // whole warps take every pass
+  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) / G; t < nr; t += groups) {
+    const bool valid = t < queued;
+    const int i = valid ? __ldg(queue + t) : 0;
+    const int r = valid ? __ldg(rid + i) : 0;
+    const ReplicaInfo& R = reps[r];
+    MixedConsts K{};
+    K.k_hi = R.k_hi;
+    K.k_lo = R.k_lo;
+    K.cl2_lo = R.cl2f_lo;
+    K.cl2_hi = R.cl2f_hi;
+    const float near2 = R.nearc2u;
+    const int4 xi = valid ? __ldg(qfix + i) : make_int4(0, 0, 0, 0);
+    int li[3];
+    image_lo(xi.w, li[0], li[1], li[2]);
+    RowSums<true> acc;
+    acc.init();
+    walk_row<G, 1, false>(F, i, valid, lane, qfix, [&](const int4* xj, const int* jj,
+                                                       const bool* ok) {
+      const float3 d = sep_mixed<false>(xi, xj[0], K);
+      const bool close = ok[0] && fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x)) < near2;
+      unsigned border = 0u;
+      pair_term_ff<false>(xi, li, xj[0], K, acc, 0, close, border, 0);
+      if (border) {
+        Fp64Consts f64{};
+        f64.cl2_bits = cl2_bits;
+        for (int a = 0; a < 3; a++) {
+          f64.len[a] = R.len[a];
+          f64.half_bits[a] = R.half_bits[a];
+        }
+        const double3 d64 = sep_fp64<true>(load_q<false>(P, i), load_q<false>(P, jj[0]), f64);
+        if (!beyond_cutoff(r2_fp64(d64), cl2_bits))
+          pair_term_ff<false>(xi, li, xj[0], K, acc, 1, true, border, 0);
+      }
+    });
+    float hx, lx, hy, ly, hz, lz;
+    acc.get(hx, lx, hy, ly, hz, lz);
+    if (G > 1) {
+      group_reduce_comp<G>(hx, lx);
+      group_reduce_comp<G>(hy, ly);
+      group_reduce_comp<G>(hz, lz);
+    }
+    const double kf = valid ? R.unit * dt * 24.0 : 0.0;
+    const double fs[3] = {kf, kf, kf};
+    kick_group<false, G, true>(P, i, lane, valid, hx, lx, hy, ly, hz, lz, fs, 0);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(flag + 1, 1) == (int)gridDim.x - 1) {
+      flag[0] = 0;
+      flag[1] = 0;
+      flag[2] = 0;
+    }
+  }
 }
 
 // Cell-tiled mixed gather (kernel 3).  One CTA per cell: it copies the

@@ -82,6 +82,7 @@ struct ReplicaInfo {
   float cl2f_lo, cl2f_hi;   // the same, -/+ the band of two-float pair terms
   float sl2u_lo, sl2u_hi;   // list radius^2 in fixed units^2, -/+ the FP32 band
   float near2u;             // split rows: near part below this r2 at the build (fixed units^2)
+  float nearc2u;            // far entries closer than this (kFarCheck) take two-float terms
   double unit;              // length per fixed unit (FP64)
   double inv_w[3];          // cells per unit length
   int nc[3];
@@ -170,12 +171,16 @@ cudaError_t launch_force_tiled(const ForceLaunch& L, const TiledList& T, const i
 
 // Batched mixed gather over the rows `rows[0..nrows)` (one size class) of a
 // replica batch; padded rows (C.ptr == nullptr).  `far` (two-float terms
-// only): rows split into the near part c and the far part *far.
+// only): rows split into the near part c and the far part *far, with the
+// close queue (close_flag: three device words, zero between launches;
+// close_rows: a slot per particle) for far entries that came inside
+// kFarCheck, whose terms a second pass adds before the call returns.
 cudaError_t launch_force_batch(const Particles& part, const Csr& c, const int4* qfix,
                                const int32_t* rid, const ReplicaInfo* reps,
                                const int32_t* rows, int nrows, double dt, double cl2, int lanes,
                                int unroll, bool vec, bool ff, cudaStream_t s,
-                               const Csr* far = nullptr);
+                               const Csr* far = nullptr, int32_t* close_flag = nullptr,
+                               int32_t* close_rows = nullptr);
 
 // Launchers (return cudaError_t of the launch)
 cudaError_t launch_fixed_image(const ForceLaunch& L, cudaStream_t s);
