@@ -333,13 +333,19 @@ typedef struct lj_md_stats {
   int32_t loop_graph;     /* 1: the steps between records ran as one launch of a
                              persistent graph (a WHILE node counted down on the
                              device); 0: as back-to-back chunk graphs */
-  int32_t reserved;
+  int32_t initial_build;  /* 1: the run started with a list build; 0: it kept
+                             the list of the context's previous run */
 } lj_md_stats;
 
 /* q, p: AoS device arrays (modified in place; p must hold the initial
  * momenta, e.g. from lj_init_momenta).  records may be NULL.  Positions are
  * wrapped into [0, L).  LJ_ERR_LIST_OVERFLOW if a rebuild would exceed the
- * list capacity (q, p are then partially advanced). */
+ * list capacity (q, p are then partially advanced).  The context keeps the
+ * neighbour list of a completed run: the next run with the same n, box, rc,
+ * skin, precision and ff_all uses it unless a particle lies more than skin/2
+ * from its position at that list's build (the Verlet criterion, checked on
+ * the positions passed in), so runs that continue a trajectory skip the
+ * initial build (stats->initial_build). */
 int lj_md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_params* params,
               int32_t nsteps, lj_md_record* records, int32_t max_records, int32_t* n_records,
               lj_md_stats* stats);

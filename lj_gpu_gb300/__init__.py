@@ -103,7 +103,7 @@ class MdRecord(C.Structure):
 class MdStats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("rebuilds", C.c_int64), ("ms_total", C.c_double),
                 ("list_capacity", C.c_int64), ("launches", C.c_int64),
-                ("loop_graph", C.c_int32), ("reserved", C.c_int32)]
+                ("loop_graph", C.c_int32), ("initial_build", C.c_int32)]
 
 
 def make_md_params(dt, rc, skin, box, precision="mixed", record_every=0, graph_steps=0,
@@ -403,7 +403,7 @@ class Context:
         return ([(recs[k].step, recs[k].kinetic, recs[k].potential) for k in range(nrec.value)],
                 {"steps": st.steps, "rebuilds": st.rebuilds, "ms_total": st.ms_total,
                  "list_capacity": st.list_capacity, "launches": st.launches,
-                 "loop_graph": st.loop_graph})
+                 "loop_graph": st.loop_graph, "initial_build": st.initial_build})
 
     def md_run_host(self, q, p, params: MdParams, nsteps, max_records=64):
         """lj_md_run_host: velocity Verlet over host AoS (n, 4) float64 arrays
@@ -429,7 +429,7 @@ class Context:
         return ([(recs[k].step, recs[k].kinetic, recs[k].potential) for k in range(nrec.value)],
                 {"steps": st.steps, "rebuilds": st.rebuilds, "ms_total": st.ms_total,
                  "list_capacity": st.list_capacity, "launches": st.launches,
-                 "loop_graph": st.loop_graph})
+                 "loop_graph": st.loop_graph, "initial_build": st.initial_build})
 
     def batch_run(self, q, p, offsets, boxes, params: MdParams, nsteps, max_records=16):
         """Replica batch (see lj_batch_run).  offsets: n_replicas + 1 ints, boxes:

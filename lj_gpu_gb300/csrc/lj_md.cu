@@ -80,6 +80,20 @@ __global__ void __launch_bounds__(256) k_md_drift(double* __restrict__ q,
   if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) > half_skin2) flags[F_REBUILD] = 1;
 }
 
+// Raises the rebuild flag when a particle of the image qfix lies more than
+// skin/2 from its position at the last build (the drift's check, for the
+// positions a run starts from).
+__global__ void k_md_moved(const int4* __restrict__ qfix, const int4* __restrict__ qref, int n,
+                           float ux, float uy, float uz, float half_skin2,
+                           int32_t* __restrict__ flags) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int4 x = qfix[i], r = qref[i];
+    const float dx = (float)wrap_sub(x.x, r.x) * ux, dy = (float)wrap_sub(x.y, r.y) * uy,
+                dz = (float)wrap_sub(x.z, r.z) * uz;
+    if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) > half_skin2) flags[F_REBUILD] = 1;
+  }
+}
+
 __global__ void k_md_copy_ref(const int4* __restrict__ qfix, int4* __restrict__ qref, int n,
                               const int32_t* __restrict__ flags) {
   if (!flags[F_REBUILD]) return;
@@ -186,6 +200,13 @@ struct MdState {
   // cnt2 the far part (launch_build_rows_split)
   DevBuf<int32_t> rows2, cnt2;
   DevBuf<int32_t> closeq;  // rows with far entries inside 2.0 sigma (k_gather_mixed_seg)
+  // The list of the last completed run, kept for the next: it holds while
+  // every particle stays within skin/2 of its position at that build (qref,
+  // checked when the next run starts) and the particle count, box, cutoff,
+  // skin and list kind (list_key) and the list's buffers are unchanged.
+  bool list_kept = false;
+  double list_key[7] = {};
+  const void* list_bufs[6] = {};
   int64_t cap2 = 0;
   bool split = false;
   DevBuf<int64_t> start, off;
@@ -343,6 +364,12 @@ static int md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_para
     return lj_fail(ctx, LJ_ERR_CUDA, "set device");
   if (!ctx->md) ctx->md.reset(new MdState());
   MdState& m = *ctx->md;
+  // the previous run's list, if this run has its particle count, box,
+  // cutoff, skin and list kind (its buffers are compared after sizing)
+  const double key[7] = {(double)n, prm->box[0], prm->box[1], prm->box[2], prm->rc,
+                         prm->skin, (double)(prm->precision * 2 + (prm->ff_all ? 1 : 0))};
+  bool reuse = m.list_kept && std::memcmp(key, m.list_key, sizeof key) == 0;
+  m.list_kept = false;  // until this run completes
   cudaStream_t s = ctx->stream;
   if (!s) {
     // graphs cannot be captured on the legacy stream: run on our own stream,
@@ -408,6 +435,10 @@ static int md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_para
   const int64_t half_cap = std::min<int64_t>(m.cap, 0x7fffffffll);
   if (!mixed) MD_CUDA(ctx, m.list.ensure((size_t)half_cap), "alloc");
   MD_CUDA(ctx, m.energy.ensure(2), "alloc");
+  // a kept list needs the buffers it was built into
+  const void* bufs[6] = {m.rows.ptr, m.cnt.ptr, m.rows2.ptr, m.cnt2.ptr, m.order2.ptr,
+                         m.list.ptr};
+  reuse = reuse && std::memcmp(bufs, m.list_bufs, sizeof bufs) == 0;
   MD_CUDA(ctx, cudaMemsetAsync(m.flags.ptr, 0, sizeof(int32_t) * F_WORDS, s), "memset");
 
   ForceLaunch K{};
@@ -509,7 +540,12 @@ static int md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_para
     MD_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
     cudaError_t ce = launch_fixed_image(K, s);
     if (ce == cudaSuccess) {
-      k_md_set<<<1, 32, 0, s>>>(m.flags.ptr, F_REBUILD, 1);
+      if (reuse)  // rebuild only if a particle moved beyond skin/2 since that build
+        k_md_moved<<<std::min(grid1(n, 256), 152 * 8), 256, 0, s>>>(
+            m.qfix.ptr, m.qref.ptr, n, D.unit[0], D.unit[1], D.unit[2], D.half_skin2,
+            m.flags.ptr);
+      else
+        k_md_set<<<1, 32, 0, s>>>(m.flags.ptr, F_REBUILD, 1);
       ce = md_rebuild(m, !mixed, K, s);
     }
     cudaError_t ee = cudaStreamEndCapture(s, &g);
@@ -569,6 +605,7 @@ static int md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_para
   int rc;
   if (io) MD_CUDA(ctx, cudaStreamWaitEvent(s, io->ev_p, 0), "wait");  // p's first use follows
   if ((rc = read_flags(f))) return rc;
+  const int32_t initial_build = f[F_COUNT];  // 0: the previous run's list holds
   if (f[F_OVERFLOW])
     return lj_fail(ctx, LJ_ERR_LIST_OVERFLOW, "a neighbour row exceeds %d entries", m.maxrow);
   if ((rc = record(0))) return rc;
@@ -655,14 +692,18 @@ static int md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_para
   cudaEventElapsedTime(&ms, t0, t1);
   if (stats) {
     stats->steps = nsteps;
-    stats->rebuilds = f[F_COUNT] - 1;  // the initial build goes through the same finish
+    stats->rebuilds = f[F_COUNT] - initial_build;  // the initial build counts there too
     stats->ms_total = ms;
     stats->list_capacity = m.cap;
     stats->launches = step_kernels < 0 ? -1 : launches + kicks + nsteps * step_kernels;
     stats->loop_graph = m.loop.exec ? 1 : 0;
+    stats->initial_build = initial_build;
   }
   if (n_records) *n_records = nrec;
   if (!ctx->stream) MD_CUDA(ctx, cudaStreamSynchronize(s), "sync");
+  std::memcpy(m.list_key, key, sizeof key);
+  std::memcpy(m.list_bufs, bufs, sizeof bufs);
+  m.list_kept = true;
   return LJ_OK;
 }
 

@@ -127,6 +127,48 @@ def test_md_run_host_matches_the_device_run(engine, precision):
         assert e.value.status == engine.LJ_ERR_LIST_OVERFLOW
 
 
+def test_runs_that_continue_a_trajectory_keep_the_list(engine):
+    """A context keeps the neighbour list of its last completed run: a run
+    that continues the trajectory (same n, box, rc, skin, list kind, and no
+    particle beyond skin/2 from its position at that list's build) starts
+    without a build and still follows the oracle's FP64 velocity Verlet.  A
+    particle moved past skin/2, another skin or another precision forces
+    the build."""
+    import torch
+    q, L = ol.init_fcc_periodic(6, 1.0, 0.05, seed=41)  # 864 particles
+    p = engine.init_momenta(q.shape[0], 1.0, seed=6)
+    rc, skin, dt = 2.5, 0.3, 0.005
+    prm = engine.make_md_params(dt, rc, skin, L, precision="mixed", graph_steps=8)
+    qd, pd = _dev(q), _dev(p)
+    with engine.Context(0) as ctx:
+        _, a = ctx.md_run(qd, pd, prm, 30, max_records=0)
+        _, b = ctx.md_run(qd, pd, prm, 30, max_records=0)
+        assert a["initial_build"] == 1 and b["initial_build"] == 0, (a, b)
+        torch.cuda.synchronize()
+        qo, po = oracle_vv(q, p, L, rc, dt, 60)
+        assert np.abs(periodic_diff(qd.cpu().numpy(), qo, L)).max() < 1e-7
+        assert ol.rel_errors(pd.cpu().numpy(), po)["max_rel_rms"] < 1e-6
+        # the host entry keeps it as well
+        hq, hp = qd.cpu().numpy().copy(), pd.cpu().numpy().copy()
+        _, c = ctx.md_run_host(hq, hp, prm, 5, max_records=0)
+        _, c2 = ctx.md_run_host(hq, hp, prm, 5, max_records=0)
+        assert c2["initial_build"] == 0
+        # one particle moved past skin/2 since the last build (it lies within
+        # skin/2 = 0.15 of its position there, so 0.35 more is past it)
+        hq[7, 0] = (hq[7, 0] + 0.35) % L
+        _, d = ctx.md_run_host(hq, hp, prm, 1, max_records=0)
+        assert d["initial_build"] == 1
+        # another skin, another precision
+        _, e = ctx.md_run_host(hq, hp, engine.make_md_params(dt, rc, 0.35, L), 1, max_records=0)
+        assert e["initial_build"] == 1
+        _, g = ctx.md_run_host(hq, hp, engine.make_md_params(dt, rc, 0.35, L, precision="fp64"),
+                               1, max_records=0)
+        assert g["initial_build"] == 1
+        _, h = ctx.md_run_host(hq, hp, engine.make_md_params(dt, rc, 0.35, L, precision="fp64"),
+                               1, max_records=0)
+        assert h["initial_build"] == 0
+
+
 def test_md_list_overflow_is_reported(engine):
     # 500 particles packed into a corner of a large box: the capacity estimate
     # from the mean density is far too small (64 entries for ~150 partners
