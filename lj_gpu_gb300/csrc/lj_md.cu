@@ -207,6 +207,10 @@ struct MdState {
   bool list_kept = false;
   double list_key[7] = {};
   const void* list_bufs[6] = {};
+  // the bytes of every argument the step graph was captured with (launch
+  // structs, buffer pointers, sizes): equal bytes relaunch it as it is
+  std::vector<unsigned char> graph_sig;
+  int64_t graph_step_kernels = -1;
   int64_t cap2 = 0;
   bool split = false;
   DevBuf<int64_t> start, off;
@@ -613,37 +617,64 @@ static int md_run(lj_ctx* ctx, double* q, double* p, int32_t n, const lj_md_para
   // ---- the persistent loop over chunks of `graph_steps` plain steps --------
   const int gsteps = prm->graph_steps > 0 ? prm->graph_steps : 20;
   int64_t step_kernels = -1;  // kernels of one step (from the captured graph)
-  if (m.graph) {
-    cudaGraphExecDestroy(m.graph);
-    m.graph = nullptr;
-  }
-  m.loop.reset();
-  if (gsteps > 1 && !prm->chunk_graphs &&
-      m.loop.build(s, m.flags.ptr + F_LOOP, m.flags.ptr + F_OVERFLOW,
-                   [&](cudaStream_t cs) {
-                     cudaError_t ce = cudaSuccess;
-                     for (int k = 0; k < gsteps && ce == cudaSuccess; k++)
-                       ce = md_step(m, D, Kfull, cs);
-                     return ce;
-                   }) == cudaSuccess) {
-    step_kernels = m.loop.kernels_per_chunk / gsteps;
-    m.graph_steps = gsteps;
-  } else if (gsteps > 1) {  // no conditional node: chunk graphs launched back to back
-    cudaGraph_t g = nullptr;
-    MD_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
-    cudaError_t ce = cudaSuccess;
-    for (int k = 0; k < gsteps && ce == cudaSuccess; k++) ce = md_step(m, D, Kfull, s);
-    cudaError_t ee = cudaStreamEndCapture(s, &g);
-    if (ce != cudaSuccess || ee != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      return lj_fail(ctx, LJ_ERR_CUDA, "graph capture: %s",
-                     cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+  std::vector<unsigned char> sig;
+  auto put = [&](const void* v, size_t bytes) {
+    const auto* c = static_cast<const unsigned char*>(v);
+    sig.insert(sig.end(), c, c + bytes);
+  };
+  put(&Kfull, sizeof Kfull);
+  put(&D, sizeof D);
+  put(&m.build, sizeof m.build);
+  put(&m.grid, sizeof m.grid);
+  const void* used[] = {m.qfix.ptr,  m.qref.ptr,  m.cq.ptr,    m.cq2.ptr,   m.flags.ptr,
+                        m.cell.ptr,  m.count.ptr, m.cursor.ptr, m.order.ptr, m.order2.ptr,
+                        m.cnt.ptr,   m.ptr.ptr,   m.rows.ptr,  m.list.ptr,  m.rows2.ptr,
+                        m.cnt2.ptr,  m.closeq.ptr, m.start.ptr, m.off.ptr,  m.scan_tmp.ptr};
+  put(used, sizeof used);
+  const int64_t sizes[] = {(int64_t)m.scan_tmp.cap, m.maxrow, m.maxrow_far, m.cap, m.cap2,
+                           m.n, gsteps, prm->chunk_graphs};
+  put(sizes, sizeof sizes);
+  const bool cached = gsteps > 1 && (m.loop.exec || m.graph) && sig == m.graph_sig;
+  if (cached) {
+    step_kernels = m.graph_step_kernels;
+  } else {
+    m.graph_sig.clear();
+    if (m.graph) {
+      cudaGraphExecDestroy(m.graph);
+      m.graph = nullptr;
     }
-    step_kernels = graph_kernels(g) / gsteps;
-    ce = cudaGraphInstantiate(&m.graph, g, 0);
-    cudaGraphDestroy(g);
-    if (ce != cudaSuccess) return lj_fail(ctx, LJ_ERR_CUDA, "graph instantiate");
-    m.graph_steps = gsteps;
+    m.loop.reset();
+    if (gsteps > 1 && !prm->chunk_graphs &&
+        m.loop.build(s, m.flags.ptr + F_LOOP, m.flags.ptr + F_OVERFLOW,
+                     [&](cudaStream_t cs) {
+                       cudaError_t ce = cudaSuccess;
+                       for (int k = 0; k < gsteps && ce == cudaSuccess; k++)
+                         ce = md_step(m, D, Kfull, cs);
+                       return ce;
+                     }) == cudaSuccess) {
+      step_kernels = m.loop.kernels_per_chunk / gsteps;
+      m.graph_steps = gsteps;
+    } else if (gsteps > 1) {  // no conditional node: chunk graphs launched back to back
+      cudaGraph_t g = nullptr;
+      MD_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
+      cudaError_t ce = cudaSuccess;
+      for (int k = 0; k < gsteps && ce == cudaSuccess; k++) ce = md_step(m, D, Kfull, s);
+      cudaError_t ee = cudaStreamEndCapture(s, &g);
+      if (ce != cudaSuccess || ee != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return lj_fail(ctx, LJ_ERR_CUDA, "graph capture: %s",
+                       cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+      }
+      step_kernels = graph_kernels(g) / gsteps;
+      ce = cudaGraphInstantiate(&m.graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return lj_fail(ctx, LJ_ERR_CUDA, "graph instantiate");
+      m.graph_steps = gsteps;
+    }
+    if (m.loop.exec || m.graph) {
+      m.graph_sig = sig;
+      m.graph_step_kernels = step_kernels;
+    }
   }
 
   // ---- integrate -------------------------------------------------------------
