@@ -51,6 +51,13 @@ def test_argument_checks_need_no_gpu(engine):
     assert L.lj_force_pairs_fp64_aos(None, None, 0, 0.001, 9.0, None, None, -5, None,
                                      None) == engine.LJ_ERR_INVALID_ARGUMENT
     assert L.lj_ctx_create(None, 0) == engine.LJ_ERR_INVALID_ARGUMENT
+    # entries that take a context reject a missing one before any CUDA call
+    prm = engine.make_md_params(0.005, 2.5, 0.3, 10.0)
+    assert L.lj_md_run_host(None, q.ctypes.data, q.ctypes.data, 4, prm, 1, None, 0, None,
+                            None) == engine.LJ_ERR_INVALID_ARGUMENT
+    assert L.lj_md_run(None, q.ctypes.data, q.ctypes.data, 4, prm, 1, None, 0, None,
+                       None) == engine.LJ_ERR_INVALID_ARGUMENT
+    assert L.lj_ctx_set_l2_window(None, 0.5) == engine.LJ_ERR_INVALID_ARGUMENT
 
 
 @pytest.mark.skipif(HAS_GPU, reason="checks the no-device path")
