@@ -123,8 +123,8 @@ int lj_ctx_set_timing(lj_ctx* ctx, int32_t on);
 /* ms[0]: position-image passes, ms[1]: pair kernels, ms[2]: both, summed
  * over *calls force calls since the last reset (synchronises). */
 int lj_ctx_get_timing(lj_ctx* ctx, double* ms, int64_t* calls);
-/* L2 persistence for the randomly gathered j positions (the benchmark spec's
- * "L2 persistence windows"): with hit_ratio in (0, 1], the pair kernel of
+/* L2 persistence for the randomly gathered j positions: with hit_ratio in
+ * (0, 1], the pair kernel of
  * every later mixed force call on ctx runs with an access-policy window over
  * the fixed-point position image (persisting hits for that fraction of it,
  * streaming misses), and the context reserves that many bytes of L2 as
