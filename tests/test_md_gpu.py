@@ -167,6 +167,17 @@ def test_runs_that_continue_a_trajectory_keep_the_list(engine):
         _, h = ctx.md_run_host(hq, hp, engine.make_md_params(dt, rc, 0.35, L, precision="fp64"),
                                1, max_records=0)
         assert h["initial_build"] == 0
+    # FP64 (compacted half list): a continued run on the kept list follows the
+    # oracle to the FP64 path's own bar
+    prm64 = engine.make_md_params(dt, rc, skin, L, precision="fp64", graph_steps=8)
+    qd, pd = _dev(q), _dev(p)
+    with engine.Context(0) as ctx:
+        _, a = ctx.md_run(qd, pd, prm64, 30, max_records=0)
+        _, b = ctx.md_run(qd, pd, prm64, 30, max_records=0)
+    assert a["initial_build"] == 1 and b["initial_build"] == 0
+    torch.cuda.synchronize()
+    assert np.abs(periodic_diff(qd.cpu().numpy(), qo, L)).max() < 1e-11
+    assert ol.rel_errors(pd.cpu().numpy(), po)["max_rel_rms"] < 1e-10
 
 
 def test_md_list_overflow_is_reported(engine):
